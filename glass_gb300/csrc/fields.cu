@@ -1,0 +1,346 @@
+// Field-generation kernels before the transform: iternorm, Philox normals,
+// correlated alm assembly, multalm and almxfl.
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include <vector>
+
+#include "glg_internal.cuh"
+
+namespace {
+
+// ---------------------------------------------------------------- iternorm
+
+// One warp per angular mode l (glass/fields.py:101-188).  The matrix m
+// (k x k, double buffered), a and atm live in shared memory.  Every sum
+// runs in the same fixed order, with explicit fma, as orc_iternorm in the
+// CPU oracle, so both give identical bits.
+__global__ void __launch_bounds__(32)
+k_iternorm(const double *__restrict__ cov, const int64_t nrows, const int64_t nl, const int k,
+           double *__restrict__ w, int64_t *__restrict__ bad) {
+    extern __shared__ double sm[];
+    const int64_t l = blockIdx.x;
+    const int lane = threadIdx.x;
+    const int kp = k + 1;
+    const int kk = k > 0 ? k * k : 1;
+    double *m = sm;
+    double *mn = sm + kk;
+    double *a = mn + kk;
+    double *atm = a + (k > 0 ? k : 1);
+    for (int t = lane; t < kk; t += 32) m[t] = 0.0;
+    for (int t = lane; t < k; t += 32) a[t] = 0.0;
+    double s = 1.0;
+    __syncwarp();
+    for (int64_t i = 0; i < nrows; ++i) {
+        const double *row = cov + ((size_t)i * nl + l) * kp;
+        if (i > 0 && k > 0) {
+            for (int j = lane; j < k; j += 32) {
+                double acc = 0.0;
+                for (int q = 0; q < k; ++q) acc = fma(a[q], m[q * k + j], acc);
+                atm[j] = acc;
+            }
+            __syncwarp();
+            const double u = s > 0 ? 1.0 : 0.0;
+            const double sd = s > 0 ? s : 1.0;
+            for (int t = lane; t < kk; t += 32) {
+                const int r = t / k, cc = t - r * k;
+                double v;
+                if (r < k - 1)
+                    v = (cc + 1 < k) ? m[(r + 1) * k + (cc + 1)] : 0.0;
+                else
+                    v = ((cc + 1 < k) ? -atm[cc + 1] : u) / sd;
+                mn[t] = v;
+            }
+            __syncwarp();
+            double *tmp = m;
+            m = mn;
+            mn = tmp;
+        }
+        for (int r = lane; r < k; r += 32) {
+            double acc = 0.0;
+            for (int cc = 0; cc < k; ++cc) acc = fma(m[r * k + cc], row[k - cc], acc);
+            a[r] = acc;
+        }
+        __syncwarp();
+        double sv = 0.0;
+        if (lane == 0) {
+            double aa = 0.0;
+            for (int r = 0; r < k; ++r) aa = fma(a[r], a[r], aa);
+            sv = row[0] - aa;
+            if (sv < 0) {
+                atomicMin((unsigned long long *)bad, (unsigned long long)i);
+                sv = 0.0;
+            }
+            sv = sqrt(sv);
+        }
+        s = __shfl_sync(0xffffffffu, sv, 0);
+        double *wo = w + ((size_t)i * nl + l) * kp;
+        for (int r = lane; r < k; r += 32) wo[r] = a[r];
+        if (lane == 0) wo[k] = s;
+        __syncwarp();
+    }
+}
+
+// ------------------------------------------------------------------ philox
+
+struct U4 {
+    uint32_t x, y, z, w;
+};
+
+__device__ __forceinline__ U4 philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
+                                            uint32_t k0, uint32_t k1) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const uint32_t lo0 = 0xD2511F53u * c0, hi0 = __umulhi(0xD2511F53u, c0);
+        const uint32_t lo1 = 0xCD9E8D57u * c2, hi1 = __umulhi(0xCD9E8D57u, c2);
+        const uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+        c0 = n0;
+        c1 = lo1;
+        c2 = n2;
+        c3 = lo0;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    return {c0, c1, c2, c3};
+}
+
+// Complex standard normal: element e of stream sid (see orc_philox_normals).
+__device__ __forceinline__ double2 philox_cnormal_f64(uint64_t seed, uint64_t sid, uint64_t e) {
+    const U4 x = philox4x32_10((uint32_t)e, (uint32_t)(e >> 32), (uint32_t)sid,
+                               (uint32_t)(sid >> 32), (uint32_t)seed, (uint32_t)(seed >> 32));
+    const double u1 = ((double)(x.x >> 5) * 67108864.0 + (double)(x.y >> 6) + 0.5) * 1.1102230246251565e-16;
+    const double u2 = ((double)(x.z >> 5) * 67108864.0 + (double)(x.w >> 6) + 0.5) * 1.1102230246251565e-16;
+    const double r = sqrt(-2.0 * log(u1));
+    double sn, cs;
+    sincospi(2.0 * u2, &sn, &cs);
+    return make_double2(r * cs, r * sn);
+}
+
+__device__ __forceinline__ float2 philox_cnormal_f32(uint64_t seed, uint64_t sid, uint64_t e) {
+    const U4 x = philox4x32_10((uint32_t)e, (uint32_t)(e >> 32), (uint32_t)sid,
+                               (uint32_t)(sid >> 32), (uint32_t)seed, (uint32_t)(seed >> 32));
+    // 24-bit uniforms in (0, 1) from the same high bits as the FP64 form
+    const float u1 = ((float)(x.x >> 8) + 0.5f) * 5.9604644775390625e-08f;
+    const float u2 = ((float)(x.z >> 8) + 0.5f) * 5.9604644775390625e-08f;
+    const float r = sqrtf(-2.0f * logf(u1));
+    float sn, cs;
+    sincospif(2.0f * u2, &sn, &cs);
+    return make_float2(r * cs, r * sn);
+}
+
+__global__ void k_philox_normals(uint64_t seed, uint64_t sid, int64_t offset, int64_t n, int dtype,
+                                 void *out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t e = (uint64_t)(offset + i);
+        if (dtype == GLG_F64)
+            reinterpret_cast<double2 *>(out)[i] = philox_cnormal_f64(seed, sid, e);
+        else
+            reinterpret_cast<float2 *>(out)[i] = philox_cnormal_f32(seed, sid, e);
+    }
+}
+
+// ------------------------------------------------------- alm correlation
+
+// Element (l, m) of shells t0..t0+nshell-1, written in HEALPix order.  One
+// thread per HEALPix index (coalesced stores); the thread keeps the window of
+// variates z_{t-k..t} in shared memory so each variate is read or generated
+// once per element.
+template <typename T2, typename T>
+__global__ void k_alm_correlate(const double *__restrict__ w, const int nshell, const int lmax,
+                                const int k, const int64_t t0, const T2 *__restrict__ z,
+                                const int64_t z_first, const uint64_t seed, const uint64_t sid_base,
+                                T2 *__restrict__ alm, const int window) {
+    extern __shared__ unsigned char zs_raw[];
+    T2 *zs = reinterpret_cast<T2 *>(zs_raw) + (size_t)threadIdx.x * window;
+    const int64_t nalm = glg_nalm(lmax);
+    const int64_t ix = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (ix >= nalm) return;
+    // HEALPix index -> (l, m)
+    const double L2 = 2.0 * lmax + 3.0;
+    int m = (int)floor((L2 - sqrt(L2 * L2 - 8.0 * (double)ix)) * 0.5);
+    while ((int64_t)m * (2 * lmax + 3 - m) / 2 > ix) --m;
+    while ((int64_t)(m + 1) * (2 * lmax + 3 - (m + 1)) / 2 <= ix) ++m;
+    const int l = (int)(ix - (int64_t)m * (2 * lmax + 3 - m) / 2) + m;
+    const int64_t g = (int64_t)l * (l + 1) / 2 + m;  // GLASS index
+    const int L = lmax + 1;
+    const int kp = k + 1;
+    // variates of shells zlo .. t0+nshell-1, ring buffer of size `window` (= k+1)
+    const int64_t zlo = t0 - k > 0 ? t0 - k : 0;
+    auto fetch = [&](int64_t t) -> T2 {
+        if (z != nullptr) return z[(t - z_first) * nalm + g];
+        if constexpr (sizeof(T) == 8) {
+            return philox_cnormal_f64(seed, sid_base + (uint64_t)t, (uint64_t)g);
+        } else {
+            return philox_cnormal_f32(seed, sid_base + (uint64_t)t, (uint64_t)g);
+        }
+    };
+    for (int64_t t = zlo; t < t0; ++t) zs[t % window] = fetch(t);
+    for (int s = 0; s < nshell; ++s) {
+        const int64_t t = t0 + s;
+        zs[t % window] = fetch(t);
+        const double *wt = w + ((size_t)s * L + l) * kp;
+        double re = 0.0, im = 0.0;
+        const int dmax = t < k ? (int)t : k;
+        for (int d = dmax; d >= 0; --d) {  // oldest first, like the reference's sum
+            const T2 zz = zs[(t - d) % window];
+            const double c = wt[k - d];
+            re += c * (double)zz.x;
+            im += c * (double)zz.y;
+        }
+        if (m == 0) {
+            re = re + im;
+            im = 0.0;
+        }
+        T2 o;
+        o.x = (T)re;
+        o.y = (T)im;
+        alm[(int64_t)s * nalm + ix] = o;
+    }
+}
+
+// ----------------------------------------------------------- multalm etc.
+
+template <typename T2>
+__global__ void k_multalm(const T2 *__restrict__ alm, const double *__restrict__ bl, int lmax,
+                          T2 *__restrict__ out) {
+    const int64_t n = glg_nalm(lmax);
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n;
+         g += (int64_t)gridDim.x * blockDim.x) {
+        int l = (int)((sqrt(8.0 * (double)g + 1.0) - 1.0) * 0.5);
+        while ((int64_t)l * (l + 1) / 2 > g) --l;
+        while ((int64_t)(l + 1) * (l + 2) / 2 <= g) ++l;
+        const double f = bl[l];
+        T2 a = alm[g];
+        a.x = a.x * f;
+        a.y = a.y * f;
+        out[g] = a;
+    }
+}
+
+template <typename T2>
+__global__ void k_almxfl(const T2 *__restrict__ alm, const double *__restrict__ fl, int nfl,
+                         int lmax, int nmaps, T2 *__restrict__ out) {
+    const int64_t n = glg_nalm(lmax);
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n * nmaps;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t ix = q % n;
+        const double L2 = 2.0 * lmax + 3.0;
+        int m = (int)floor((L2 - sqrt(L2 * L2 - 8.0 * (double)ix)) * 0.5);
+        while ((int64_t)m * (2 * lmax + 3 - m) / 2 > ix) --m;
+        while ((int64_t)(m + 1) * (2 * lmax + 3 - (m + 1)) / 2 <= ix) ++m;
+        const int l = (int)(ix - (int64_t)m * (2 * lmax + 3 - m) / 2) + m;
+        const double f = l < nfl ? fl[l] : 0.0;
+        T2 a = alm[q];
+        a.x = a.x * f;
+        a.y = a.y * f;
+        out[q] = a;
+    }
+}
+
+int grid_for(int64_t n, int threads) {
+    int64_t b = (n + threads - 1) / threads;
+    if (b > 152 * 64) b = 152 * 64;
+    return (int)(b > 0 ? b : 1);
+}
+
+}  // namespace
+
+extern "C" int glg_iternorm(const double *cov, int64_t nrows, int64_t nl, int k, double *w,
+                            uint64_t *status, void *stream) {
+    GLG_REQUIRE(cov && w && status, "glg_iternorm: null pointer");
+    GLG_REQUIRE(nrows >= 0 && nl >= 0, "glg_iternorm: negative size");
+    GLG_REQUIRE(k >= 0 && k <= 126, "glg_iternorm: k must be in [0, 126]");
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e = cudaMemsetAsync(status, 0xff, sizeof(uint64_t), st);
+    if (e != cudaSuccess) return glg_cuda_status(e, "glg_iternorm: status reset");
+    if (nrows == 0 || nl == 0) return GLG_OK;
+    const int kk = k > 0 ? k * k : 1;
+    const size_t smem = sizeof(double) * (2 * (size_t)kk + 2 * (size_t)(k > 0 ? k : 1));
+    if (smem > 48 * 1024)
+        cudaFuncSetAttribute(k_iternorm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    GLG_LAUNCH_SCOPE("k_iternorm", st);
+    k_iternorm<<<(unsigned)nl, 32, smem, st>>>(cov, nrows, nl, k, w, (int64_t *)status);
+    GLG_CHECK_LAUNCH("k_iternorm");
+    return GLG_OK;
+}
+
+extern "C" int glg_philox_normals(uint64_t seed, uint64_t sid, int64_t offset, int64_t n, int dtype,
+                                  void *out, void *stream) {
+    GLG_REQUIRE(out || n == 0, "glg_philox_normals: null output");
+    GLG_REQUIRE(dtype == GLG_F64 || dtype == GLG_F32, "glg_philox_normals: bad dtype");
+    GLG_REQUIRE(n >= 0 && offset >= 0, "glg_philox_normals: negative size");
+    if (n == 0) return GLG_OK;
+    GLG_LAUNCH_SCOPE("k_philox_normals", (cudaStream_t)stream);
+    k_philox_normals<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(seed, sid, offset, n, dtype, out);
+    GLG_CHECK_LAUNCH("k_philox_normals");
+    return GLG_OK;
+}
+
+extern "C" int glg_alm_correlate(const double *w, int nshell, int lmax, int k, int64_t t0,
+                                 const void *z, int64_t z_first, uint64_t seed, uint64_t sid_base,
+                                 int dtype, void *alm, void *stream) {
+    GLG_REQUIRE(w && alm, "glg_alm_correlate: null pointer");
+    GLG_REQUIRE(nshell >= 0 && lmax >= 0 && k >= 0 && t0 >= 0, "glg_alm_correlate: bad size");
+    GLG_REQUIRE(dtype == GLG_F64 || dtype == GLG_F32, "glg_alm_correlate: bad dtype");
+    GLG_REQUIRE(k <= 126, "glg_alm_correlate: k must be <= 126");
+    if (z) GLG_REQUIRE(z_first == (t0 - k > 0 ? t0 - k : 0), "glg_alm_correlate: z must start at max(0, t0-k)");
+    if (nshell == 0) return GLG_OK;
+    const int64_t n = glg_nalm(lmax);
+    const int window = k + 1;
+    const int threads = 64;
+    const size_t esz = dtype == GLG_F64 ? sizeof(double2) : sizeof(float2);
+    const size_t smem = esz * (size_t)window * threads;
+    cudaStream_t st = (cudaStream_t)stream;
+    const unsigned blocks = (unsigned)((n + threads - 1) / threads);
+    GLG_LAUNCH_SCOPE("k_alm_correlate", st);
+    if (dtype == GLG_F64) {
+        if (smem > 48 * 1024)
+            cudaFuncSetAttribute(k_alm_correlate<double2, double>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_alm_correlate<double2, double><<<blocks, threads, smem, st>>>(
+            w, nshell, lmax, k, t0, (const double2 *)z, z_first, seed, sid_base, (double2 *)alm, window);
+    } else {
+        if (smem > 48 * 1024)
+            cudaFuncSetAttribute(k_alm_correlate<float2, float>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_alm_correlate<float2, float><<<blocks, threads, smem, st>>>(
+            w, nshell, lmax, k, t0, (const float2 *)z, z_first, seed, sid_base, (float2 *)alm, window);
+    }
+    GLG_CHECK_LAUNCH("k_alm_correlate");
+    return GLG_OK;
+}
+
+extern "C" int glg_multalm(const void *alm, const double *bl, int lmax, int dtype, void *out,
+                           void *stream) {
+    GLG_REQUIRE((alm && bl && out) || lmax < 0, "glg_multalm: null pointer");
+    GLG_REQUIRE(dtype == GLG_F64 || dtype == GLG_F32, "glg_multalm: bad dtype");
+    if (lmax < 0) return GLG_OK;
+    const int64_t n = glg_nalm(lmax);
+    cudaStream_t st = (cudaStream_t)stream;
+    GLG_LAUNCH_SCOPE("k_multalm", st);
+    if (dtype == GLG_F64)
+        k_multalm<double2><<<grid_for(n, 256), 256, 0, st>>>((const double2 *)alm, bl, lmax, (double2 *)out);
+    else
+        k_multalm<float2><<<grid_for(n, 256), 256, 0, st>>>((const float2 *)alm, bl, lmax, (float2 *)out);
+    GLG_CHECK_LAUNCH("k_multalm");
+    return GLG_OK;
+}
+
+extern "C" int glg_almxfl(const void *alm, const double *fl, int nfl, int lmax, int nmaps, int dtype,
+                          void *out, void *stream) {
+    GLG_REQUIRE(alm && out, "glg_almxfl: null pointer");
+    GLG_REQUIRE(fl || nfl == 0, "glg_almxfl: null fl");
+    GLG_REQUIRE(lmax >= 0 && nmaps >= 0 && nfl >= 0, "glg_almxfl: bad size");
+    GLG_REQUIRE(dtype == GLG_F64 || dtype == GLG_F32, "glg_almxfl: bad dtype");
+    const int64_t n = glg_nalm(lmax) * nmaps;
+    if (n == 0) return GLG_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    GLG_LAUNCH_SCOPE("k_almxfl", st);
+    if (dtype == GLG_F64)
+        k_almxfl<double2><<<grid_for(n, 256), 256, 0, st>>>((const double2 *)alm, fl, nfl, lmax, nmaps, (double2 *)out);
+    else
+        k_almxfl<float2><<<grid_for(n, 256), 256, 0, st>>>((const float2 *)alm, fl, nfl, lmax, nmaps, (float2 *)out);
+    GLG_CHECK_LAUNCH("k_almxfl");
+    return GLG_OK;
+}

@@ -1,0 +1,99 @@
+// Internal definitions shared by the glass_gb300 CUDA translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/glass_gb300.h"
+
+// ------------------------------------------------------------------ errors
+
+void glg_set_error(const std::string &msg);
+int glg_cuda_status(cudaError_t err, const char *where);
+
+#define GLG_CHECK_LAUNCH(where)                                   \
+    do {                                                          \
+        cudaError_t e_ = cudaGetLastError();                      \
+        if (e_ != cudaSuccess) return glg_cuda_status(e_, where); \
+    } while (0)
+
+#define GLG_REQUIRE(cond, msg)          \
+    do {                                \
+        if (!(cond)) {                  \
+            glg_set_error(msg);         \
+            return GLG_ERR_INVALID;     \
+        }                               \
+    } while (0)
+
+// ------------------------------------------------------------------ timing
+
+// Scope around one kernel launch: counts the launch and, when timing is
+// enabled (glg_timing_enable), brackets it with CUDA events on its stream.
+struct glg_launch_scope {
+    glg_launch_scope(const char *name, cudaStream_t st);
+    ~glg_launch_scope();
+    const char *name;
+    cudaStream_t st;
+    cudaEvent_t ev0, ev1;
+    bool timed;
+};
+
+#define GLG_LAUNCH_SCOPE(name, st) glg_launch_scope glg_scope_(name, st)
+
+// -------------------------------------------------------------------- plan
+
+// Maximum number of radix passes of one ring FFT (n = 4 i <= 4 * 8192).
+#define GLG_MAX_FFT_STAGES 20
+
+struct glg_plan {
+    int nside, lmax, mmax;
+    int nrings, npairs;
+    int64_t npix, nalm;
+    int device;
+    size_t bytes;
+
+    // ring pairs p = 0 .. npairs-1: north ring p (0-based), south ring
+    // nrings-1-p; the last pair is the equator (north == south).
+    double *cth, *sth;       // [npairs]
+    int *nph;                // [npairs]
+    int *half;               // [npairs] 1: phi0 = pi / nph, 0: phi0 = 0
+    int64_t *startN, *startS;  // [npairs] first pixel of each ring
+
+    // Legendre recurrence lambda_l = A (x lambda_{l-1}) - B lambda_{l-2}
+    int64_t *mofs;           // [mmax+2] HEALPix index of (l=m, m)
+    double2 *coef;           // [nalm] (A, B) at mofs[m] + l - m (l >= m+2)
+    double *lmm;             // [mmax+1][npairs] lambda_mm mantissa
+    int *lmm_scale;          // [mmax+1][npairs] exponent scale (x 2^800)
+
+    // ring FFTs for lengths n = 4 i, i = 1 .. nside
+    int *fft_radix;          // [nside+1][GLG_MAX_FFT_STAGES]
+    int *fft_nst;            // [nside+1]
+    int64_t *tw_ofs;         // [nside+1] offset of the table of length i
+    double2 *tw;             // tw[ofs_i + t] = exp(i pi t / (4 i)), t < 8 i
+};
+
+// ---------------------------------------------------------- device helpers
+
+__host__ __device__ inline int64_t glg_nalm(int lmax) {
+    return (int64_t)(lmax + 1) * (lmax + 2) / 2;
+}
+
+// extended-range constants of the Legendre recurrence
+#define GLG_TWO_P800 6.668014432879854e+240
+#define GLG_TWO_M800 1.499696813895631e-241
+#define GLG_TWO_P400 2.5822498780869086e+120
+#define GLG_TWO_M400 3.872591914849318e-121
+
+// Launch helpers implemented in the individual .cu files.
+int glg_launch_leg_syn(const glg_plan *P, const double2 *alm, int nmaps, double2 *F,
+                       cudaStream_t st);
+int glg_launch_leg_syn_spin(const glg_plan *P, const double2 *elm, const double2 *blm, int spin,
+                            double2 *F, cudaStream_t st);
+int glg_launch_ring_syn(const glg_plan *P, const double2 *F, int nmaps, double *maps,
+                        const glg_epilogue *epi, cudaStream_t st);
+int glg_launch_ring_ana(const glg_plan *P, const double *maps, int nmaps, double2 *G,
+                        cudaStream_t st);
+int glg_launch_leg_ana(const glg_plan *P, const double2 *G, int nmaps, double2 *alm, int accumulate,
+                       cudaStream_t st);

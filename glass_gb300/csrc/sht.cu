@@ -1,0 +1,96 @@
+// C-ABI entry points of the spherical-harmonic transforms (plain FP64 form):
+// alm2map, alm2map_spin and map2alm, built from the Legendre and ring-FFT
+// launches.  Every call works in caller-provided device workspace.
+#include <cuda_runtime.h>
+
+#include "glg_internal.cuh"
+
+namespace {
+
+__global__ void k_residual(const double *__restrict__ f, double *__restrict__ r, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        r[i] = f[i] - r[i];
+}
+
+size_t ring_coef_bytes(const glg_plan *P, int nmaps) {
+    return sizeof(double2) * (size_t)nmaps * P->nrings * (P->mmax + 1);
+}
+
+}  // namespace
+
+extern "C" size_t glg_alm2map_workspace(const glg_plan *P, int nmaps, int form) {
+    if (!P || nmaps <= 0) return 0;
+    (void)form;
+    return ring_coef_bytes(P, nmaps);
+}
+
+extern "C" int glg_alm2map(const glg_plan *P, const void *alm, int nmaps, int form, void *maps,
+                           const glg_epilogue *epi, void *ws, size_t ws_bytes, void *stream) {
+    GLG_REQUIRE(P != nullptr, "glg_alm2map: null plan");
+    GLG_REQUIRE(nmaps >= 0, "glg_alm2map: negative nmaps");
+    if (nmaps == 0) return GLG_OK;
+    GLG_REQUIRE(alm && maps, "glg_alm2map: null pointer");
+    GLG_REQUIRE(form == GLG_FORM_PLAIN, "glg_alm2map: unknown form");
+    GLG_REQUIRE(ws && ws_bytes >= glg_alm2map_workspace(P, nmaps, form),
+                "glg_alm2map: workspace too small");
+    cudaStream_t st = (cudaStream_t)stream;
+    double2 *F = (double2 *)ws;
+    int rc = glg_launch_leg_syn(P, (const double2 *)alm, nmaps, F, st);
+    if (rc) return rc;
+    return glg_launch_ring_syn(P, F, nmaps, (double *)maps, epi, st);
+}
+
+extern "C" size_t glg_alm2map_spin_workspace(const glg_plan *P) {
+    return P ? ring_coef_bytes(P, 2) : 0;
+}
+
+extern "C" int glg_alm2map_spin(const glg_plan *P, const void *elm, const void *blm, int spin,
+                                void *q, void *u, void *ws, size_t ws_bytes, void *stream) {
+    GLG_REQUIRE(P != nullptr, "glg_alm2map_spin: null plan");
+    GLG_REQUIRE(elm && q && u, "glg_alm2map_spin: null pointer");
+    GLG_REQUIRE(spin == 1 || spin == 2, "glg_alm2map_spin: spin must be 1 or 2");
+    GLG_REQUIRE(ws && ws_bytes >= glg_alm2map_spin_workspace(P), "glg_alm2map_spin: workspace too small");
+    cudaStream_t st = (cudaStream_t)stream;
+    double2 *F = (double2 *)ws;
+    int rc = glg_launch_leg_syn_spin(P, (const double2 *)elm, (const double2 *)blm, spin, F, st);
+    if (rc) return rc;
+    rc = glg_launch_ring_syn(P, F, 1, (double *)q, nullptr, st);
+    if (rc) return rc;
+    return glg_launch_ring_syn(P, F + (size_t)P->nrings * (P->mmax + 1), 1, (double *)u, nullptr, st);
+}
+
+extern "C" size_t glg_map2alm_workspace(const glg_plan *P, int nmaps) {
+    if (!P || nmaps <= 0) return 0;
+    return ring_coef_bytes(P, nmaps) + sizeof(double) * (size_t)nmaps * P->npix;
+}
+
+extern "C" int glg_map2alm(const glg_plan *P, const void *maps, int nmaps, int niter, void *alm,
+                           void *ws, size_t ws_bytes, void *stream) {
+    GLG_REQUIRE(P != nullptr, "glg_map2alm: null plan");
+    GLG_REQUIRE(nmaps >= 0 && niter >= 0, "glg_map2alm: negative size");
+    if (nmaps == 0) return GLG_OK;
+    GLG_REQUIRE(maps && alm, "glg_map2alm: null pointer");
+    GLG_REQUIRE(ws && ws_bytes >= glg_map2alm_workspace(P, nmaps), "glg_map2alm: workspace too small");
+    cudaStream_t st = (cudaStream_t)stream;
+    double2 *G = (double2 *)ws;
+    double *tmp = (double *)((char *)ws + ring_coef_bytes(P, nmaps));
+    const double *f = (const double *)maps;
+    double2 *a = (double2 *)alm;
+    int rc = glg_launch_ring_ana(P, f, nmaps, G, st);
+    if (rc) return rc;
+    if ((rc = glg_launch_leg_ana(P, G, nmaps, a, 0, st))) return rc;
+    const int64_t n = (int64_t)nmaps * P->npix;
+    for (int it = 0; it < niter; ++it) {
+        if ((rc = glg_launch_leg_syn(P, a, nmaps, G, st))) return rc;
+        if ((rc = glg_launch_ring_syn(P, G, nmaps, tmp, nullptr, st))) return rc;
+        {
+            GLG_LAUNCH_SCOPE("k_residual", st);
+            k_residual<<<1216, 256, 0, st>>>(f, tmp, n);
+            GLG_CHECK_LAUNCH("k_residual");
+        }
+        if ((rc = glg_launch_ring_ana(P, tmp, nmaps, G, st))) return rc;
+        if ((rc = glg_launch_leg_ana(P, G, nmaps, a, 1, st))) return rc;
+    }
+    return GLG_OK;
+}

@@ -1,0 +1,246 @@
+"""HEALPix spherical-harmonic transforms on the GPU.
+
+Drop-in for the transform façade of ``glass/healpix.py`` (``alm2map``
+:38-78, ``alm2map_spin`` :81-108, ``almxfl`` :111-140, ``get_nside``
+:214-229, ``map2alm`` :232-276, ``nside2npix`` :296, ``npix2nside``), which
+the reference delegates to healpy.  Inputs may be numpy arrays (results come
+back as numpy) or torch tensors (results stay on the device).  Everything is
+computed by the CUDA library; nothing falls back to the CPU.
+
+Conventions (HEALPix): RING ordering, alm in m-major order with mmax = lmax,
+Condon-Shortley phase; spin-s maps ``Q + iU = -sum_lm (E_lm + i B_lm) sY_lm``.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import math
+import warnings
+from collections.abc import Sequence
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import c_p, check, get_plan, lib, ptr, stream_ptr
+
+__all__ = [
+    "alm2map",
+    "alm2map_spin",
+    "almxfl",
+    "get_nside",
+    "map2alm",
+    "npix2nside",
+    "nside2npix",
+    "pixwin",
+]
+
+
+def nside2npix(nside: int) -> int:
+    return 12 * int(nside) * int(nside)
+
+
+def npix2nside(npix: int) -> int:
+    nside = math.isqrt(int(npix) // 12)
+    if 12 * nside * nside != int(npix):
+        raise ValueError(f"{npix} is not a valid number of HEALPix pixels")
+    return nside
+
+
+def get_nside(m) -> int:
+    n = m.shape[-1]
+    return npix2nside(n)
+
+
+def _lmax_from_size(n: int) -> int:
+    lmax = (math.isqrt(8 * n + 1) - 3) // 2
+    if (lmax + 1) * (lmax + 2) // 2 != n:
+        raise ValueError(f"wrong alm size {n}: not (lmax+1)(lmax+2)/2 for any lmax")
+    return lmax
+
+
+def _as_device_alm(a) -> torch.Tensor:
+    return _lib.to_device(a, torch.complex128)
+
+
+def _finish(t: torch.Tensor, numpy_out: bool):
+    return t.cpu().numpy() if numpy_out else t
+
+
+def _resize_alm(alm: torch.Tensor, lmax_in: int, lmax_out: int) -> torch.Tensor:
+    """Truncate or zero-pad HEALPix-order alm (mmax = lmax) to another lmax."""
+    if lmax_in == lmax_out:
+        return alm
+    out = torch.zeros(alm.shape[:-1] + ((lmax_out + 1) * (lmax_out + 2) // 2,), dtype=alm.dtype,
+                      device=alm.device)
+    lm = min(lmax_in, lmax_out)
+    for m in range(lm + 1):
+        si = m * (2 * lmax_in + 1 - m) // 2
+        so = m * (2 * lmax_out + 1 - m) // 2
+        out[..., so + m:so + lm + 1] = alm[..., si + m:si + lm + 1]
+    return out
+
+
+def synth(alm: torch.Tensor, nside: int, lmax: int, *, epilogue=None) -> torch.Tensor:
+    """Spin-0 synthesis of complex128 alm [nmaps, nalm] -> float64 maps [nmaps, npix]."""
+    plan = get_plan(nside, lmax, alm.device)
+    nmaps = alm.shape[0]
+    maps = torch.empty((nmaps, plan.npix), dtype=torch.float64, device=alm.device)
+    ws_bytes = int(lib().glg_alm2map_workspace(plan.handle, nmaps, _lib.FORM_PLAIN))
+    ws = torch.empty(max(ws_bytes, 1), dtype=torch.uint8, device=alm.device)
+    epi = None
+    if epilogue is not None:
+        kind, var, lam = epilogue
+        kinds = list(kind) if isinstance(kind, (list, tuple)) else [int(kind)] * nmaps
+        kinds_a = (ctypes.c_int * nmaps)(*kinds)
+        var_a = (ctypes.c_double * nmaps)(*var)
+        lam_a = (ctypes.c_double * nmaps)(*lam)
+        epi = _lib.Epilogue(_lib.EPI_NONE, kinds_a, var_a, lam_a)
+    check(lib().glg_alm2map(plan.handle, c_p(ptr(alm)), nmaps, _lib.FORM_PLAIN, c_p(ptr(maps)),
+                            ctypes.byref(epi) if epi is not None else None, c_p(ptr(ws)), ws_bytes,
+                            c_p(stream_ptr(alm.device))), "glg_alm2map")
+    return maps
+
+
+def alm2map(alms, nside: int, *, inplace: bool = False, lmax: int | None = None,
+            pixwin: bool = False, pol: bool = True):
+    """HEALPix map(s) from alm (glass/healpix.py:38-78).
+
+    ``alms`` is one complex array, or a sequence of them; with ``pol=True``
+    and three arrays they are (T, E, B) and (T, Q, U) maps are returned.
+    ``pixwin=True`` needs HEALPix pixel-window tables and is not supported.
+    """
+    if pixwin:
+        raise NotImplementedError(
+            "pixwin=True needs HEALPix pixel-window tables, which are not available"
+        )
+    seq = isinstance(alms, (list, tuple))
+    items = list(alms) if seq else [alms]
+    numpy_out = all(_lib.is_numpy_like(a) for a in items)
+    dev = [_as_device_alm(a) for a in items]
+    if any(d.ndim != 1 for d in dev) and not (not seq and dev[0].ndim == 2):
+        raise ValueError("alm must be one-dimensional")
+    if not seq and dev[0].ndim == 2:
+        dev = list(dev[0])
+        seq = True
+    n = dev[0].shape[-1]
+    lmax_in = _lmax_from_size(n)
+    lmax = lmax_in if lmax is None else int(lmax)
+    if seq and pol and len(dev) == 3:
+        t = synth(_resize_alm(dev[0], lmax_in, lmax)[None], nside, lmax)[0]
+        q, u = _spin_synth(_resize_alm(dev[1], lmax_in, lmax), _resize_alm(dev[2], lmax_in, lmax),
+                           nside, 2, lmax)
+        out = [t, q, u]
+        return [_finish(o, numpy_out) for o in out] if not numpy_out else np.stack([o.cpu().numpy() for o in out])
+    stack = torch.stack([_resize_alm(d, lmax_in, lmax) for d in dev])
+    maps = synth(stack, nside, lmax)
+    if not seq:
+        return _finish(maps[0], numpy_out)
+    return maps.cpu().numpy() if numpy_out else list(maps)
+
+
+def _spin_synth(elm: torch.Tensor, blm: torch.Tensor | None, nside: int, spin: int, lmax: int):
+    plan = get_plan(nside, lmax, elm.device)
+    q = torch.empty(plan.npix, dtype=torch.float64, device=elm.device)
+    u = torch.empty_like(q)
+    ws_bytes = int(lib().glg_alm2map_spin_workspace(plan.handle))
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device=elm.device)
+    check(lib().glg_alm2map_spin(plan.handle, c_p(ptr(elm)), c_p(ptr(blm)) if blm is not None else None,
+                                 spin, c_p(ptr(q)), c_p(ptr(u)), c_p(ptr(ws)), ws_bytes,
+                                 c_p(stream_ptr(elm.device))), "glg_alm2map_spin")
+    return q, u
+
+
+def alm2map_spin(alms: Sequence, nside: int, spin: int, lmax: int):
+    """Spin-weighted maps [Q, U] from [E, B] alm (glass/healpix.py:81-108)."""
+    if len(alms) != 2:
+        raise ValueError("alm2map_spin needs exactly two alm arrays")
+    numpy_out = all(_lib.is_numpy_like(a) for a in alms)
+    e = _as_device_alm(alms[0])
+    b = _as_device_alm(alms[1])
+    lmax_in = _lmax_from_size(e.shape[-1])
+    e = _resize_alm(e, lmax_in, lmax)
+    b = _resize_alm(b, lmax_in, lmax)
+    if not bool(torch.any(b != 0)):
+        b = None
+    q, u = _spin_synth(e, b, nside, int(spin), int(lmax))
+    return [_finish(q, numpy_out), _finish(u, numpy_out)]
+
+
+def analysis(maps: torch.Tensor, lmax: int, niter: int = 3) -> torch.Tensor:
+    """float64 maps [nmaps, npix] -> complex128 alm [nmaps, nalm]."""
+    nside = npix2nside(maps.shape[-1])
+    plan = get_plan(nside, lmax, maps.device)
+    nmaps = maps.shape[0]
+    alm = torch.empty((nmaps, plan.nalm), dtype=torch.complex128, device=maps.device)
+    ws_bytes = int(lib().glg_map2alm_workspace(plan.handle, nmaps))
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device=maps.device)
+    check(lib().glg_map2alm(plan.handle, c_p(ptr(maps)), nmaps, int(niter), c_p(ptr(alm)),
+                            c_p(ptr(ws)), ws_bytes, c_p(stream_ptr(maps.device))), "glg_map2alm")
+    return alm
+
+
+_WARNED_WEIGHTS = False
+
+
+def map2alm(maps, *, lmax: int | None = None, pol: bool = True,
+            use_pixel_weights: bool = False, iter: int = 3):  # noqa: A002
+    """alm of RING-ordered map(s) (glass/healpix.py:232-276).
+
+    Uses uniform pixel weights and ``iter`` Jacobi refinements (healpy's
+    default of 3).  HEALPix pixel-weight files are not available, so
+    ``use_pixel_weights=True`` falls back to the same iterated quadrature.
+    """
+    global _WARNED_WEIGHTS
+    if use_pixel_weights and not _WARNED_WEIGHTS:
+        warnings.warn("pixel-weight files are not available: using uniform weights with "
+                      f"{iter} refinement iterations", RuntimeWarning, stacklevel=2)
+        _WARNED_WEIGHTS = True
+    seq = isinstance(maps, (list, tuple))
+    items = list(maps) if seq else [maps]
+    numpy_out = all(_lib.is_numpy_like(m) for m in items)
+    dev = torch.stack([_lib.to_device(m, torch.float64).reshape(-1) for m in items]) if seq else \
+        _lib.to_device(maps, torch.float64)
+    if dev.ndim == 1:
+        dev = dev[None]
+        single = True
+    else:
+        single = False
+    nside = npix2nside(dev.shape[-1])
+    lmax = 3 * nside - 1 if lmax is None else int(lmax)
+    if seq and pol and len(items) == 3:
+        raise NotImplementedError("polarised map2alm (TQU -> TEB) is not part of this path")
+    alm = analysis(dev, lmax, iter)
+    if single:
+        return _finish(alm[0], numpy_out)
+    return alm.cpu().numpy() if numpy_out else list(alm)
+
+
+def almxfl(alm, fl, *, inplace: bool = False):
+    """alm[l, m] * fl[l] in HEALPix order (glass/healpix.py:111-140)."""
+    numpy_out = _lib.is_numpy_like(alm)
+    a = _as_device_alm(alm)
+    f = _lib.to_device(fl, torch.float64, a.device).reshape(-1)
+    single = a.ndim == 1
+    a2 = a.reshape(-1, a.shape[-1])
+    lmax = _lmax_from_size(a2.shape[-1])
+    out = a2 if (inplace and not numpy_out and isinstance(alm, torch.Tensor) and alm.dtype == torch.complex128) \
+        else torch.empty_like(a2)
+    check(lib().glg_almxfl(c_p(ptr(a2)), c_p(ptr(f)) if f.numel() else None, int(f.numel()), lmax,
+                           a2.shape[0], _lib.GLG_F64, c_p(ptr(out)), c_p(stream_ptr(a.device))),
+          "glg_almxfl")
+    res = out[0] if single else out
+    if numpy_out:
+        r = res.cpu().numpy()
+        if inplace and isinstance(alm, np.ndarray):
+            alm[...] = r
+            return alm
+        return r
+    return res
+
+
+def pixwin(nside: int, *, lmax: int | None = None, pol: bool = False, xp=None):
+    """HEALPix pixel window functions: the tables are not available here."""
+    raise NotImplementedError(
+        "HEALPix pixel-window tables are not available; use discretized=False"
+    )

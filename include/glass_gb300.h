@@ -1,0 +1,170 @@
+/*
+ * glass_gb300 -- C ABI of the GB300 (sm_103a) field-generation path.
+ *
+ * Every entry point takes DEVICE pointers (CUDA global memory), plain sizes
+ * and a cudaStream_t passed as void*, launches asynchronously on that
+ * stream, and returns an int status (GLG_OK = 0, negative on error; the
+ * message is in glg_last_error()).  Nothing here traps or aborts.  Complex
+ * arrays are interleaved (re, im) pairs of the element type named by the
+ * `dtype` argument: GLG_F64 = complex128 / float64, GLG_F32 = complex64 /
+ * float32.
+ *
+ * Each function names the reference interface it replaces (GLASS, file:line
+ * within the glass-dev/glass project).  The Python package glass_gb300 binds
+ * these through ctypes; INTEGRATION.md shows the binding a GLASS maintainer
+ * would add.
+ */
+#ifndef GLASS_GB300_H
+#define GLASS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define GLG_OK 0
+#define GLG_ERR_INVALID (-1)      /* bad argument        -> ValueError  */
+#define GLG_ERR_NOT_POSDEF (-2)   /* iternorm s^2 < 0    -> ValueError  */
+#define GLG_ERR_CUDA (-3)         /* CUDA runtime error  -> RuntimeError */
+#define GLG_ERR_NOMEM (-4)        /* allocation failed   -> MemoryError */
+#define GLG_ERR_UNSUPPORTED (-5)  /* size beyond a kernel limit          */
+#define GLG_ERR_TIMEOUT (-6)      /* a bounded device wait gave up       */
+
+/* element types */
+#define GLG_F64 0
+#define GLG_F32 1
+
+/* precision forms of the spherical-harmonic transforms */
+#define GLG_FORM_PLAIN 0   /* FP64 everywhere (drop-in form)                 */
+#define GLG_FORM_FAST 1    /* FP32 maps; split-precision Legendre contraction */
+
+/* fused map epilogues (glass/grf/_transformations.py) */
+#define GLG_EPI_NONE 0       /* Normal.__call__, :26-28                   */
+#define GLG_EPI_LOGNORMAL 1  /* Lognormal.__call__, :83-89: l*expm1(x - v/2) */
+
+typedef struct glg_plan glg_plan;
+
+/* Library version string and last error message of the calling thread. */
+const char *glg_version(void);
+const char *glg_last_error(void);
+
+/*
+ * Plan: HEALPix ring geometry, Legendre recurrence tables (FP64) and ring-FFT
+ * twiddle tables for one (nside, lmax), resident on the current device.
+ * Replaces the implicit per-call set-up inside healpy.alm2map / map2alm
+ * (called at glass/healpix.py:71, :107, :270).  nside must be a power of two.
+ * Creating a plan allocates device memory (cudaMalloc) and is the only
+ * allocating call of this library besides glg_plan_destroy.
+ */
+int glg_plan_create(int nside, int lmax, void *stream, glg_plan **plan);
+void glg_plan_destroy(glg_plan *plan);
+size_t glg_plan_device_bytes(const glg_plan *plan);
+int glg_plan_info(const glg_plan *plan, int *nside, int *lmax, int *nrings, int64_t *npix,
+                  int64_t *nalm);
+
+/*
+ * Iterative Cholesky scaling vectors, glass/fields.py:101-188 (iternorm).
+ * cov: float64 [nrows][nl][k+1], row i = the covariance row of field i for
+ * every mode l, as produced by cls2cov (glass/fields.py:191-236).
+ * w: float64 [nrows][nl][k+1] = [a_0..a_{k-1}, s].  status: one uint64 of
+ * device memory; it is set to UINT64_MAX before the launch and, when a row's
+ * variance becomes negative, to the first such row -- the caller then raises
+ * "covariance matrix is not positive definite" (glass/fields.py:180-181).
+ * Asynchronous; allocates nothing.  Bit-identical to the fixed-order
+ * restatement in oracle/orc_sht.c.  Limit: k <= 126.
+ */
+int glg_iternorm(const double *cov, int64_t nrows, int64_t nl, int k, double *w,
+                 uint64_t *status, void *stream);
+
+/*
+ * Standard complex normals of the counter-based stream that replaces the
+ * reference's numpy draw standard_normal((z_size, 2)) @ [1, 1j]
+ * (glass/fields.py:407; generator seam glass/rng.py:21-55).  Element e of
+ * stream `sid` under `seed` is one Philox4x32-10 block (counter = e, sid;
+ * key = seed) mapped by Box-Muller; writes n complex values for elements
+ * offset..offset+n-1.
+ */
+int glg_philox_normals(uint64_t seed, uint64_t sid, int64_t offset, int64_t n, int dtype,
+                       void *out, void *stream);
+
+/*
+ * Correlated alm of shells t0..t0+nshell-1 (glass/fields.py:401-425):
+ *   alm_t = sum_{d=0..min(t,k)} multalm(z_{t-d}, w_t[:, k-d])
+ * (glass/harmonics.py:17-47), reordered from GLASS to HEALPix order
+ * (glass/fields.py:943-962) with the m = 0 realification of
+ * glass/fields.py:425.  w: float64 [nshell][L][k+1] (iternorm output of
+ * those shells, L = lmax+1).  z: complex [nz][nalm] in GLASS order holding
+ * shells z_first..t0+nshell-1 (z_first = max(0, t0-k)), or NULL to draw them
+ * from the Philox stream (key seed, stream sid_base + shell index, element =
+ * GLASS index).  alm: complex [nshell][nalm], HEALPix order.  dtype applies
+ * to z and alm.
+ */
+int glg_alm_correlate(const double *w, int nshell, int lmax, int k, int64_t t0, const void *z,
+                      int64_t z_first, uint64_t seed, uint64_t sid_base, int dtype, void *alm,
+                      void *stream);
+
+/* multalm, glass/harmonics.py:17-47: alm (GLASS order) * repeat(bl, l+1). */
+int glg_multalm(const void *alm, const double *bl, int lmax, int dtype, void *out, void *stream);
+
+/* almxfl, glass/healpix.py:111-140: HEALPix-order alm * fl[l] (0 beyond nfl). */
+int glg_almxfl(const void *alm, const double *fl, int nfl, int lmax, int nmaps, int dtype,
+               void *out, void *stream);
+
+/* Fused epilogue applied while maps are stored. */
+typedef struct glg_epilogue {
+    int kind;             /* GLG_EPI_* for every map, unless `kinds` is set  */
+    const int *kinds;     /* host array [nmaps] of GLG_EPI_*, or NULL        */
+    const double *var;    /* host array [nmaps]: Gaussian variance sigma^2   */
+    const double *lamda;  /* host array [nmaps]: lognormal shift lambda      */
+} glg_epilogue;
+
+/*
+ * Spin-0 synthesis, glass/healpix.py:38-78 (healpy.alm2map with pol=False,
+ * pixwin=False; as called at glass/fields.py:429).  alm: complex [nmaps][nalm]
+ * (HEALPix order, mmax = lmax of the plan); maps: [nmaps][npix] RING order.
+ * form GLG_FORM_PLAIN: FP64 throughout (alm and maps dtype GLG_F64).
+ * workspace: device scratch of glg_alm2map_workspace() bytes.
+ */
+size_t glg_alm2map_workspace(const glg_plan *plan, int nmaps, int form);
+int glg_alm2map(const glg_plan *plan, const void *alm, int nmaps, int form, void *maps,
+                const glg_epilogue *epi, void *workspace, size_t workspace_bytes, void *stream);
+
+/*
+ * Spin-s synthesis (s = 1, 2), glass/healpix.py:81-108 (healpy.alm2map_spin,
+ * as called at glass/lensing.py:343, :366).  elm, blm: complex128 [nalm]
+ * (blm may be NULL = zero B-modes); q, u: float64 [npix].
+ * Convention: Q + iU = -sum (E + iB) sY_lm.
+ */
+size_t glg_alm2map_spin_workspace(const glg_plan *plan);
+int glg_alm2map_spin(const glg_plan *plan, const void *elm, const void *blm, int spin, void *q,
+                     void *u, void *workspace, size_t workspace_bytes, void *stream);
+
+/*
+ * Spin-0 analysis, glass/healpix.py:232-276 (healpy.map2alm with pol=False,
+ * as called at glass/lensing.py:306), uniform pixel weights 4 pi / npix and
+ * `niter` Jacobi refinements (healpy's default iter = 3).  maps: float64
+ * [nmaps][npix]; alm: complex128 [nmaps][nalm].
+ */
+size_t glg_map2alm_workspace(const glg_plan *plan, int nmaps);
+int glg_map2alm(const glg_plan *plan, const void *maps, int nmaps, int niter, void *alm,
+                void *workspace, size_t workspace_bytes, void *stream);
+
+/*
+ * Launch accounting (no counterpart in the reference, which has no GPU
+ * code): every kernel launch of this library is counted; with timing
+ * enabled each launch is bracketed by CUDA events on its own stream and
+ * glg_timing_query sums the durations per kernel name (it waits for them).
+ */
+int glg_timing_enable(int on);
+int glg_timing_reset(void);
+int64_t glg_launch_count(void);
+int glg_timing_query(const char *kernel, double *total_ms, int64_t *launches);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GLASS_GB300_H */

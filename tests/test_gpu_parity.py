@@ -1,0 +1,285 @@
+"""GPU parity tests: the CUDA path (through the C ABI) against the oracle.
+
+Tolerances: plain form (FP64 throughout) <= 1e-12 relative to the largest
+oracle value; iternorm and the Philox integer stream bit-exact; the
+glass-side glue (alm assembly) to 1e-15 absolute against the reference's own
+fixtures.
+"""
+
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import pytest
+
+import oracle.fields as of
+import oracle.rng as orng
+import oracle.sht as osht
+from tests.conftest import random_alm, rel_err, spectra_cfg1, spectra_cfg2
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12
+
+
+@pytest.fixture(scope="module")
+def g(cuda_lib):
+    import glass_gb300
+
+    return glass_gb300
+
+
+# ------------------------------------------------------------- iternorm
+
+
+def _iternorm_gpu(cov):
+    import torch
+
+    from glass_gb300 import fields
+
+    w, status = fields._iternorm_device(torch.as_tensor(cov, device="cuda").contiguous())
+    return w.cpu().numpy(), fields._first_bad(status)
+
+
+def test_iternorm_bit_exact_vs_oracle(g, golden):
+    for nc in (5, 2):
+        cov = golden[f"cls2cov_cfg2_nc{nc}"]
+        w, bad = _iternorm_gpu(cov)
+        wo, bado = of.iternorm_stack(cov)
+        assert bad == bado == -1
+        np.testing.assert_array_equal(w, wo)
+        np.testing.assert_allclose(w, golden[f"iternorm_cfg2_nc{nc}"], rtol=1e-13, atol=1e-16)
+
+
+def test_iternorm_bit_exact_large_k(g):
+    gls, _ = spectra_cfg2(40, 300, seed=4)
+    cov = np.stack([c.copy() for c in of.cls2cov(gls, 301, 40, 39)])
+    w, bad = _iternorm_gpu(cov)
+    wo, bado = of.iternorm_stack(cov)
+    assert bad == bado == -1
+    np.testing.assert_array_equal(w, wo)
+
+
+def test_iternorm_generator_api(g, golden):
+    for k in (0, 1, 2):
+        for nd in ("0d", "nd"):
+            rows = [golden[f"iternorm_k{k}_{nd}_in{i}"] for i in range(3)]
+            ws = list(g.iternorm(iter(rows)))
+            for i, w in enumerate(ws):
+                np.testing.assert_allclose(w, golden[f"iternorm_k{k}_{nd}_row{i}"], rtol=1e-13, atol=1e-16)
+
+
+def test_iternorm_errors(g):
+    with pytest.raises(ValueError, match="shape mismatch"):
+        list(g.iternorm([np.ones(1), np.ones((5, 2))]))
+    gen = g.iternorm([np.asarray([1.0]), np.asarray([0.1, 1.0])])
+    assert next(gen).shape == (1,)
+    with pytest.raises(ValueError, match="not positive definite"):
+        next(gen)
+
+
+# -------------------------------------------------------------- variates
+
+
+def test_philox_normals_vs_oracle(g):
+    import torch
+
+    r = g.rng.Generator(1234)
+    z = r.complex_normal(50_000, sid=7, offset=100).cpu().numpy()
+    zo = orng.complex_normals(1234, 7, 100, 50_000)
+    assert rel_err(z, zo) < 1e-13
+    z32 = r.complex_normal(50_000, sid=7, offset=100, dtype=torch.complex64).cpu().numpy()
+    assert np.max(np.abs(z32 - zo)) < 2e-5  # 24-bit uniforms, FP32 Box-Muller
+
+
+# --------------------------------------------------------- transforms
+
+
+@pytest.mark.parametrize(("nside", "lmax"), [(1, 2), (2, 3), (4, 11), (8, 7), (16, 40), (32, 64),
+                                             (64, 128), (64, 200)])
+def test_alm2map_plain_vs_oracle(g, nside, lmax):
+    alm = random_alm(lmax, seed=lmax, nmaps=3)
+    got = g.healpix.alm2map(list(alm), nside, pol=False)
+    ref = osht.alm2map(alm, nside, lmax)
+    assert rel_err(got, ref) < TOL
+
+
+def test_alm2map_plain_vs_direct_sum(g):
+    nside, lmax = 8, 20
+    alm = random_alm(lmax, seed=5)
+    assert rel_err(g.healpix.alm2map(alm, nside), osht.alm2map_direct(alm, nside, lmax)) < TOL
+
+
+def test_alm2map_extended_range(g):
+    """lmax >> nside: high-m, near-pole values need the scaled recurrence."""
+    nside, lmax = 32, 1000
+    alm = random_alm(lmax, seed=9)
+    got = g.healpix.alm2map(alm, nside)
+    ref = osht.alm2map(alm, nside, lmax)
+    assert rel_err(got, ref) < TOL
+
+
+@pytest.mark.parametrize("spin", [1, 2])
+@pytest.mark.parametrize(("nside", "lmax"), [(4, 11), (16, 40), (32, 95)])
+def test_alm2map_spin_vs_oracle(g, spin, nside, lmax):
+    e = random_alm(lmax, seed=1)
+    b = random_alm(lmax, seed=2)
+    q, u = g.healpix.alm2map_spin([e, b], nside, spin, lmax)
+    qo, uo = osht.alm2map_spin([e, b], nside, spin, lmax)
+    assert rel_err(q, qo) < 1e-11
+    assert rel_err(u, uo) < 1e-11
+
+
+@pytest.mark.parametrize("niter", [0, 3])
+def test_map2alm_vs_oracle(g, niter):
+    nside, lmax = 16, 47
+    rng = np.random.default_rng(3)
+    m = rng.standard_normal(12 * nside * nside)
+    got = g.healpix.map2alm(m, lmax=lmax, iter=niter)
+    ref = osht.map2alm(m, lmax, iter=niter)
+    assert rel_err(got, ref) < 1e-11
+
+
+def test_map2alm_roundtrip(g):
+    nside, lmax = 32, 40
+    alm = random_alm(lmax, seed=11)
+    m = g.healpix.alm2map(alm, nside)
+    back = g.healpix.map2alm(m, lmax=lmax, iter=3)
+    assert rel_err(back, alm) < 1e-7
+
+
+def test_almxfl_and_multalm(g, golden):
+    np.testing.assert_array_equal(g.multalm(golden["multalm_alm"], golden["multalm_bl"]),
+                                  golden["multalm_out"])
+    # reference test values (tests/core/test_harmonics.py:15-52)
+    np.testing.assert_array_equal(g.multalm(np.array([1.0, 2, 3, 4, 5, 6]), np.array([2.0, 0.5, 1.0])),
+                                  [2.0, 1.0, 1.5, 4.0, 5.0, 6.0])
+    np.testing.assert_array_equal(g.multalm(np.array([1.0, 2, 3, 4, 5, 6]), np.array([0.0, 1.0, 0.0])),
+                                  [0.0, 2.0, 3.0, 0.0, 0.0, 0.0])
+    assert g.multalm(np.array([]), np.array([])).shape == (0,)
+    alm = random_alm(30, seed=4)
+    fl = np.random.default_rng(0).standard_normal(25)
+    np.testing.assert_array_equal(g.healpix.almxfl(alm, fl), osht.almxfl(alm, fl))
+
+
+# ------------------------------------------------------- field generation
+
+
+@pytest.mark.parametrize("tag,ncorr", [("all", None), ("nc1", 1)])
+def test_generate_vs_reference_fixture(g, golden, tag, ncorr):
+    gls3 = [golden[f"gls3_{i}"] for i in range(6)]
+    fields = [g.grf.Lognormal(1.0), g.grf.Lognormal(0.7), g.grf.Normal()]
+    maps = np.stack(list(g.generate(fields, gls3, 8, ncorr=ncorr, rng=np.random.default_rng(42))))
+    assert rel_err(maps, golden[f"generate_maps_{tag}"]) < TOL
+
+
+def test_generate_lognormal_vs_reference_fixture(g, golden):
+    gls4 = [golden[f"gls4_{i}"] for i in range(10)]
+    with pytest.deprecated_call():
+        maps = np.stack(list(g.generate_lognormal(gls4, 4, rng=np.random.default_rng(7))))
+    assert rel_err(maps, golden["lognormal4_maps"]) < TOL
+
+
+def test_correlated_alm_vs_reference_fixture(g, golden):
+    from glass_gb300 import fields
+
+    gls3 = [golden[f"gls3_{i}"] for i in range(6)]
+    b = fields._FieldBatcher(gls3, 8, None, np.random.default_rng(42), "plain")
+    alm = np.stack([b.alm(t, 1)[0].cpu().numpy() for t in range(3)])
+    np.testing.assert_allclose(alm, golden["generate_alm_all"], rtol=0, atol=1e-15)
+
+
+def test_generate_philox_vs_oracle(g):
+    """Config-1 sizes (3 shells, nside 64, lmax 128) with the device stream."""
+    gls = spectra_cfg1(3, 128)
+    r = g.rng.Generator(42)
+    maps = np.stack(list(g.generate_lognormal(gls, 64, rng=r)))
+    sid0 = 0
+    ref = np.stack(list(of.generate_lognormal(
+        gls, 64, [1.0] * 3, z_of_shell=lambda t, s: orng.complex_normals(42, sid0 + t, 0, s))))
+    assert rel_err(maps, ref) < TOL
+
+
+def test_generate_batched_matches_per_shell(g):
+    """Batched shells (one SHT launch) equal shell-by-shell results."""
+    gls, lam = spectra_cfg2(6, 64, seed=2)
+    fields = [g.grf.Lognormal(float(x)) for x in lam]
+    a = np.stack(list(g.generate(fields, gls, 32, rng=g.rng.Generator(5))))
+    import os
+
+    os.environ["GLASS_GB300_BATCH_BYTES"] = "1"
+    try:
+        b = np.stack(list(g.generate(fields, gls, 32, rng=g.rng.Generator(5))))
+    finally:
+        del os.environ["GLASS_GB300_BATCH_BYTES"]
+    assert rel_err(a, b) < 1e-14
+
+
+def test_generate_custom_callables(g):
+    """glass tests/core/test_fields.py:403-438: x and x**2 of the same field."""
+    fields = [lambda x, var: x, lambda x, var: x**2]
+    gls = [np.ones(10), np.ones(10), np.ones(10)]
+    res = list(g.generate(fields, gls, nside=16))
+    assert len(res) == 2 and all(r.shape == (12 * 16 * 16,) for r in res)
+    np.testing.assert_allclose(res[1], res[0] ** 2, atol=1e-5)
+    assert len(list(g.generate(fields, gls, nside=16, ncorr=1))) == 2
+
+
+def test_generate_grf_ncorr_invariance(g):
+    from glass_gb300 import fields
+
+    gls = [np.asarray([1.0, 0.5, 0.1])]
+    a = list(fields._generate_grf(gls, 4, rng=np.random.default_rng(42)))
+    b = list(fields._generate_grf(gls, 4, ncorr=1, rng=np.random.default_rng(42)))
+    np.testing.assert_array_equal(a[0], b[0])
+    with pytest.raises(ValueError, match="all gls are empty"):
+        list(fields._generate_grf([np.asarray([])], 4))
+
+
+def test_generate_not_posdef_raises_at_shell(g):
+    gls = [np.ones(4), np.ones(4), np.ones(4) * 5.0]  # C10 > sqrt(C00 C11)
+    gen = g.generate([g.grf.Normal(), g.grf.Normal()], gls, 4, rng=np.random.default_rng(1))
+    first = next(gen)
+    assert first.shape == (192,)
+    with pytest.raises(ValueError, match="not positive definite"):
+        next(gen)
+
+
+def test_torch_in_torch_out(g):
+    import torch
+
+    gls = [torch.as_tensor(c, device="cuda") for c in spectra_cfg1(2, 16)]
+    maps = list(g.generate([g.grf.Lognormal(), g.grf.Lognormal()], gls, 8))
+    assert all(isinstance(m, torch.Tensor) and m.is_cuda for m in maps)
+
+
+# --------------------------------------------------------------- lensing
+
+
+def test_from_convergence_vs_oracle(g):
+    nside = 16
+    rng = np.random.default_rng(0)
+    kappa = rng.random(12 * nside * nside) * 10
+    assert g.from_convergence(kappa) == ()
+    psi, alpha, gamma = g.from_convergence(kappa, potential=True, deflection=True, shear=True,
+                                           discretized=False)
+    lmax = 3 * nside - 1
+    alm = osht.map2alm(kappa, lmax, iter=3)
+    ell = np.arange(lmax + 1, dtype=float)
+    fl = np.zeros_like(ell)
+    fl[1:] = -2 / (ell[1:] * (ell[1:] + 1))
+    alm = osht.almxfl(alm, fl)
+    np.testing.assert_allclose(psi, osht.alm2map(alm, nside, lmax), rtol=0, atol=1e-10 * np.abs(psi).max())
+    alm = osht.almxfl(alm, np.sqrt(ell * (ell + 1)))
+    a0, a1 = osht.alm2map_spin([alm, None], nside, 1, lmax)
+    assert rel_err(alpha, a0 + 1j * a1) < 1e-10
+    fl = np.zeros_like(ell)
+    fl[1:] = np.sqrt((ell[1:] - 1) * (ell[1:] + 2)) / 2
+    alm = osht.almxfl(alm, fl)
+    g0, g1 = osht.alm2map_spin([alm, None], nside, 2, lmax)
+    assert rel_err(gamma, g0 + 1j * g1) < 1e-10
+    for combo in ((True, False, False), (False, True, False), (False, False, True),
+                  (True, True, False), (True, False, True), (False, True, True)):
+        res = g.from_convergence(kappa, potential=combo[0], deflection=combo[1], shear=combo[2],
+                                 discretized=False)
+        assert len(res) == sum(combo)

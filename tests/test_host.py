@@ -1,0 +1,100 @@
+"""CPU tests of the host-side logic mirroring glass/fields.py (no GPU calls)."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import glass_gb300 as g
+from glass_gb300 import fields
+
+
+def test_cls2cov_values_and_buffer_reuse():
+    # glass tests/core/test_fields.py:166-252 semantics
+    gen = g.cls2cov([np.asarray([1.0, 0.5, 0.3]), None, np.asarray([0.7, 0.6, 0.1])], 3, 2, 2)
+    cov = next(gen)
+    assert cov.shape == (3, 3)
+    np.testing.assert_array_equal(cov[:, 0], [0.5, 0.25, 0.15])
+    np.testing.assert_array_equal(cov[:, 1:], 0.0)
+    with pytest.raises(ValueError, match="negative values in cl"):
+        next(g.cls2cov([np.asarray([-1.0, 0.5, 0.3]), np.ones(3), np.ones(3)], 3, 3, 2))
+    cls = [np.asarray(a) for a in ([1.0, 0.5, 0.3], [0.8, 0.4, 0.2], [0.7, 0.6, 0.1],
+                                   [0.9, 0.5, 0.3], [0.6, 0.3, 0.2], [0.8, 0.7, 0.4])]
+    gen = g.cls2cov(cls, 3, 3, 2)
+    c1 = next(gen)
+    c1c = c1.copy()
+    c2 = next(gen)
+    c3 = next(gen)
+    np.testing.assert_array_equal(c1[:, 0], [0.45, 0.25, 0.15])
+    np.testing.assert_array_equal(c1, c3)
+    np.testing.assert_array_equal(c2, c3)
+    np.testing.assert_array_equal(c1c[:, 0], [0.5, 0.25, 0.15])
+
+
+def test_cls2cov_matches_golden(golden):
+    gls6 = [golden[f"gls6_{i}"] for i in range(21)]
+    got = np.stack([c.copy() for c in g.cls2cov(gls6, 41, 6, 5)])
+    np.testing.assert_array_equal(got, golden["cls2cov_cfg2_nc5"])
+
+
+def test_triangle_numbers():
+    for n in range(2000):
+        assert g.nfields_from_nspectra(n * (n + 1) // 2) == n
+    for t in [2, 4, 5, 7, 8, 9, 11]:
+        with pytest.raises(ValueError, match=f"invalid number of spectra: {t}"):
+            g.nfields_from_nspectra(t)
+        with pytest.raises(ValueError, match=f"not a triangle number: {t}"):
+            fields._inv_triangle_number(t)
+
+
+def test_getcl_and_enumerate():
+    cls = [np.asarray([i, j], dtype=float) for i in range(6) for j in range(i, -1, -1)]
+    for i in range(6):
+        for j in range(6):
+            np.testing.assert_array_equal(np.sort(g.getcl(cls, i, j)), [min(i, j), max(i, j)])
+            assert g.getcl(cls, i, j, lmax=0).shape == (1,)
+            r = g.getcl(cls, i, j, lmax=20)
+            assert r.shape == (21,)
+            np.testing.assert_array_equal(r[2:], 0)
+    idx = [(i, j) for i in range(5) for j in range(i, -1, -1)]
+    assert [(a, b) for a, b, _ in g.enumerate_spectra(range(15))] == idx
+    np.testing.assert_array_equal(g.spectra_indices(3), [[0, 0], [1, 1], [1, 0], [2, 2], [2, 1], [2, 0]])
+
+
+def test_glass_to_healpix_alm_numpy():
+    inp = np.asarray([0, 10, 11, 20, 21, 22, 30, 31, 32, 33], dtype=np.complex128)
+    np.testing.assert_array_equal(fields._glass_to_healpix_alm(inp),
+                                  [0, 10, 20, 30, 11, 21, 31, 22, 32, 33])
+
+
+def test_generate_field_count_error():
+    fs = [lambda x, v: x, lambda x, v: x]
+    with pytest.raises(ValueError, match="mismatch between number of fields and gls"):
+        list(g.generate(fs, [np.ones(10), np.ones(10)], nside=16))
+
+
+def test_iternorm_empty_error():
+    with pytest.raises(ValueError, match="empty covariance"):
+        list(g.iternorm([np.ones(0)]))
+
+
+def test_transformations():
+    x = np.linspace(-2, 2, 11)
+    np.testing.assert_array_equal(g.grf.Normal()(x, 1.0), x)
+    np.testing.assert_array_equal(g.grf.Lognormal(1.0)(x, 0.3), np.expm1(x - 0.15))
+    np.testing.assert_array_equal(g.grf.Lognormal(0.7)(x, 0.3), 0.7 * np.expm1(x - 0.15))
+    np.testing.assert_array_equal(g.grf.SquaredNormal(0.5, 2.0)(x, 0.3), 2.0 * ((x - 0.5) ** 2 - 1))
+    assert g.grf.fused_kind(g.grf.Lognormal(0.7)) == ("lognormal", 0.7)
+    assert g.grf.fused_kind(g.grf.Normal()) == ("normal", 1.0)
+    assert g.grf.fused_kind(lambda x, v: x) is None
+
+
+def test_no_cpu_fallback_without_gpu():
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("GPU present")
+    from glass_gb300 import _lib
+
+    with pytest.raises(RuntimeError, match="no CPU fallback"):
+        _lib.lib()

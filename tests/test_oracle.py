@@ -1,0 +1,141 @@
+"""CPU tests of the oracle: pinned against brute force, KATs and the reference."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import oracle.fields as of
+import oracle.rng as orng
+import oracle.sht as osht
+from tests.conftest import random_alm, rel_err
+
+
+@pytest.mark.parametrize(("nside", "lmax"), [(1, 2), (2, 5), (4, 11), (8, 20), (8, 30)])
+def test_alm2map_matches_direct_sum(nside, lmax):
+    alm = random_alm(lmax, seed=nside + lmax)
+    assert rel_err(osht.alm2map(alm, nside, lmax), osht.alm2map_direct(alm, nside, lmax)) < 1e-13
+
+
+@pytest.mark.parametrize("spin", [1, 2])
+@pytest.mark.parametrize(("nside", "lmax"), [(2, 6), (4, 11), (8, 16)])
+def test_spin_matches_goldberg(spin, nside, lmax):
+    e = random_alm(lmax, seed=1)
+    b = random_alm(lmax, seed=2)
+    q, u = osht.alm2map_spin([e, b], nside, spin, lmax)
+    qd, ud = osht.alm2map_spin_direct(e, b, nside, spin, lmax)
+    assert rel_err(q, qd) < 1e-11
+    assert rel_err(u, ud) < 1e-11
+
+
+def test_known_answers():
+    nside, lmax = 8, 4
+    theta, _ = osht.pix_angles(nside)
+    a = np.zeros(osht.nalm(lmax), complex)
+    a[0] = 2.0
+    np.testing.assert_allclose(osht.alm2map(a, nside, lmax), 2 / np.sqrt(4 * np.pi), rtol=1e-14)
+    a[:] = 0
+    a[osht.alm_index(1, 0, lmax)] = 1.5
+    np.testing.assert_allclose(osht.alm2map(a, nside, lmax),
+                               1.5 * np.sqrt(3 / (4 * np.pi)) * np.cos(theta), atol=1e-14)
+
+
+def test_map2alm_roundtrip():
+    nside, lmax = 16, 16
+    alm = random_alm(lmax, seed=3)
+    m = osht.alm2map(alm, nside, lmax)
+    assert rel_err(osht.map2alm(m, lmax, iter=3), alm) < 1e-6
+
+
+def test_extended_range_large_m():
+    """High-m modes on near-polar rings underflow FP64 without the exponent scale."""
+    nside, lmax = 64, 400
+    alm = np.zeros(osht.nalm(lmax), complex)
+    for m in (300, 350, 399):
+        alm[osht.alm_index(lmax, m, lmax)] = 1.0
+    F = osht.alm2ring(alm, nside, lmax)
+    assert np.all(np.isfinite(F))
+    assert np.abs(F).max() > 1e-3  # non-negligible near the equator
+
+
+def test_philox_known_answers():
+    # Random123 Philox4x32-10 published known-answer vectors
+    np.testing.assert_array_equal(orng.philox4x32_10([0, 0, 0, 0], [0, 0]),
+                                  [0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8])
+    np.testing.assert_array_equal(orng.philox4x32_10([0xFFFFFFFF] * 4, [0xFFFFFFFF] * 2),
+                                  [0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD])
+    np.testing.assert_array_equal(
+        orng.philox4x32_10([0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344], [0xA4093822, 0x299F31D0]),
+        [0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1])
+
+
+def test_philox_normals_moments():
+    z = orng.complex_normals(42, 3, 0, 100_000)
+    assert abs(z.real.mean()) < 0.02 and abs(z.imag.mean()) < 0.02
+    assert abs(z.real.std() - 1) < 0.02 and abs(z.imag.std() - 1) < 0.02
+    z2 = orng.complex_normals(42, 3, 500, 10)
+    np.testing.assert_array_equal(z2, z[500:510])
+
+
+# ------------------------------------------------- pinned to the reference
+
+
+def test_iternorm_matches_reference(golden):
+    for nc in (5, 2):
+        w, bad = of.iternorm_stack(golden[f"cls2cov_cfg2_nc{nc}"])
+        assert bad == -1
+        np.testing.assert_allclose(w, golden[f"iternorm_cfg2_nc{nc}"], rtol=1e-13, atol=1e-16)
+
+
+@pytest.mark.parametrize("k", [0, 1, 2])
+@pytest.mark.parametrize("nd", ["0d", "nd"])
+def test_iternorm_reference_test_matrices(golden, k, nd):
+    rows = [golden[f"iternorm_k{k}_{nd}_in{i}"] for i in range(3)]
+    kmax = max(r.shape[-1] for r in rows) - 1
+    stack = np.zeros((3,) + rows[0].shape[:-1] + (kmax + 1,))
+    for i, r in enumerate(rows):
+        stack[i, ..., : r.shape[-1]] = r
+    stack = stack.reshape(3, -1, kmax + 1)
+    w, bad = of.iternorm_stack(stack)
+    for i, r in enumerate(rows):
+        kk = r.shape[-1] - 1
+        ref = golden[f"iternorm_k{k}_{nd}_row{i}"].reshape(-1, kk + 1)
+        np.testing.assert_allclose(w[i][:, kmax - kk:], ref, rtol=1e-13, atol=1e-16)
+
+
+def test_iternorm_not_posdef():
+    cov = np.array([[[1.0, 0.0]], [[0.1, 1.0]]])  # second row: var 0.1 < corr^2
+    _, bad = of.iternorm_stack(cov)
+    assert bad == 1
+
+
+def test_cls2cov_matches_reference(golden):
+    gls6 = [golden[f"gls6_{i}"] for i in range(21)]
+    for nc in (5, 2):
+        got = np.stack([c.copy() for c in of.cls2cov(gls6, 41, 6, nc)])
+        np.testing.assert_array_equal(got, golden[f"cls2cov_cfg2_nc{nc}"])
+
+
+@pytest.mark.parametrize("tag,ncorr", [("all", None), ("nc1", 1)])
+def test_generate_alm_matches_reference(golden, tag, ncorr):
+    gls3 = [golden[f"gls3_{i}"] for i in range(6)]
+    alm = np.stack(list(of.generate_grf_alm(gls3, ncorr=ncorr)))
+    np.testing.assert_allclose(alm, golden[f"generate_alm_{tag}"], rtol=0, atol=1e-15)
+
+
+def test_generate_lognormal_matches_reference(golden):
+    gls4 = [golden[f"gls4_{i}"] for i in range(10)]
+    rng = np.random.default_rng(7)
+    maps = np.stack(list(of.generate_lognormal(
+        gls4, 4, [1.0] * 4, z_of_shell=lambda t, s: rng.standard_normal((s, 2)) @ np.asarray([1, 1j]))))
+    np.testing.assert_allclose(maps, golden["lognormal4_maps"], rtol=1e-13, atol=1e-15)
+
+
+def test_multalm_and_reorder_match_reference(golden):
+    np.testing.assert_array_equal(of.multalm(golden["multalm_alm"], golden["multalm_bl"]),
+                                  golden["multalm_out"])
+    np.testing.assert_array_equal(of.glass_to_healpix_alm(golden["reorder_in"]), golden["reorder_out"])
+    # the reference's own permutation test (tests/core/test_fields.py:649-655)
+    inp = np.array([0, 10, 11, 20, 21, 22, 30, 31, 32, 33], dtype=complex)
+    np.testing.assert_array_equal(of.glass_to_healpix_alm(inp),
+                                  np.array([0, 10, 20, 30, 11, 21, 31, 22, 32, 33], dtype=complex))
