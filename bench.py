@@ -1,0 +1,319 @@
+"""Benchmark: lognormal shell maps per second at nside 2048 (40 shells, lmax 4096).
+
+One step = one call of ``glass_gb300.generate`` producing 40 correlated
+lognormal shell maps (HEALPix nside 2048, lmax 4096, float32 maps, complex64
+alm) from their Gaussian angular power spectra: iternorm, Philox variates,
+correlated alm, tensor-core Legendre contraction, ring FFTs and the fused
+lognormal transform.  Synthetic spectra: C_l^ii = A_i (l+1)^-1.3 with A_i
+log-uniform in [1e-3, 1e-1], correlation exp(-|i-j|/3), shifts uniform in
+[0.5, 3], all from seed 0.
+
+Printed JSON (one line, rank 0):
+  value  -- shell-maps/s with spectra and maps resident on the device,
+  e2e    -- the same through the public API from host (numpy) spectra to host
+            (numpy) maps, copies inside the timed region,
+  plain  -- the FP64 drop-in form on the same workload, and the fast form's
+            relative RMS map error against it,
+  roofline / gpu_launches / clocks / cpu_baseline as described in the design doc.
+
+``--impl reference`` times the CPU restatement of the reference's path
+(oracle/: GLASS glue + FP64 ring SHT with all host threads) on a bounded
+sample of the same workload.  Multi-GPU (torchrun): replicas only -- every
+rank runs the full workload; value = shells of all ranks / max time.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import pathlib
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "shell-maps/sec and pixels/sec at nside 2048 vs plain FP64 GPU @1e-6; p50/p99 latency"
+UNIT = "shell-maps/s"
+WORKLOAD = dict(workload="40-shell lognormal field generation (configs[2])", nshell=40, nside=2048,
+                lmax=4096)
+
+
+def spectra_cfg3(nshell: int, lmax: int, seed: int = 0):
+    rng = np.random.default_rng(seed)
+    amp = 10 ** rng.uniform(-3, -1, nshell)
+    lam = rng.uniform(0.5, 3.0, nshell)
+    ell = np.arange(lmax + 1)
+    auto = [a * (ell + 1.0) ** -1.3 for a in amp]
+    gls = [np.exp(-abs(i - j) / 3.0) * np.sqrt(auto[i] * auto[j])
+           for i in range(nshell) for j in range(i, -1, -1)]
+    return gls, lam
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    def __init__(self, index: int = 0):
+        self.index = index
+        self.rows: list[list[str]] = []
+        self.proc = None
+        self.thread = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[0]))
+                mx.append(float(r[1]))
+                for n, v in zip(names, r[3:7]):
+                    if v.lower() in ("active", "1", "yes"):
+                        reasons.add(n)
+            except (ValueError, IndexError):
+                pass
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return json.loads(p.read_text())
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "fallback": True}
+
+
+def tf32_peak_tflops(peaks: dict) -> tuple[float, str]:
+    """Dense TF32 tensor peak: half the measured dense bf16 rate (same tensor
+    pipe, tf32 issues at half the bf16 rate on this generation)."""
+    bf = peaks.get("bf16_tflops", 1900.0)
+    tag = "of measured" if "fallback" not in peaks else "of fallback"
+    return bf / 2.0, f"tf32 = bf16_tflops/2 ({tag})"
+
+
+# ------------------------------------------------------------------- ours
+
+
+def run_ours(args, rank: int, world: int) -> dict | None:
+    import torch
+
+    import glass_gb300 as g
+    from glass_gb300 import _lib
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    torch.cuda.set_device(dev)
+    nshell, nside, lmax = args.nshell, args.nside, args.lmax
+    gls_np, lam = spectra_cfg3(nshell, lmax)
+    gls_dev = [torch.as_tensor(c, device=dev) for c in gls_np]
+    fields = [g.grf.Lognormal(float(x)) for x in lam]
+    npix = 12 * nside * nside
+
+    def step_device(form="fast"):
+        out = list(g.generate(fields, gls_dev, nside, rng=g.rng.Generator(42), form=form))
+        return out
+
+    # warm-up (plan tables, seeds, allocator)
+    for _ in range(args.warmup):
+        step_device()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    _lib.timing_reset()
+    launches0 = _lib.launch_count()
+    stream = torch.cuda.current_stream()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev.index) as clk:
+        torch.cuda.synchronize()
+        t0.record(stream)
+        for _ in range(args.steps):
+            step_device()
+        t1.record(stream)
+        torch.cuda.synchronize()
+    ms = t0.elapsed_time(t1)
+    launches = _lib.launch_count() - launches0
+    if world > 1:
+        tt = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        ms = float(tt.item())
+    ms_step = ms / args.steps
+    value = world * nshell / (ms_step / 1e3)
+
+    # per-kernel timing of the dominant kernel (one extra step, events per launch)
+    _lib.timing_enable(True)
+    _lib.timing_reset()
+    step_device()
+    torch.cuda.synchronize()
+    kt = {k: _lib.kernel_time(k) for k in ("k_leg_tc", "k_pack_b", "k_ring_syn", "k_alm_correlate",
+                                           "k_iternorm")}
+    _lib.timing_enable(False)
+    leg_ms, leg_n = kt["k_leg_tc"]
+    nalm = (lmax + 1) * (lmax + 2) // 2
+    flops = 4.0 * nalm * 2 * nside * nshell  # algorithmic, dense (Legendre contraction)
+    peaks = measured_peaks()
+    peak_tf, peak_note = tf32_peak_tflops(peaks)
+    achieved = flops / (leg_ms / max(leg_n, 1) / 1e3) / 1e12 if leg_ms > 0 else None
+    roofline = {"bound": "tensor", "kernel": "k_leg_tc", "achieved": achieved, "peak": peak_tf,
+                "unit": "TFLOP/s", "frac": (achieved / peak_tf) if achieved else None,
+                "traffic": None, "peak_note": peak_note, "passes": 3,
+                "issued_frac": (3 * achieved / peak_tf) if achieved else None,
+                "algorithmic_flops_per_launch": flops}
+    if rank != 0:
+        return None
+
+    # plain FP64 form on the same workload, and the fast form's error against it
+    plain = {}
+    if args.plain_steps > 0:
+        torch.cuda.synchronize()
+        a = time.perf_counter()
+        pm = step_device("plain")
+        torch.cuda.synchronize()
+        plain_s = time.perf_counter() - a
+        fm = step_device("fast")
+        errs = []
+        for x, y in zip(fm, pm):
+            d = x.double() - y
+            errs.append(float(torch.sqrt(torch.mean(d * d)) / torch.sqrt(torch.mean(y * y))))
+        plain = {"value": nshell / plain_s, "unit": UNIT, "ms_per_step": plain_s * 1e3,
+                 "fast_vs_plain_rel_rms_max": max(errs), "fast_vs_plain_rel_rms_median": float(np.median(errs)),
+                 "speedup": (nshell / plain_s) and value / (nshell / plain_s)}
+        del pm, fm
+
+    # end to end: numpy spectra in, numpy maps out, through the public API
+    e2e = {}
+    if args.e2e_steps > 0:
+        torch.cuda.synchronize()
+        a = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            maps = list(g.generate(fields, gls_np, nside, rng=g.rng.Generator(42), form="fast"))
+        torch.cuda.synchronize()
+        e_s = (time.perf_counter() - a) / args.e2e_steps
+        e2e = {"value": nshell / e_s, "unit": UNIT, "ms_per_step": e_s * 1e3,
+               "h2d_bytes_per_step": int(sum(c.nbytes for c in gls_np)),
+               "d2h_bytes_per_step": int(sum(m.nbytes for m in maps))}
+        del maps
+
+    cpu = cpu_baseline(args) if args.cpu_baseline else None
+    res = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 maps / 3xtf32 contraction / f64 recurrence seeds",
+        "data": "synthetic spectra (seeded), Philox variates",
+        "config": dict(WORKLOAD, form="fast", l2="inputs/outputs larger than L2 (maps 8 GB/step)",
+                       parallelism="replicas" if world > 1 else "1 gpu"),
+        "pixels_per_sec": value * npix, "e2e": e2e, "plain_fp64": plain, "roofline": roofline,
+        "kernel_ms": {k: v[0] / max(v[1], 1) for k, v in kt.items()}, "gpu_launches": launches,
+        "clocks": clk.summary(), "cpu_baseline": cpu,
+    }
+    return res
+
+
+def cpu_baseline(args) -> dict:
+    """The oracle (GLASS glue + FP64 ring SHT, all host threads) on a 1-shell
+    sample of the same workload; value in shell-maps/s."""
+    import oracle
+    import oracle.fields as of
+    import oracle.rng as orng
+
+    gls, lam = spectra_cfg3(args.nshell, args.lmax)
+    sample = max(1, args.cpu_shells)
+    a = time.perf_counter()
+    it = of.generate_lognormal(gls, args.nside, list(lam), ncorr=None,
+                               z_of_shell=lambda t, s: orng.complex_normals(42, t, 0, s))
+    for _ in range(sample):
+        next(it)
+    dt = time.perf_counter() - a
+    return {"value": sample / dt, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
+            "sample": f"{sample} of {args.nshell} shells at nside {args.nside}, lmax {args.lmax} "
+                      "(iternorm of all shells, Philox variates, C Legendre sums, numpy ring FFTs)"}
+
+
+# -------------------------------------------------------------- reference
+
+
+def run_reference(args, rank: int, world: int) -> dict | None:
+    if rank != 0:
+        return None
+    args.cpu_shells = 1
+    vals = []
+    for _ in range(max(args.warmup, 0)):
+        pass  # the oracle has no device state to warm
+    for _ in range(args.steps):
+        r = cpu_baseline(args)
+        vals.append(r["value"])
+    v = float(np.median(vals))
+    return {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 / v, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic spectra (seeded)",
+            "config": dict(WORKLOAD, form="cpu port"), "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": r["cores"], "kind": "port",
+                             "sample": r["sample"]},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--nshell", type=int, default=40)
+    ap.add_argument("--nside", type=int, default=2048)
+    ap.add_argument("--lmax", type=int, default=4096)
+    ap.add_argument("--plain-steps", type=int, default=1)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--cpu-shells", type=int, default=1)
+    ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1 and args.impl == "ours":
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    if args.impl == "reference":
+        res = run_reference(args, rank, world)
+    else:
+        res = run_ours(args, rank, world)
+    if rank == 0 and res is not None:
+        print(json.dumps(res))
+    if world > 1 and args.impl == "ours":
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -119,10 +119,15 @@ __device__ __forceinline__ double2 philox_cnormal_f64(uint64_t seed, uint64_t si
 __device__ __forceinline__ float2 philox_cnormal_f32(uint64_t seed, uint64_t sid, uint64_t e) {
     const U4 x = philox4x32_10((uint32_t)e, (uint32_t)(e >> 32), (uint32_t)sid,
                                (uint32_t)(sid >> 32), (uint32_t)seed, (uint32_t)(seed >> 32));
-    // 24-bit uniforms in (0, 1) from the same high bits as the FP64 form
-    const float u1 = ((float)(x.x >> 8) + 0.5f) * 5.9604644775390625e-08f;
-    const float u2 = ((float)(x.z >> 8) + 0.5f) * 5.9604644775390625e-08f;
-    const float r = sqrtf(-2.0f * logf(u1));
+    // the FP64 form's 53-bit uniforms rounded to FP32 (relative error ~1e-7
+    // even deep in the tails, where u1 is small)
+    const float u1 = fmaf((float)(x.x >> 5), 67108864.0f, (float)(x.y >> 6) + 0.5f) * 1.1102230246251565e-16f;
+    const float u2 = fmaf((float)(x.z >> 5), 67108864.0f, (float)(x.w >> 6) + 0.5f) * 1.1102230246251565e-16f;
+    // 1 - u1 from the integer bits, so that log(u1) stays accurate near u1 = 1
+    const float v1 = fmaf((float)(0x7FFFFFFu - (x.x >> 5)), 67108864.0f,
+                          (float)(0x3FFFFFFu - (x.y >> 6)) + 0.5f) * 1.1102230246251565e-16f;
+    const float lg = u1 < 0.5f ? logf(u1) : log1pf(-v1);
+    const float r = sqrtf(-2.0f * lg);
     float sn, cs;
     sincospif(2.0f * u2, &sn, &cs);
     return make_float2(r * cs, r * sn);

@@ -72,7 +72,22 @@ struct glg_plan {
     int *fft_nst;            // [nside+1]
     int64_t *tw_ofs;         // [nside+1] offset of the table of length i
     double2 *tw;             // tw[ofs_i + t] = exp(i pi t / (4 i)), t < 8 i
+
+    // fast-form tables (built on first use by glg_plan_prepare_fast)
+    bool fast_ready;
+    float *cth32;            // [npairs]
+    float2 *tw32;            // FP32 copy of tw
+    float2 *coef32;          // [nalm] FP32 (A, B)
+    int64_t *goff;           // [mmax+2] first 16-l group of m: sum_{m'<m} ceil((lmax-m'+1)/16)
+    int64_t ngroups;         // total groups
+    float2 *seeds;           // [ngroups][npairs] (lambda_s0, lambda_s0+1) per group
+    int *lstart;             // [mmax+1][npairs] first l with |lambda| >= 2^-100
 };
+
+// l values per group of the fast Legendre contraction (8 even + 8 odd)
+#define GLG_GROUP 16
+
+int glg_plan_prepare_fast(glg_plan *P, cudaStream_t st);
 
 // ---------------------------------------------------------- device helpers
 
@@ -97,3 +112,11 @@ int glg_launch_ring_ana(const glg_plan *P, const double *maps, int nmaps, double
                         cudaStream_t st);
 int glg_launch_leg_ana(const glg_plan *P, const double2 *G, int nmaps, double2 *alm, int accumulate,
                        cudaStream_t st);
+int glg_launch_ring_syn_f32(const glg_plan *P, const float2 *F, int nmaps, float *maps,
+                            const glg_epilogue *epi, cudaStream_t st);
+size_t glg_leg_tc_pack_bytes(const glg_plan *P, int nmaps);
+int glg_launch_leg_tc(const glg_plan *P, const float2 *alm, int nmaps, float *bpack, float2 *F,
+                      int *err, cudaStream_t st);
+
+// Fast-form workspace: [status ints | B pack | F (float2 [map][m][ring])]
+#define GLG_WS_STATUS_BYTES 256

@@ -1,0 +1,394 @@
+// Fast form of the Legendre sums: a shells-batched contraction on the
+// sm_103a tensor cores (tcgen05, split-precision 3xTF32, FP32 accumulation).
+//
+// For one ring tile (128 ring pairs, one per TMEM lane) and one m:
+//   D_E[p][n] = sum_{l-m even} lambda_lm(x_p) B[l][n],
+//   D_O[p][n] = sum_{l-m odd}  lambda_lm(x_p) B[l][n],
+// with n = 2 * map + (0: re, 1: im); north F = D_E + D_O, south F = D_E - D_O
+// (lambda_lm(-x) = (-1)^(l+m) lambda_lm(x)).  This is the work healpy does
+// inside alm2map (glass/healpix.py:71, called from glass/fields.py:429).
+//
+// lambda is generated on the fly in FP32 by the producer warps, restarting
+// every 16 l from seeds computed once per plan by an FP64 recurrence, split
+// into TF32 hi + lo parts and written straight into tensor memory (the MMA's
+// A operand).  B (the alm, split the same way) is packed per 16-l group in
+// the canonical no-swizzle K-major layout and streamed into shared memory
+// with 1-D bulk copies.  Each group issues, per parity,
+//   D += A_hi B_hi + A_hi B_lo + A_lo B_hi     (M = 128, N = 2*maps, K = 8).
+//
+// Warp roles (320 threads): warps 0-3 and 4-7 produce lambda for alternate
+// groups (warps 0-3 also drain D after each unit), warp 8 issues the MMAs,
+// warp 9 streams B.  Every wait is bounded; on time-out the kernel records
+// GLG_ERR_TIMEOUT in *err, drains its outstanding MMAs and copies, frees its
+// tensor memory and returns.
+#include <cuda_runtime.h>
+
+#include "glg_internal.cuh"
+#include "tc_ptx.cuh"
+
+using namespace glg_tc;
+
+namespace {
+
+constexpr int NST = 8;            // pipeline stages (A in TMEM, B in smem)
+constexpr int A_COL0 = 256;       // first TMEM column of the A stages
+constexpr int TMEM_COLS = 512;
+constexpr uint32_t WAIT_LIMIT = 1u << 22;
+
+struct LegTcArgs {
+    int npairs, nrings, lmax, nmaps, ntiles;
+    int64_t nunits;
+    const float *cth32;
+    const float2 *coef32;
+    const int64_t *mofs;
+    const int64_t *goff;
+    const float2 *seeds;
+    const int *lstart;
+    const unsigned char *bpack;
+    float2 *F;  // [map][m][ring]
+    int *err;
+};
+
+__device__ __forceinline__ uint32_t tf32_rna(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return r;
+}
+
+__device__ __forceinline__ int unit_m(int64_t mi, int lmax) {
+    return (mi & 1) ? lmax - (int)(mi >> 1) : (int)(mi >> 1);
+}
+
+template <int N>
+struct Smem {
+    unsigned char b[NST][128 * N];
+    uint64_t full_a[NST], full_b[NST], empty[NST];
+    uint64_t done, epi_done, drain;
+    uint32_t tmem_base;
+    int abort;
+};
+
+template <int N>
+__global__ void __launch_bounds__(320, 1) k_leg_tc(const LegTcArgs a) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    Smem<N> &S = *reinterpret_cast<Smem<N> *>(smem_raw);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    constexpr uint32_t BBYTES = 128 * N;
+    constexpr uint32_t IDESC = idesc_tf32(128, N);
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < NST; ++s) {
+            mbar_init(&S.full_a[s], 4);
+            mbar_init(&S.full_b[s], 1);
+            mbar_init(&S.empty[s], 1);
+        }
+        mbar_init(&S.done, 1);
+        mbar_init(&S.epi_done, 4);
+        mbar_init(&S.drain, 1);
+        S.abort = 0;
+        fence_barrier_init();
+    }
+    if (warp == 0) {
+        tmem_alloc(&S.tmem_base, TMEM_COLS);
+        tmem_relinquish();
+    }
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+    const uint32_t tb = S.tmem_base;
+    volatile int *abort_flag = &S.abort;
+    auto fail = [&]() {
+        *abort_flag = 1;
+        atomicExch(a.err, GLG_ERR_TIMEOUT);
+    };
+    auto wait = [&](uint64_t *bar, uint32_t parity) -> bool {
+        for (uint32_t i = 0; i < WAIT_LIMIT; ++i) {
+            if (mbar_try_wait(bar, parity)) return true;
+            if (*abort_flag) return false;
+        }
+        fail();
+        return false;
+    };
+
+    const int lmax = a.lmax;
+    if (warp < 8) {
+        // ---------------------------------------------------- lambda producers
+        const int set = warp >> 2;
+        const int r = ((warp & 3) << 5) + lane;  // TMEM lane = ring pair in tile
+        const uint32_t lane_base = (uint32_t)((warp & 3) << 5) << 16;
+        int64_t gc = 0, ui = 0;
+        bool ok = true;
+        for (int64_t u = blockIdx.x; u < a.nunits && ok; u += gridDim.x, ++ui) {
+            const int tile = (int)(u % a.ntiles);
+            const int m = unit_m(u / a.ntiles, lmax);
+            const int G = (lmax - m + GLG_GROUP) / GLG_GROUP;
+            const int p = tile * 128 + r;
+            const bool live = p < a.npairs;
+            const int pp = live ? p : a.npairs - 1;
+            const float x = a.cth32[pp];
+            const int ls = live ? a.lstart[(int64_t)m * a.npairs + pp] : lmax + 1;
+            const int64_t mb = a.mofs[m];
+            const int64_t gb = a.goff[m];
+            for (int g = 0; g < G; ++g) {
+                const int64_t gg = gc + g;
+                if ((int)(gg & 1) != set) continue;
+                const int s = (int)(gg % NST);
+                const int64_t use = gg / NST;
+                if (use > 0 && !wait(&S.empty[s], (uint32_t)((use - 1) & 1))) { ok = false; break; }
+                fence_after_sync();
+                const int l0 = m + g * GLG_GROUP;
+                const int s0 = l0 > ls ? l0 : ls;
+                float2 seed = make_float2(0.f, 0.f);
+                if (s0 <= l0 + GLG_GROUP - 1 && s0 <= lmax) seed = a.seeds[(gb + g) * a.npairs + pp];
+                float lm2 = 0.f, lm1 = 0.f;
+                uint32_t ehi[8], elo[8], ohi[8], olo[8];
+#pragma unroll
+                for (int j = 0; j < GLG_GROUP; ++j) {
+                    const int l = l0 + j;
+                    float v;
+                    if (l < s0 || l > lmax) {
+                        v = 0.f;
+                    } else if (l == s0) {
+                        v = seed.x;
+                    } else if (l == s0 + 1) {
+                        v = seed.y;
+                    } else {
+                        const float2 ab = __ldg(a.coef32 + mb + (l - m));
+                        v = fmaf(ab.x, x * lm1, -ab.y * lm2);
+                    }
+                    lm2 = lm1;
+                    lm1 = v;
+                    const uint32_t hi = tf32_rna(v);
+                    const uint32_t lo = tf32_rna(v - __uint_as_float(hi));
+                    if (j & 1) {
+                        ohi[j >> 1] = hi;
+                        olo[j >> 1] = lo;
+                    } else {
+                        ehi[j >> 1] = hi;
+                        elo[j >> 1] = lo;
+                    }
+                }
+                const uint32_t col = tb + lane_base + A_COL0 + 32 * s;
+                tmem_st8(col + 0, ehi);
+                tmem_st8(col + 8, elo);
+                tmem_st8(col + 16, ohi);
+                tmem_st8(col + 24, olo);
+                tmem_wait_st();
+                fence_before_sync();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&S.full_a[s]);
+            }
+            gc += G;
+            if (!ok) break;
+            if (set == 0) {
+                // ------------------------------------------------- epilogue
+                if (!wait(&S.done, (uint32_t)(ui & 1))) { ok = false; break; }
+                fence_after_sync();
+                const int rs = a.nrings - 1 - p;
+                for (int c0 = 0; c0 < N; c0 += 16) {
+                    uint32_t e[16], o[16];
+                    tmem_ld16(tb + lane_base + c0, e);
+                    tmem_ld16(tb + lane_base + N + c0, o);
+                    tmem_wait_ld();
+                    if (live) {
+#pragma unroll
+                        for (int j = 0; j < 16; j += 2) {
+                            const int map = (c0 + j) >> 1;
+                            if (map < a.nmaps) {
+                                const float er = __uint_as_float(e[j]), ei = __uint_as_float(e[j + 1]);
+                                const float orr = __uint_as_float(o[j]), oi = __uint_as_float(o[j + 1]);
+                                float2 *Fm = a.F + ((int64_t)map * (lmax + 1) + m) * a.nrings;
+                                Fm[p] = make_float2(er + orr, ei + oi);
+                                if (rs != p) Fm[rs] = make_float2(er - orr, ei - oi);
+                            }
+                        }
+                    }
+                }
+                fence_before_sync();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&S.epi_done);
+            }
+        }
+        if (!ok) fail();
+    } else if (warp == 8) {
+        // ---------------------------------------------------------- MMA issue
+        if (lane == 0) {
+            int64_t gc = 0, ui = 0;
+            bool ok = true;
+            bool issued = false;
+            for (int64_t u = blockIdx.x; u < a.nunits && ok; u += gridDim.x, ++ui) {
+                const int m = unit_m(u / a.ntiles, lmax);
+                const int G = (lmax - m + GLG_GROUP) / GLG_GROUP;
+                if (ui > 0 && !wait(&S.epi_done, (uint32_t)((ui - 1) & 1))) { ok = false; break; }
+                fence_after_sync();
+                for (int g = 0; g < G; ++g) {
+                    const int64_t gg = gc + g;
+                    const int s = (int)(gg % NST);
+                    const uint32_t par = (uint32_t)((gg / NST) & 1);
+                    if (!wait(&S.full_a[s], par) || !wait(&S.full_b[s], par)) { ok = false; break; }
+                    fence_after_sync();
+                    const uint32_t acol = tb + A_COL0 + 32 * s;
+                    const uint32_t bb = smem_u32(S.b[s]);
+                    const uint32_t tsz = 32 * N;  // bytes of one B tile
+                    const uint64_t bEh = sdesc_noswz(bb, 128, 256), bEl = sdesc_noswz(bb + tsz, 128, 256);
+                    const uint64_t bOh = sdesc_noswz(bb + 2 * tsz, 128, 256);
+                    const uint64_t bOl = sdesc_noswz(bb + 3 * tsz, 128, 256);
+                    const uint32_t acc = g > 0 ? 1u : 0u;
+                    mma_tf32_ts(tb, acol + 0, bEh, IDESC, acc);
+                    mma_tf32_ts(tb, acol + 0, bEl, IDESC, 1u);
+                    mma_tf32_ts(tb, acol + 8, bEh, IDESC, 1u);
+                    mma_tf32_ts(tb + N, acol + 16, bOh, IDESC, acc);
+                    mma_tf32_ts(tb + N, acol + 16, bOl, IDESC, 1u);
+                    mma_tf32_ts(tb + N, acol + 24, bOh, IDESC, 1u);
+                    mma_commit(&S.empty[s]);
+                    issued = true;
+                }
+                gc += G;
+                if (!ok) break;
+                mma_commit(&S.done);
+            }
+            if (!ok) fail();
+            if (issued) {  // every MMA of this CTA retired before TMEM is freed
+                mma_commit(&S.drain);
+                for (uint32_t i = 0; i < WAIT_LIMIT && !mbar_try_wait(&S.drain, 0); ++i) {
+                }
+            }
+        }
+        __syncwarp();
+    } else {
+        // -------------------------------------------------------- B streaming
+        if (lane == 0) {
+            int64_t gc = 0;
+            bool ok = true;
+            int64_t last_use[NST];
+            for (int s = 0; s < NST; ++s) last_use[s] = -1;
+            for (int64_t u = blockIdx.x; u < a.nunits && ok; u += gridDim.x) {
+                const int m = unit_m(u / a.ntiles, lmax);
+                const int G = (lmax - m + GLG_GROUP) / GLG_GROUP;
+                const int64_t gb = a.goff[m];
+                for (int g = 0; g < G; ++g) {
+                    const int64_t gg = gc + g;
+                    const int s = (int)(gg % NST);
+                    const int64_t use = gg / NST;
+                    if (use > 0 && !wait(&S.empty[s], (uint32_t)((use - 1) & 1))) { ok = false; break; }
+                    mbar_arrive_expect_tx(&S.full_b[s], BBYTES);
+                    bulk_g2s(S.b[s], a.bpack + (size_t)(gb + g) * BBYTES, BBYTES, &S.full_b[s]);
+                    last_use[s] = use;
+                }
+                gc += G;
+            }
+            if (!ok) fail();
+            // outstanding copies land before the CTA exits
+            for (int s = 0; s < NST; ++s)
+                if (last_use[s] >= 0)
+                    for (uint32_t i = 0; i < WAIT_LIMIT && !mbar_try_wait(&S.full_b[s], (uint32_t)(last_use[s] & 1)); ++i) {
+                    }
+        }
+        __syncwarp();
+    }
+    fence_before_sync();
+    __syncthreads();
+    if (warp == 0) {
+        fence_after_sync();
+        tmem_dealloc(tb, TMEM_COLS);
+    }
+}
+
+// ------------------------------------------------------------------ packing
+
+// Bpack[goff[m] + g] = 4 tiles (E_hi, E_lo, O_hi, O_lo) of N x 8 tf32 values,
+// element (n, k) of a tile at float index (n/8)*64 + (k/4)*32 + (n%8)*4 + k%4,
+// holding the re (n even) or im (n odd) part of a_lm of map n/2 at
+// l = m + 16 g + 2 k + parity.
+template <int N>
+__global__ void k_pack_b(int lmax, int nmaps, int64_t nalm, const int64_t *__restrict__ mofs,
+                         const int64_t *__restrict__ goff, const float2 *__restrict__ alm,
+                         float *__restrict__ bpack) {
+    const int m = blockIdx.y;
+    const int G = (lmax - m + GLG_GROUP) / GLG_GROUP;
+    const int64_t mb = mofs[m];
+    for (int g = blockIdx.x; g < G; g += gridDim.x) {
+        float *dst = bpack + (goff[m] + g) * (int64_t)(32 * N);
+        for (int o = threadIdx.x; o < 32 * N; o += blockDim.x) {
+            const int t = o / (8 * N), q = o % (8 * N);
+            const int par = t >> 1, hl = t & 1;
+            const int ng = q / 64, r1 = q % 64, kc = r1 / 32, r2 = r1 % 32;
+            const int n = ng * 8 + r2 / 4, k = kc * 4 + (r2 & 3);
+            const int l = m + g * GLG_GROUP + 2 * k + par;
+            const int map = n >> 1;
+            float v = 0.f;
+            if (l <= lmax && map < nmaps) {
+                const float2 z = alm[(int64_t)map * nalm + mb + (l - m)];
+                v = (n & 1) ? z.y : z.x;
+                if (m == 0 && (n & 1)) v = 0.f;  // imaginary part of a_l0 is ignored
+            }
+            const uint32_t hi = tf32_rna(v);
+            dst[o] = hl ? __uint_as_float(tf32_rna(v - __uint_as_float(hi))) : __uint_as_float(hi);
+        }
+    }
+}
+
+template <int N>
+int launch_tc(const glg_plan *P, const float2 *alm, int nmaps, float *bpack, float2 *F, int *err,
+              cudaStream_t st) {
+    {
+        dim3 grid(64, P->mmax + 1);
+        GLG_LAUNCH_SCOPE("k_pack_b", st);
+        k_pack_b<N><<<grid, 256, 0, st>>>(P->lmax, nmaps, P->nalm, P->mofs, P->goff, alm, bpack);
+        GLG_CHECK_LAUNCH("k_pack_b");
+    }
+    LegTcArgs a;
+    a.npairs = P->npairs;
+    a.nrings = P->nrings;
+    a.lmax = P->lmax;
+    a.nmaps = nmaps;
+    a.ntiles = (P->npairs + 127) / 128;
+    a.nunits = (int64_t)a.ntiles * (P->mmax + 1);
+    a.cth32 = P->cth32;
+    a.coef32 = P->coef32;
+    a.mofs = P->mofs;
+    a.goff = P->goff;
+    a.seeds = P->seeds;
+    a.lstart = P->lstart;
+    a.bpack = reinterpret_cast<const unsigned char *>(bpack);
+    a.F = F;
+    a.err = err;
+    // more than half of the SM's shared memory: one CTA per SM, so no two
+    // CTAs contend for the 512 tensor-memory columns
+    size_t smem = sizeof(Smem<N>) + 128;
+    if (smem < 120 * 1024) smem = 120 * 1024;
+    cudaFuncSetAttribute(k_leg_tc<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int nsm = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t grid = a.nunits < nsm ? a.nunits : nsm;
+    GLG_LAUNCH_SCOPE("k_leg_tc", st);
+    k_leg_tc<N><<<(unsigned)grid, 320, smem, st>>>(a);
+    GLG_CHECK_LAUNCH("k_leg_tc");
+    return GLG_OK;
+}
+
+}  // namespace
+
+size_t glg_leg_tc_pack_bytes(const glg_plan *P, int nmaps) {
+    const int N = ((2 * nmaps + 15) / 16) * 16;
+    return (size_t)P->ngroups * 128 * N;
+}
+
+int glg_launch_leg_tc(const glg_plan *P, const float2 *alm, int nmaps, float *bpack, float2 *F,
+                      int *err, cudaStream_t st) {
+    const int N = ((2 * nmaps + 15) / 16) * 16;
+    switch (N) {
+        case 16: return launch_tc<16>(P, alm, nmaps, bpack, F, err, st);
+        case 32: return launch_tc<32>(P, alm, nmaps, bpack, F, err, st);
+        case 48: return launch_tc<48>(P, alm, nmaps, bpack, F, err, st);
+        case 64: return launch_tc<64>(P, alm, nmaps, bpack, F, err, st);
+        case 80: return launch_tc<80>(P, alm, nmaps, bpack, F, err, st);
+        case 96: return launch_tc<96>(P, alm, nmaps, bpack, F, err, st);
+        case 112: return launch_tc<112>(P, alm, nmaps, bpack, F, err, st);
+        case 128: return launch_tc<128>(P, alm, nmaps, bpack, F, err, st);
+        default:
+            glg_set_error("fast Legendre contraction: at most 64 maps per launch");
+            return GLG_ERR_UNSUPPORTED;
+    }
+}

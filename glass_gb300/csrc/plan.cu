@@ -198,11 +198,115 @@ static int dalloc(glg_plan *P, T **ptr, size_t count) {
 
 extern "C" void glg_plan_destroy(glg_plan *P) {
     if (!P) return;
-    void *ptrs[] = {P->cth, P->sth, P->nph, P->half, P->startN, P->startS, P->mofs, P->coef,
-                    P->lmm, P->lmm_scale, P->fft_radix, P->fft_nst, P->tw_ofs, P->tw};
+    void *ptrs[] = {P->cth,   P->sth,       P->nph,     P->half,   P->startN, P->startS,
+                    P->mofs,  P->coef,      P->lmm,     P->lmm_scale, P->fft_radix,
+                    P->fft_nst, P->tw_ofs,  P->tw,      P->cth32,  P->tw32,   P->coef32,
+                    P->goff,  P->seeds,     P->lstart};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     delete P;
+}
+
+// ------------------------------------------------------- fast-form tables
+
+// FP64 recurrence per (m, ring pair) that records, for every group of 16 l
+// values starting at l0 = m + 16 j, the seed pair (lambda_s0, lambda_s0+1)
+// with s0 = max(l0, ls), ls the first l whose |lambda| reaches 2^-100.  The
+// FP32 recurrence of the fast contraction restarts from these seeds, so its
+// rounding error never accumulates over more than 16 steps.
+__global__ void k_plan_seeds(int lmax, int npairs, const double *__restrict__ cth,
+                             const int64_t *__restrict__ mofs, const double2 *__restrict__ coef,
+                             const double *__restrict__ lmm, const int *__restrict__ lmm_scale,
+                             const int64_t *__restrict__ goff, float2 *__restrict__ seeds,
+                             int *__restrict__ lstart) {
+    const int m = blockIdx.y;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npairs) return;
+    const double x = cth[p];
+    const double thr = 7.888609052210118e-31;  // 2^-100
+    double l0 = 0.0, l1 = lmm[(int64_t)m * npairs + p];
+    int sc = lmm_scale[(int64_t)m * npairs + p];
+    int ls = -1;
+    float sx = 0.f;
+    int64_t pend = -1;  // group whose seed still needs lambda_{s0+1}
+    const int64_t base = mofs[m];
+    const int64_t g0 = goff[m];
+    for (int l = m; l <= lmax; ++l) {
+        if (l > m) {
+            double nl;
+            if (l == m + 1) {
+                nl = sqrt(2.0 * m + 3.0) * x * l1;
+            } else {
+                const double2 ab = coef[base + l - m];
+                nl = ab.x * (x * l1) - ab.y * l0;
+            }
+            l0 = l1;
+            l1 = nl;
+            if (sc < 0 && fabs(nl) > GLG_TWO_P400) {
+                l0 *= GLG_TWO_M800;
+                l1 *= GLG_TWO_M800;
+                sc += 1;
+            }
+        }
+        const double tv = sc == 0 ? l1 : 0.0;
+        if (ls < 0 && fabs(tv) >= thr) ls = l;
+        const int j = (l - m) / GLG_GROUP;
+        const int lg0 = m + j * GLG_GROUP;
+        if (pend >= 0) {  // l == s0 + 1 of the pending seed
+            seeds[pend * npairs + p] = make_float2(sx, (float)tv);
+            pend = -1;
+        }
+        if (ls >= 0 && l == (lg0 > ls ? lg0 : ls)) {
+            sx = (float)tv;
+            pend = g0 + j;
+        }
+        const bool group_end = ((l - m) % GLG_GROUP == GLG_GROUP - 1) || l == lmax;
+        if (group_end && ls < 0) seeds[(g0 + j) * npairs + p] = make_float2(0.f, 0.f);
+    }
+    if (pend >= 0) seeds[pend * npairs + p] = make_float2(sx, 0.f);
+    lstart[(int64_t)m * npairs + p] = ls < 0 ? lmax + 1 : ls;
+}
+
+__global__ void k_plan_f32(int64_t n, const double2 *__restrict__ src, float2 *__restrict__ dst) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        dst[i] = make_float2((float)src[i].x, (float)src[i].y);
+}
+
+__global__ void k_plan_cth32(int n, const double *__restrict__ src, float *__restrict__ dst) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = (float)src[i];
+}
+
+int glg_plan_prepare_fast(glg_plan *P, cudaStream_t st) {
+    static std::mutex mu;
+    std::lock_guard<std::mutex> lk(mu);
+    if (P->fast_ready) return GLG_OK;
+    const int np = P->npairs, lmax = P->lmax;
+    std::vector<int64_t> goff(lmax + 2, 0);
+    for (int m = 0; m <= lmax; ++m)
+        goff[m + 1] = goff[m] + (lmax - m + 1 + GLG_GROUP - 1) / GLG_GROUP;
+    P->ngroups = goff[lmax + 1];
+    const int64_t ntw = 4LL * P->nside * (P->nside + 1);
+    int rc;
+    if ((rc = dalloc(P, &P->cth32, np)) || (rc = dalloc(P, &P->tw32, ntw)) ||
+        (rc = dalloc(P, &P->coef32, P->nalm)) || (rc = dalloc(P, &P->goff, lmax + 2)) ||
+        (rc = dalloc(P, &P->seeds, (size_t)P->ngroups * np)) ||
+        (rc = dalloc(P, &P->lstart, (size_t)(lmax + 1) * np)))
+        return rc;
+    cudaError_t e = cudaMemcpyAsync(P->goff, goff.data(), sizeof(int64_t) * goff.size(),
+                                    cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return glg_cuda_status(e, "glg_plan_prepare_fast: upload");
+    k_plan_cth32<<<(np + 255) / 256, 256, 0, st>>>(np, P->cth, P->cth32);
+    k_plan_f32<<<1024, 256, 0, st>>>(ntw, P->tw, P->tw32);
+    k_plan_f32<<<1024, 256, 0, st>>>(P->nalm, P->coef, P->coef32);
+    dim3 gs((np + 127) / 128, lmax + 1);
+    k_plan_seeds<<<gs, 128, 0, st>>>(lmax, np, P->cth, P->mofs, P->coef, P->lmm, P->lmm_scale,
+                                     P->goff, P->seeds, P->lstart);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return glg_cuda_status(e, "glg_plan_prepare_fast");
+    P->fast_ready = true;
+    return GLG_OK;
 }
 
 extern "C" int glg_plan_create(int nside, int lmax, void *stream, glg_plan **out) {

@@ -1,4 +1,4 @@
-// Ring FFTs of the HEALPix ring SHT, FP64 plain form.
+// Ring FFTs of the HEALPix ring SHT, FP64 (plain form) and FP32 (fast form).
 //
 // Synthesis (inside healpy.alm2map, glass/healpix.py:71): for every ring
 // pair, the Legendre sums F_m of the north and the south ring are folded
@@ -22,66 +22,88 @@ namespace {
 constexpr int FFT_THREADS = 256;
 constexpr int SMALL_RADIX_MAX = 13;
 
+template <typename R>
 struct cplx {
-    double x, y;
+    R x, y;
 };
-__device__ __forceinline__ cplx cmul(cplx a, cplx b) {
+template <typename R>
+struct vec2;
+template <>
+struct vec2<double> {
+    using type = double2;
+};
+template <>
+struct vec2<float> {
+    using type = float2;
+};
+template <typename R>
+using V2 = typename vec2<R>::type;
+
+template <typename R>
+__device__ __forceinline__ cplx<R> cmul(cplx<R> a, cplx<R> b) {
     return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
 }
-__device__ __forceinline__ cplx cadd(cplx a, cplx b) { return {a.x + b.x, a.y + b.y}; }
-__device__ __forceinline__ cplx csub(cplx a, cplx b) { return {a.x - b.x, a.y - b.y}; }
-__device__ __forceinline__ cplx cconj(cplx a) { return {a.x, -a.y}; }
-__device__ __forceinline__ cplx ld(const double2 *p) {
-    double2 v = *p;
+template <typename R>
+__device__ __forceinline__ cplx<R> cadd(cplx<R> a, cplx<R> b) {
+    return {a.x + b.x, a.y + b.y};
+}
+template <typename R>
+__device__ __forceinline__ cplx<R> csub(cplx<R> a, cplx<R> b) {
+    return {a.x - b.x, a.y - b.y};
+}
+template <typename R>
+__device__ __forceinline__ cplx<R> cconj(cplx<R> a) {
+    return {a.x, -a.y};
+}
+template <typename R>
+__device__ __forceinline__ cplx<R> ld(const V2<R> *p) {
+    V2<R> v = *p;
     return {v.x, v.y};
 }
 
+template <typename R>
 struct RingCtx {
     int n;
-    const double2 *tw;  // omega_{2n}^t, t < 2n (synthesis direction e^{+i})
+    const V2<R> *tw;  // omega_{2n}^t, t < 2n (synthesis direction e^{+i})
     const int *radix;
     int nst;
     int dir;  // +1 synthesis (e^{+2 pi i/n}), -1 analysis
 };
 
 // omega_n^t in direction dir, 0 <= t < n
-__device__ __forceinline__ cplx wn(const RingCtx &c, int t) {
-    cplx w = ld(c.tw + 2 * t);
+template <typename R>
+__device__ __forceinline__ cplx<R> wn(const RingCtx<R> &c, int t) {
+    cplx<R> w = ld<R>(c.tw + 2 * t);
     if (c.dir < 0) w.y = -w.y;
     return w;
 }
 
-template <int R>
-__device__ __forceinline__ void bfly_small(cplx *Z, const RingCtx &c, int base, int msub, int L,
-                                           int j1) {
-    cplx v[R];
+template <typename R, int RD>
+__device__ __forceinline__ void bfly_small(cplx<R> *Z, const RingCtx<R> &c, int base, int msub,
+                                           int L, int j1) {
+    cplx<R> v[RD];
 #pragma unroll
-    for (int j = 0; j < R; ++j) v[j] = Z[base + msub * j];
-    cplx y[R];
-    if (R == 2) {
+    for (int j = 0; j < RD; ++j) v[j] = Z[base + msub * j];
+    cplx<R> y[RD];
+    if (RD == 2) {
         y[0] = cadd(v[0], v[1]);
         y[1] = csub(v[0], v[1]);
-    } else if (R == 4) {
+    } else if (RD == 4) {
         // omega_4 = dir * i
-        cplx a = cadd(v[0], v[2]), b = csub(v[0], v[2]);
-        cplx cc = cadd(v[1], v[3]), d = csub(v[1], v[3]);
-        cplx id = c.dir > 0 ? cplx{-d.y, d.x} : cplx{d.y, -d.x};  // (dir i) * d
+        cplx<R> a = cadd(v[0], v[2]), b = csub(v[0], v[2]);
+        cplx<R> cc = cadd(v[1], v[3]), d = csub(v[1], v[3]);
+        cplx<R> id = c.dir > 0 ? cplx<R>{-d.y, d.x} : cplx<R>{d.y, -d.x};
         y[0] = cadd(a, cc);
         y[2] = csub(a, cc);
         y[1] = cadd(b, id);
         y[3] = csub(b, id);
     } else {
-        const int step = c.n / R;
+        const int step = c.n / RD;
 #pragma unroll
-        for (int k = 0; k < R; ++k) {
-            cplx acc = v[0];
+        for (int k = 0; k < RD; ++k) {
+            cplx<R> acc = v[0];
 #pragma unroll
-            for (int j = 1; j < R; ++j) {
-                const int t = (j * k) % R;
-                cplx w = wn(c, t * step);
-                cplx pr = cmul(v[j], w);
-                acc = cadd(acc, pr);
-            }
+            for (int j = 1; j < RD; ++j) acc = cadd(acc, cmul(v[j], wn(c, ((j * k) % RD) * step)));
             y[k] = acc;
         }
     }
@@ -89,51 +111,52 @@ __device__ __forceinline__ void bfly_small(cplx *Z, const RingCtx &c, int base, 
     const int tstep = (c.n / L) * j1;
     Z[base] = y[0];
 #pragma unroll
-    for (int k = 1; k < R; ++k) Z[base + msub * k] = cmul(y[k], wn(c, tstep * k));
+    for (int k = 1; k < RD; ++k) Z[base + msub * k] = cmul(y[k], wn(c, tstep * k));
 }
 
 // In-place DIF mixed-radix FFT of Z[0..n) in shared memory.
-__device__ void fft_dif(cplx *Z, cplx *scratch, const RingCtx &c) {
+template <typename R>
+__device__ void fft_dif(cplx<R> *Z, cplx<R> *scratch, const RingCtx<R> &c) {
     int L = c.n;
     for (int s = 0; s < c.nst; ++s) {
-        const int R = c.radix[s];
-        const int msub = L / R;
-        const int nbf = c.n / R;
-        if (R <= SMALL_RADIX_MAX) {
+        const int RD = c.radix[s];
+        const int msub = L / RD;
+        const int nbf = c.n / RD;
+        if (RD <= SMALL_RADIX_MAX) {
             for (int bf = threadIdx.x; bf < nbf; bf += blockDim.x) {
                 const int blk = bf / msub, j1 = bf - blk * msub;
                 const int base = blk * L + j1;
-                switch (R) {
-                    case 2: bfly_small<2>(Z, c, base, msub, L, j1); break;
-                    case 3: bfly_small<3>(Z, c, base, msub, L, j1); break;
-                    case 4: bfly_small<4>(Z, c, base, msub, L, j1); break;
-                    case 5: bfly_small<5>(Z, c, base, msub, L, j1); break;
-                    case 7: bfly_small<7>(Z, c, base, msub, L, j1); break;
-                    case 11: bfly_small<11>(Z, c, base, msub, L, j1); break;
-                    case 13: bfly_small<13>(Z, c, base, msub, L, j1); break;
+                switch (RD) {
+                    case 2: bfly_small<R, 2>(Z, c, base, msub, L, j1); break;
+                    case 3: bfly_small<R, 3>(Z, c, base, msub, L, j1); break;
+                    case 4: bfly_small<R, 4>(Z, c, base, msub, L, j1); break;
+                    case 5: bfly_small<R, 5>(Z, c, base, msub, L, j1); break;
+                    case 7: bfly_small<R, 7>(Z, c, base, msub, L, j1); break;
+                    case 11: bfly_small<R, 11>(Z, c, base, msub, L, j1); break;
+                    case 13: bfly_small<R, 13>(Z, c, base, msub, L, j1); break;
                     default: break;
                 }
             }
             __syncthreads();
         } else {
             // large prime radix: one butterfly at a time, threads over outputs
-            const int step = c.n / R;
+            const int step = c.n / RD;
             for (int bf = 0; bf < nbf; ++bf) {
                 const int blk = bf / msub, j1 = bf - blk * msub;
                 const int base = blk * L + j1;
                 const int tstep = (c.n / L) * j1;
-                for (int k = threadIdx.x; k < R; k += blockDim.x) {
-                    cplx acc = {0.0, 0.0};
-                    int t = 0;  // (j k) mod R
-                    for (int j = 0; j < R; ++j) {
+                for (int k = threadIdx.x; k < RD; k += blockDim.x) {
+                    cplx<R> acc = {R(0), R(0)};
+                    int t = 0;  // (j k) mod RD
+                    for (int j = 0; j < RD; ++j) {
                         acc = cadd(acc, cmul(Z[base + msub * j], wn(c, t * step)));
                         t += k;
-                        if (t >= R) t -= R;
+                        if (t >= RD) t -= RD;
                     }
                     scratch[k] = k == 0 ? acc : cmul(acc, wn(c, tstep * k));
                 }
                 __syncthreads();
-                for (int k = threadIdx.x; k < R; k += blockDim.x) Z[base + msub * k] = scratch[k];
+                for (int k = threadIdx.x; k < RD; k += blockDim.x) Z[base + msub * k] = scratch[k];
                 __syncthreads();
             }
         }
@@ -142,13 +165,14 @@ __device__ void fft_dif(cplx *Z, cplx *scratch, const RingCtx &c) {
 }
 
 // Position of output k after the in-place DIF passes (mixed-radix digit reversal).
-__device__ __forceinline__ int dif_pos(const RingCtx &c, int k) {
+template <typename R>
+__device__ __forceinline__ int dif_pos(const RingCtx<R> &c, int k) {
     int pos = 0, span = c.n;
     for (int s = 0; s < c.nst; ++s) {
-        const int R = c.radix[s];
-        span /= R;
-        const int d = k % R;
-        k /= R;
+        const int RD = c.radix[s];
+        span /= RD;
+        const int d = k % RD;
+        k /= RD;
         pos += d * span;
     }
     return pos;
@@ -161,30 +185,44 @@ __device__ __forceinline__ double apply_epi(double v, int kind, double var, doub
     }
     return v;
 }
+__device__ __forceinline__ float apply_epi(float v, int kind, double var, double lam) {
+    if (kind == GLG_EPI_LOGNORMAL) {
+        v = expm1f(v - (float)(var * 0.5));
+        if (lam != 1.0) v = (float)lam * v;
+    }
+    return v;
+}
 
 struct EpiArgs {
-    int kind[8];            // per map of this launch chunk
+    int kind[8];  // per map of this launch chunk
     double var[8], lam[8];
 };
 
-// grid (npairs, nmaps): F [nmaps][nrings][mmax+1] -> maps [nmaps][npix]
+// Strides of the Legendre-sum array F (in complex elements).
+struct FLayout {
+    int64_t map, ring, m;
+};
+
+// grid (npairs, nmaps): F -> maps [nmaps][npix]
+template <typename R>
 __global__ void __launch_bounds__(FFT_THREADS)
 k_ring_syn(const int nrings, const int mmax, const int *__restrict__ nph, const int *__restrict__ half,
            const int64_t *__restrict__ startN, const int64_t *__restrict__ startS,
            const int *__restrict__ fft_radix, const int *__restrict__ fft_nst,
-           const int64_t *__restrict__ tw_ofs, const double2 *__restrict__ tw,
-           const double2 *__restrict__ F, double *__restrict__ maps, const int64_t npix,
+           const int64_t *__restrict__ tw_ofs, const V2<R> *__restrict__ tw,
+           const V2<R> *__restrict__ F, const FLayout fl, R *__restrict__ maps, const int64_t npix,
            const int map0, const EpiArgs epi) {
-    extern __shared__ double2 smem_raw[];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
     const int p = blockIdx.x;
     const int map = map0 + blockIdx.y;
     const int n = nph[p];
     const int i4 = n / 4;
-    cplx *Z = reinterpret_cast<cplx *>(smem_raw);
-    cplx *scratch = Z + n;
+    cplx<R> *Z = reinterpret_cast<cplx<R> *>(smem_raw);
+    cplx<R> *scratch = Z + n;
     __shared__ int radix_s[GLG_MAX_FFT_STAGES];
-    if (threadIdx.x < GLG_MAX_FFT_STAGES) radix_s[threadIdx.x] = fft_radix[i4 * GLG_MAX_FFT_STAGES + threadIdx.x];
-    RingCtx c;
+    if (threadIdx.x < GLG_MAX_FFT_STAGES)
+        radix_s[threadIdx.x] = fft_radix[i4 * GLG_MAX_FFT_STAGES + threadIdx.x];
+    RingCtx<R> c;
     c.n = n;
     c.tw = tw + tw_ofs[i4];
     c.radix = radix_s;
@@ -193,36 +231,38 @@ k_ring_syn(const int nrings, const int mmax, const int *__restrict__ nph, const 
     const int h = half[p];
     const int rn = p, rs = nrings - 1 - p;
     const bool equator = rn == rs;
-    const double2 *FN = F + ((int64_t)blockIdx.y * nrings + rn) * (mmax + 1);
-    const double2 *FS = F + ((int64_t)blockIdx.y * nrings + rs) * (mmax + 1);
+    const V2<R> *FN = F + (int64_t)map * fl.map + (int64_t)rn * fl.ring;
+    const V2<R> *FS = F + (int64_t)map * fl.map + (int64_t)rs * fl.ring;
     // fold: B_k = 1/2 sum_{m = k mod n} c_m G_m + 1/2 sum_{m = -k mod n} c_m conj(G_m)
     for (int k = threadIdx.x; k < n; k += blockDim.x) {
-        cplx bn = {0.0, 0.0}, bs = {0.0, 0.0};
+        cplx<R> bn = {R(0), R(0)}, bs = {R(0), R(0)};
         for (int m = k; m <= mmax; m += n) {
-            const double cm = m == 0 ? 0.5 : 1.0;
-            cplx ph = h ? ld(c.tw + (int)(((int64_t)m) % (2 * n))) : cplx{1.0, 0.0};
-            cplx gn = cmul(ld(FN + m), ph), gs = cmul(ld(FS + m), ph);
-            bn = cadd(bn, {cm * gn.x, cm * gn.y});
-            bs = cadd(bs, {cm * gs.x, cm * gs.y});
+            const R cm = m == 0 ? R(0.5) : R(1);
+            cplx<R> ph = h ? ld<R>(c.tw + (m % (2 * n))) : cplx<R>{R(1), R(0)};
+            cplx<R> gn = cmul(ld<R>(FN + m * fl.m), ph);
+            cplx<R> gs = cmul(ld<R>(FS + m * fl.m), ph);
+            bn = cadd(bn, cplx<R>{cm * gn.x, cm * gn.y});
+            bs = cadd(bs, cplx<R>{cm * gs.x, cm * gs.y});
         }
         for (int m = (n - k) % n; m <= mmax; m += n) {
-            const double cm = m == 0 ? 0.5 : 1.0;
-            cplx ph = h ? ld(c.tw + (int)(((int64_t)m) % (2 * n))) : cplx{1.0, 0.0};
-            cplx gn = cconj(cmul(ld(FN + m), ph)), gs = cconj(cmul(ld(FS + m), ph));
-            bn = cadd(bn, {cm * gn.x, cm * gn.y});
-            bs = cadd(bs, {cm * gs.x, cm * gs.y});
+            const R cm = m == 0 ? R(0.5) : R(1);
+            cplx<R> ph = h ? ld<R>(c.tw + (m % (2 * n))) : cplx<R>{R(1), R(0)};
+            cplx<R> gn = cconj(cmul(ld<R>(FN + m * fl.m), ph));
+            cplx<R> gs = cconj(cmul(ld<R>(FS + m * fl.m), ph));
+            bn = cadd(bn, cplx<R>{cm * gn.x, cm * gn.y});
+            bs = cadd(bs, cplx<R>{cm * gs.x, cm * gs.y});
         }
-        if (equator) bs = {0.0, 0.0};
+        if (equator) bs = {R(0), R(0)};
         Z[k] = {bn.x - bs.y, bn.y + bs.x};  // B^N + i B^S
     }
     __syncthreads();
-    fft_dif(Z, scratch, c);
+    fft_dif<R>(Z, scratch, c);
     const int slot = blockIdx.y;
     const double var = epi.var[slot], lam = epi.lam[slot];
     const int ekind = epi.kind[slot];
-    double *mp = maps + (int64_t)map * npix;
+    R *mp = maps + (int64_t)map * npix;
     for (int j = threadIdx.x; j < n; j += blockDim.x) {
-        const cplx v = Z[dif_pos(c, j)];
+        const cplx<R> v = Z[dif_pos(c, j)];
         mp[startN[p] + j] = apply_epi(v.x, ekind, var, lam);
         if (!equator) mp[startS[p] + j] = apply_epi(v.y, ekind, var, lam);
     }
@@ -236,16 +276,17 @@ k_ring_ana(const int nrings, const int mmax, const int *__restrict__ nph, const 
            const int *__restrict__ fft_radix, const int *__restrict__ fft_nst,
            const int64_t *__restrict__ tw_ofs, const double2 *__restrict__ tw,
            const double *__restrict__ maps, const int64_t npix, double2 *__restrict__ G) {
-    extern __shared__ double2 smem_raw[];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
     const int p = blockIdx.x;
     const int map = blockIdx.y;
     const int n = nph[p];
     const int i4 = n / 4;
-    cplx *Z = reinterpret_cast<cplx *>(smem_raw);
-    cplx *scratch = Z + n;
+    cplx<double> *Z = reinterpret_cast<cplx<double> *>(smem_raw);
+    cplx<double> *scratch = Z + n;
     __shared__ int radix_s[GLG_MAX_FFT_STAGES];
-    if (threadIdx.x < GLG_MAX_FFT_STAGES) radix_s[threadIdx.x] = fft_radix[i4 * GLG_MAX_FFT_STAGES + threadIdx.x];
-    RingCtx c;
+    if (threadIdx.x < GLG_MAX_FFT_STAGES)
+        radix_s[threadIdx.x] = fft_radix[i4 * GLG_MAX_FFT_STAGES + threadIdx.x];
+    RingCtx<double> c;
     c.n = n;
     c.tw = tw + tw_ofs[i4];
     c.radix = radix_s;
@@ -261,19 +302,19 @@ k_ring_ana(const int nrings, const int mmax, const int *__restrict__ nph, const 
         Z[j] = {fn, fs};
     }
     __syncthreads();
-    fft_dif(Z, scratch, c);
+    fft_dif<double>(Z, scratch, c);
     const double w = 4.0 * 3.14159265358979323846 / (double)npix;
     double2 *GN = G + ((int64_t)map * nrings + rn) * (mmax + 1);
     double2 *GS = G + ((int64_t)map * nrings + rs) * (mmax + 1);
     for (int m = threadIdx.x; m <= mmax; m += blockDim.x) {
         const int k = m % n;
         const int kc = (n - k) % n;
-        const cplx X = Z[dif_pos(c, k)];
-        const cplx Xc = cconj(Z[dif_pos(c, kc)]);
+        const cplx<double> X = Z[dif_pos(c, k)];
+        const cplx<double> Xc = cconj(Z[dif_pos(c, kc)]);
         // spectra of the real parts: N = (X + conj X_{-k})/2, S = (X - conj X_{-k})/(2i)
-        cplx sn = {0.5 * (X.x + Xc.x), 0.5 * (X.y + Xc.y)};
-        cplx ss = {0.5 * (X.y - Xc.y), -0.5 * (X.x - Xc.x)};
-        cplx ph = h ? cconj(ld(c.tw + (int)(((int64_t)m) % (2 * n)))) : cplx{1.0, 0.0};
+        cplx<double> sn = {0.5 * (X.x + Xc.x), 0.5 * (X.y + Xc.y)};
+        cplx<double> ss = {0.5 * (X.y - Xc.y), -0.5 * (X.x - Xc.x)};
+        cplx<double> ph = h ? cconj(ld<double>(c.tw + (m % (2 * n)))) : cplx<double>{1.0, 0.0};
         sn = cmul(sn, ph);
         ss = cmul(ss, ph);
         GN[m] = make_double2(w * sn.x, w * sn.y);
@@ -281,21 +322,21 @@ k_ring_ana(const int nrings, const int mmax, const int *__restrict__ nph, const 
     }
 }
 
+template <typename R>
 size_t ring_smem_bytes(int nmax) {
     // data + large-radix scratch (a prime radix is at most n / 4)
-    return sizeof(double2) * ((size_t)nmax + (size_t)nmax / 4 + 1);
+    return sizeof(cplx<R>) * ((size_t)nmax + (size_t)nmax / 4 + 1);
 }
 
-}  // namespace
-
-int glg_launch_ring_syn(const glg_plan *P, const double2 *F, int nmaps, double *maps,
-                        const glg_epilogue *epi, cudaStream_t st) {
-    const size_t smem = ring_smem_bytes(4 * P->nside);
+template <typename R>
+int launch_ring_syn(const glg_plan *P, const V2<R> *tw, const V2<R> *F, FLayout fl, int nmaps,
+                    R *maps, const glg_epilogue *epi, cudaStream_t st) {
+    const size_t smem = ring_smem_bytes<R>(4 * P->nside);
     if (smem > 227 * 1024) {
-        glg_set_error("ring FFT: nside too large for the FP64 shared-memory FFT");
+        glg_set_error("ring FFT: nside too large for the shared-memory FFT of this precision");
         return GLG_ERR_UNSUPPORTED;
     }
-    cudaFuncSetAttribute(k_ring_syn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_ring_syn<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     for (int m0 = 0; m0 < nmaps; m0 += 8) {
         const int cnt = nmaps - m0 < 8 ? nmaps - m0 : 8;
         EpiArgs ea;
@@ -306,17 +347,32 @@ int glg_launch_ring_syn(const glg_plan *P, const double2 *F, int nmaps, double *
         }
         dim3 grid(P->npairs, cnt);
         GLG_LAUNCH_SCOPE("k_ring_syn", st);
-        k_ring_syn<<<grid, FFT_THREADS, smem, st>>>(
-            P->nrings, P->mmax, P->nph, P->half, P->startN, P->startS, P->fft_radix, P->fft_nst,
-            P->tw_ofs, P->tw, F + (int64_t)m0 * P->nrings * (P->mmax + 1), maps, P->npix, m0, ea);
+        k_ring_syn<R><<<grid, FFT_THREADS, smem, st>>>(P->nrings, P->mmax, P->nph, P->half, P->startN,
+                                                       P->startS, P->fft_radix, P->fft_nst, P->tw_ofs,
+                                                       tw, F, fl, maps, P->npix, m0, ea);
         GLG_CHECK_LAUNCH("k_ring_syn");
     }
     return GLG_OK;
 }
 
+}  // namespace
+
+int glg_launch_ring_syn(const glg_plan *P, const double2 *F, int nmaps, double *maps,
+                        const glg_epilogue *epi, cudaStream_t st) {
+    const FLayout fl{(int64_t)P->nrings * (P->mmax + 1), (int64_t)(P->mmax + 1), 1};
+    return launch_ring_syn<double>(P, P->tw, F, fl, nmaps, maps, epi, st);
+}
+
+// FP32 synthesis from F laid out [map][m][ring] (the fast contraction's output).
+int glg_launch_ring_syn_f32(const glg_plan *P, const float2 *F, int nmaps, float *maps,
+                            const glg_epilogue *epi, cudaStream_t st) {
+    const FLayout fl{(int64_t)P->nrings * (P->mmax + 1), 1, (int64_t)P->nrings};
+    return launch_ring_syn<float>(P, P->tw32, F, fl, nmaps, maps, epi, st);
+}
+
 int glg_launch_ring_ana(const glg_plan *P, const double *maps, int nmaps, double2 *G,
                         cudaStream_t st) {
-    const size_t smem = ring_smem_bytes(4 * P->nside);
+    const size_t smem = ring_smem_bytes<double>(4 * P->nside);
     if (smem > 227 * 1024) {
         glg_set_error("ring FFT: nside too large for the FP64 shared-memory FFT");
         return GLG_ERR_UNSUPPORTED;

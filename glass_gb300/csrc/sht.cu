@@ -19,9 +19,19 @@ size_t ring_coef_bytes(const glg_plan *P, int nmaps) {
 
 }  // namespace
 
+static size_t fast_pack_bytes(const glg_plan *P, int nmaps) {
+    // group counts are fixed by (lmax); the tables need not exist yet
+    int64_t ng = 0;
+    for (int m = 0; m <= P->lmax; ++m) ng += (P->lmax - m + GLG_GROUP) / GLG_GROUP;
+    const int N = ((2 * nmaps + 15) / 16) * 16;
+    return (size_t)ng * 128 * N;
+}
+
 extern "C" size_t glg_alm2map_workspace(const glg_plan *P, int nmaps, int form) {
     if (!P || nmaps <= 0) return 0;
-    (void)form;
+    if (form == GLG_FORM_FAST)
+        return GLG_WS_STATUS_BYTES + fast_pack_bytes(P, nmaps) +
+               sizeof(float2) * (size_t)nmaps * P->nrings * (P->mmax + 1);
     return ring_coef_bytes(P, nmaps);
 }
 
@@ -31,14 +41,40 @@ extern "C" int glg_alm2map(const glg_plan *P, const void *alm, int nmaps, int fo
     GLG_REQUIRE(nmaps >= 0, "glg_alm2map: negative nmaps");
     if (nmaps == 0) return GLG_OK;
     GLG_REQUIRE(alm && maps, "glg_alm2map: null pointer");
-    GLG_REQUIRE(form == GLG_FORM_PLAIN, "glg_alm2map: unknown form");
+    GLG_REQUIRE(form == GLG_FORM_PLAIN || form == GLG_FORM_FAST, "glg_alm2map: unknown form");
     GLG_REQUIRE(ws && ws_bytes >= glg_alm2map_workspace(P, nmaps, form),
                 "glg_alm2map: workspace too small");
     cudaStream_t st = (cudaStream_t)stream;
+    if (form == GLG_FORM_FAST) {
+        GLG_REQUIRE(nmaps <= 64, "glg_alm2map: the fast form takes at most 64 maps per call");
+        int rc = glg_plan_prepare_fast(const_cast<glg_plan *>(P), st);
+        if (rc) return rc;
+        int *err = (int *)ws;
+        float *bpack = (float *)((char *)ws + GLG_WS_STATUS_BYTES);
+        float2 *F = (float2 *)((char *)ws + GLG_WS_STATUS_BYTES + fast_pack_bytes(P, nmaps));
+        cudaError_t e = cudaMemsetAsync(err, 0, GLG_WS_STATUS_BYTES, st);
+        if (e != cudaSuccess) return glg_cuda_status(e, "glg_alm2map: status reset");
+        rc = glg_launch_leg_tc(P, (const float2 *)alm, nmaps, bpack, F, err, st);
+        if (rc) return rc;
+        return glg_launch_ring_syn_f32(P, F, nmaps, (float *)maps, epi, st);
+    }
     double2 *F = (double2 *)ws;
     int rc = glg_launch_leg_syn(P, (const double2 *)alm, nmaps, F, st);
     if (rc) return rc;
     return glg_launch_ring_syn(P, F, nmaps, (double *)maps, epi, st);
+}
+
+extern "C" int glg_workspace_status(const void *ws, void *stream) {
+    GLG_REQUIRE(ws != nullptr, "glg_workspace_status: null workspace");
+    int st_host = 0;
+    cudaError_t e = cudaMemcpyAsync(&st_host, ws, sizeof(int), cudaMemcpyDeviceToHost, (cudaStream_t)stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (e != cudaSuccess) return glg_cuda_status(e, "glg_workspace_status");
+    if (st_host != 0) {
+        glg_set_error("a bounded device wait of the fast Legendre contraction timed out");
+        return st_host;
+    }
+    return GLG_OK;
 }
 
 extern "C" size_t glg_alm2map_spin_workspace(const glg_plan *P) {

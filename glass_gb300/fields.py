@@ -241,6 +241,10 @@ class _FieldBatcher:
         self.lmax = n - 1
         self.nside = int(nside)
         self.form = form
+        if form not in ("plain", "fast"):
+            raise ValueError(f"form must be 'plain' or 'fast', not {form!r}")
+        self.cdtype = torch.complex128 if form == "plain" else torch.complex64
+        self.code = _lib.GLG_F64 if form == "plain" else _lib.GLG_F32
         self.z_size = n * (n + 1) // 2
         gls_dev = [_lib.to_device(g, torch.float64, self.device) if g is not None else None for g in gls]
         covs = [c.clone() for c in cls2cov(gls_dev, n, self.ngrf, self.ncorr)]
@@ -262,11 +266,11 @@ class _FieldBatcher:
 
     def _host_variates(self, t: int) -> torch.Tensor:
         z = self.np_rng.standard_normal((self.z_size, 2)) @ np.asarray([1, 1j])
-        return torch.as_tensor(z, dtype=torch.complex128).to(self.device)
+        return torch.as_tensor(z, dtype=self.cdtype).to(self.device)
 
     def alm(self, t0: int, nshell: int) -> torch.Tensor:
         """Correlated alm of shells t0..t0+nshell-1 (HEALPix order) [nshell][nalm]."""
-        alm = torch.empty((nshell, self.z_size), dtype=torch.complex128, device=self.device)
+        alm = torch.empty((nshell, self.z_size), dtype=self.cdtype, device=self.device)
         w = self.w[t0:t0 + nshell].contiguous()
         zlo = max(0, t0 - self.k)
         if self.np_rng is not None:
@@ -276,19 +280,19 @@ class _FieldBatcher:
                 self.zwin.popleft()
             z = torch.stack(list(self.zwin))
             check(lib().glg_alm_correlate(c_p(ptr(w)), nshell, self.lmax, self.k, t0, c_p(ptr(z)),
-                                          zlo, 0, 0, _lib.GLG_F64, c_p(ptr(alm)),
+                                          zlo, 0, 0, self.code, c_p(ptr(alm)),
                                           c_p(stream_ptr(self.device))), "glg_alm_correlate")
         else:
             # shell t draws Philox stream sid0 + t (streams reserved per generate call)
             check(lib().glg_alm_correlate(c_p(ptr(w)), nshell, self.lmax, self.k, t0, None, zlo,
                                           ctypes.c_uint64(self.g_rng.seed), ctypes.c_uint64(self.sid0),
-                                          _lib.GLG_F64, c_p(ptr(alm)), c_p(stream_ptr(self.device))),
+                                          self.code, c_p(ptr(alm)), c_p(stream_ptr(self.device))),
                   "glg_alm_correlate")
         return alm
 
     def maps(self, t0: int, nshell: int, epi=None) -> torch.Tensor:
         alm = self.alm(t0, nshell)
-        return hp.synth(alm, self.nside, self.lmax, epilogue=epi)
+        return hp.synth(alm, self.nside, self.lmax, epilogue=epi, form=self.form)
 
 
 def _group_size(ngrf: int, nside: int, lmax: int, form: str, host_rng: bool = False) -> int:

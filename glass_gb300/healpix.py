@@ -81,25 +81,63 @@ def _resize_alm(alm: torch.Tensor, lmax_in: int, lmax_out: int) -> torch.Tensor:
     return out
 
 
-def synth(alm: torch.Tensor, nside: int, lmax: int, *, epilogue=None) -> torch.Tensor:
-    """Spin-0 synthesis of complex128 alm [nmaps, nalm] -> float64 maps [nmaps, npix]."""
+FAST_MAX_MAPS = 40  # maps per fast-form launch (N = 80 tensor-core columns)
+
+
+def synth(alm: torch.Tensor, nside: int, lmax: int, *, epilogue=None, form: str = "plain") -> torch.Tensor:
+    """Spin-0 synthesis of alm [nmaps, nalm] -> maps [nmaps, npix].
+
+    ``form="plain"``: complex128 alm, float64 maps (FP64 throughout).
+    ``form="fast"``: complex64 alm, float32 maps (tensor-core Legendre sums).
+    """
+    if form == "fast":
+        return _synth_fast(alm, nside, lmax, epilogue)
     plan = get_plan(nside, lmax, alm.device)
     nmaps = alm.shape[0]
     maps = torch.empty((nmaps, plan.npix), dtype=torch.float64, device=alm.device)
     ws_bytes = int(lib().glg_alm2map_workspace(plan.handle, nmaps, _lib.FORM_PLAIN))
     ws = torch.empty(max(ws_bytes, 1), dtype=torch.uint8, device=alm.device)
-    epi = None
-    if epilogue is not None:
-        kind, var, lam = epilogue
-        kinds = list(kind) if isinstance(kind, (list, tuple)) else [int(kind)] * nmaps
-        kinds_a = (ctypes.c_int * nmaps)(*kinds)
-        var_a = (ctypes.c_double * nmaps)(*var)
-        lam_a = (ctypes.c_double * nmaps)(*lam)
-        epi = _lib.Epilogue(_lib.EPI_NONE, kinds_a, var_a, lam_a)
+    epi = _make_epilogue(epilogue, nmaps)
     check(lib().glg_alm2map(plan.handle, c_p(ptr(alm)), nmaps, _lib.FORM_PLAIN, c_p(ptr(maps)),
                             ctypes.byref(epi) if epi is not None else None, c_p(ptr(ws)), ws_bytes,
                             c_p(stream_ptr(alm.device))), "glg_alm2map")
     return maps
+
+
+def _synth_fast(alm: torch.Tensor, nside: int, lmax: int, epilogue) -> torch.Tensor:
+    plan = get_plan(nside, lmax, alm.device)
+    alm = alm.to(torch.complex64).contiguous()
+    nmaps = alm.shape[0]
+    maps = torch.empty((nmaps, plan.npix), dtype=torch.float32, device=alm.device)
+    step = min(nmaps, FAST_MAX_MAPS)
+    ws_bytes = int(lib().glg_alm2map_workspace(plan.handle, step, _lib.FORM_FAST))
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device=alm.device)
+    stream = c_p(stream_ptr(alm.device))
+    for m0 in range(0, nmaps, step):
+        cnt = min(step, nmaps - m0)
+        epi = None
+        if epilogue is not None:
+            kind, var, lam = epilogue
+            kinds = list(kind) if isinstance(kind, (list, tuple)) else [int(kind)] * nmaps
+            epi = _make_epilogue((kinds[m0:m0 + cnt], var[m0:m0 + cnt], lam[m0:m0 + cnt]), cnt)
+        check(lib().glg_alm2map(plan.handle, c_p(ptr(alm[m0:m0 + cnt])), cnt, _lib.FORM_FAST,
+                                c_p(ptr(maps[m0:m0 + cnt])), ctypes.byref(epi) if epi is not None else None,
+                                c_p(ptr(ws)), ws_bytes, stream), "glg_alm2map (fast)")
+    check(lib().glg_workspace_status(c_p(ptr(ws)), stream), "glg_alm2map (fast)")
+    return maps
+
+
+def _make_epilogue(epilogue, nmaps):
+    if epilogue is None:
+        return None
+    kind, var, lam = epilogue
+    kinds = list(kind) if isinstance(kind, (list, tuple)) else [int(kind)] * nmaps
+    kinds_a = (ctypes.c_int * nmaps)(*kinds)
+    var_a = (ctypes.c_double * nmaps)(*var)
+    lam_a = (ctypes.c_double * nmaps)(*lam)
+    epi = _lib.Epilogue(_lib.EPI_NONE, kinds_a, var_a, lam_a)
+    epi._keep = (kinds_a, var_a, lam_a)
+    return epi
 
 
 def alm2map(alms, nside: int, *, inplace: bool = False, lmax: int | None = None,

@@ -125,12 +125,23 @@ typedef struct glg_epilogue {
  * Spin-0 synthesis, glass/healpix.py:38-78 (healpy.alm2map with pol=False,
  * pixwin=False; as called at glass/fields.py:429).  alm: complex [nmaps][nalm]
  * (HEALPix order, mmax = lmax of the plan); maps: [nmaps][npix] RING order.
- * form GLG_FORM_PLAIN: FP64 throughout (alm and maps dtype GLG_F64).
- * workspace: device scratch of glg_alm2map_workspace() bytes.
+ * form GLG_FORM_PLAIN: FP64 throughout (alm complex128, maps float64).
+ * form GLG_FORM_FAST: alm complex64, maps float32; the Legendre sums run on
+ *   the tensor cores as split-precision 3xTF32 with FP32 accumulation,
+ *   lambda_lm from an FP32 recurrence restarted every 16 l from FP64 seeds
+ *   (built once per plan on first use; that first call synchronises the
+ *   stream); at most 64 maps per call.
+ * workspace: device scratch of glg_alm2map_workspace() bytes.  For the fast
+ * form its first int receives GLG_ERR_TIMEOUT if a bounded device wait gave
+ * up; glg_workspace_status() reads it.
  */
 size_t glg_alm2map_workspace(const glg_plan *plan, int nmaps, int form);
 int glg_alm2map(const glg_plan *plan, const void *alm, int nmaps, int form, void *maps,
                 const glg_epilogue *epi, void *workspace, size_t workspace_bytes, void *stream);
+
+/* Status word of a fast-form workspace (synchronises `stream`): GLG_OK or
+ * GLG_ERR_TIMEOUT.  No counterpart in the reference (no device waits there). */
+int glg_workspace_status(const void *workspace, void *stream);
 
 /*
  * Spin-s synthesis (s = 1, 2), glass/healpix.py:81-108 (healpy.alm2map_spin,
