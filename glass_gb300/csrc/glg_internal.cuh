@@ -75,9 +75,9 @@ struct glg_plan {
 
     // fast-form tables (built on first use by glg_plan_prepare_fast)
     bool fast_ready;
-    float *cth32;            // [npairs]
+    float2 *cth32;           // [npairs] cos theta as FP32 (hi, lo)
     float2 *tw32;            // FP32 copy of tw
-    float2 *coef32;          // [nalm] FP32 (A, B)
+    float4 *coef32;          // [nalm] (A_hi, A_lo, B_hi, B_lo) in FP32
     int64_t *goff;           // [mmax+2] first 16-l group of m: sum_{m'<m} ceil((lmax-m'+1)/16)
     int64_t ngroups;         // total groups
     float2 *seeds;           // [ngroups][npairs] (lambda_s0, lambda_s0+1) per group

@@ -38,8 +38,8 @@ constexpr uint32_t WAIT_LIMIT = 1u << 22;
 struct LegTcArgs {
     int npairs, nrings, lmax, nmaps, ntiles;
     int64_t nunits;
-    const float *cth32;
-    const float2 *coef32;
+    const float2 *cth32;
+    const float4 *coef32;
     const int64_t *mofs;
     const int64_t *goff;
     const float2 *seeds;
@@ -53,6 +53,25 @@ __device__ __forceinline__ uint32_t tf32_rna(float x) {
     uint32_t r;
     asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
     return r;
+}
+
+// One step lambda_l = A (x lambda_{l-1}) - B lambda_{l-2} in FP32 with the
+// products and the coefficients carried as (hi, lo) pairs (error-free
+// transformations with fma): only the FP32 state itself is rounded, which
+// keeps the 16-step runs between FP64 seeds near 1e-7.  The __f*_rn forms
+// keep the compiler from fusing the rounded products away.
+__device__ __forceinline__ float rec_step_comp(const float4 c, const float2 x, float lm1, float lm2) {
+    const float yh = __fmul_rn(x.x, lm1);
+    float ye = fmaf(x.x, lm1, -yh);
+    ye = fmaf(x.y, lm1, ye);
+    const float ph = __fmul_rn(c.x, yh);
+    float pe = fmaf(c.x, yh, -ph);
+    pe = fmaf(c.x, ye, pe);
+    pe = fmaf(c.y, yh, pe);
+    const float qh = __fmul_rn(c.z, lm2);
+    float qe = fmaf(c.z, lm2, -qh);
+    qe = fmaf(c.w, lm2, qe);
+    return __fadd_rn(__fsub_rn(ph, qh), __fsub_rn(pe, qe));
 }
 
 __device__ __forceinline__ int unit_m(int64_t mi, int lmax) {
@@ -125,7 +144,7 @@ __global__ void __launch_bounds__(320, 1) k_leg_tc(const LegTcArgs a) {
             const int p = tile * 128 + r;
             const bool live = p < a.npairs;
             const int pp = live ? p : a.npairs - 1;
-            const float x = a.cth32[pp];
+            const float2 x = a.cth32[pp];  // cos theta as (hi, lo)
             const int ls = live ? a.lstart[(int64_t)m * a.npairs + pp] : lmax + 1;
             const int64_t mb = a.mofs[m];
             const int64_t gb = a.goff[m];
@@ -153,8 +172,7 @@ __global__ void __launch_bounds__(320, 1) k_leg_tc(const LegTcArgs a) {
                     } else if (l == s0 + 1) {
                         v = seed.y;
                     } else {
-                        const float2 ab = __ldg(a.coef32 + mb + (l - m));
-                        v = fmaf(ab.x, x * lm1, -ab.y * lm2);
+                        v = rec_step_comp(__ldg(a.coef32 + mb + (l - m)), x, lm1, lm2);
                     }
                     lm2 = lm1;
                     lm1 = v;

@@ -272,9 +272,22 @@ __global__ void k_plan_f32(int64_t n, const double2 *__restrict__ src, float2 *_
         dst[i] = make_float2((float)src[i].x, (float)src[i].y);
 }
 
-__global__ void k_plan_cth32(int n, const double *__restrict__ src, float *__restrict__ dst) {
+// FP64 -> FP32 (hi, lo) pairs: hi = fl32(v), lo = fl32(v - hi).
+__device__ __forceinline__ float2 split_f64(double v) {
+    const float h = (float)v;
+    return make_float2(h, (float)(v - (double)h));
+}
+
+__global__ void k_plan_cth32(int n, const double *__restrict__ src, float2 *__restrict__ dst) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) dst[i] = (float)src[i];
+    if (i < n) dst[i] = split_f64(src[i]);
+}
+
+__global__ void k_plan_coef32(int64_t n, const double2 *__restrict__ src, float4 *__restrict__ dst) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float2 a = split_f64(src[i].x), b = split_f64(src[i].y);
+        dst[i] = make_float4(a.x, a.y, b.x, b.y);
+    }
 }
 
 int glg_plan_prepare_fast(glg_plan *P, cudaStream_t st) {
@@ -298,7 +311,7 @@ int glg_plan_prepare_fast(glg_plan *P, cudaStream_t st) {
     if (e != cudaSuccess) return glg_cuda_status(e, "glg_plan_prepare_fast: upload");
     k_plan_cth32<<<(np + 255) / 256, 256, 0, st>>>(np, P->cth, P->cth32);
     k_plan_f32<<<1024, 256, 0, st>>>(ntw, P->tw, P->tw32);
-    k_plan_f32<<<1024, 256, 0, st>>>(P->nalm, P->coef, P->coef32);
+    k_plan_coef32<<<1024, 256, 0, st>>>(P->nalm, P->coef, P->coef32);
     dim3 gs((np + 127) / 128, lmax + 1);
     k_plan_seeds<<<gs, 128, 0, st>>>(lmax, np, P->cth, P->mofs, P->coef, P->lmm, P->lmm_scale,
                                      P->goff, P->seeds, P->lstart);
