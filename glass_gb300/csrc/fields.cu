@@ -119,18 +119,30 @@ __device__ __forceinline__ double2 philox_cnormal_f64(uint64_t seed, uint64_t si
 __device__ __forceinline__ float2 philox_cnormal_f32(uint64_t seed, uint64_t sid, uint64_t e) {
     const U4 x = philox4x32_10((uint32_t)e, (uint32_t)(e >> 32), (uint32_t)sid,
                                (uint32_t)(sid >> 32), (uint32_t)seed, (uint32_t)(seed >> 32));
-    // the FP64 form's 53-bit uniforms rounded to FP32 (relative error ~1e-7
-    // even deep in the tails, where u1 is small)
-    const float u1 = fmaf((float)(x.x >> 5), 67108864.0f, (float)(x.y >> 6) + 0.5f) * 1.1102230246251565e-16f;
-    const float u2 = fmaf((float)(x.z >> 5), 67108864.0f, (float)(x.w >> 6) + 0.5f) * 1.1102230246251565e-16f;
-    // 1 - u1 from the integer bits, so that log(u1) stays accurate near u1 = 1
-    const float v1 = fmaf((float)(0x7FFFFFFu - (x.x >> 5)), 67108864.0f,
-                          (float)(0x3FFFFFFu - (x.y >> 6)) + 0.5f) * 1.1102230246251565e-16f;
-    const float lg = u1 < 0.5f ? logf(u1) : log1pf(-v1);
+    // The FP64 form's 53-bit uniforms u = (K + 1/2) 2^-53, K = a 2^26 + b, held
+    // as an exact FP32 head h = (a >> 3) 2^-24 plus a small tail t, so that
+    // the FP32 normals track the FP64 ones to about one FP32 ulp.
+    const float s24 = 5.9604644775390625e-08f, s53 = 1.1102230246251565e-16f;
+    const uint32_t a1 = x.x >> 5, b1 = x.y >> 6, a2 = x.z >> 5, b2 = x.w >> 6;
+    const float h1 = (float)(a1 >> 3) * s24, t1 = ((float)((a1 & 7u) << 26 | b1) + 0.5f) * s53;
+    const float h2 = (float)(a2 >> 3) * s24, t2 = ((float)((a2 & 7u) << 26 | b2) + 0.5f) * s53;
+    float lg;
+    if (h1 >= 0.5f) {
+        // log(u1) = log1p(-v), v = 1 - u1 from the complemented bits
+        const uint32_t ca = 0x7FFFFFFu - a1, cb = 0x3FFFFFFu - b1;
+        const float vh = (float)(ca >> 3) * s24, vt = ((float)((ca & 7u) << 26 | cb) + 0.5f) * s53;
+        lg = log1pf(-vh) - vt / (1.0f - vh);
+    } else if (h1 > 0.0f) {
+        const float q = t1 / h1;  // < 1; only near u1 ~ 2^-24 is it not tiny
+        lg = logf(h1) + (q < 1e-3f ? q : log1pf(q));
+    } else {
+        lg = logf(t1);
+    }
     const float r = sqrtf(-2.0f * lg);
     float sn, cs;
-    sincospif(2.0f * u2, &sn, &cs);
-    return make_float2(r * cs, r * sn);
+    sincospif(2.0f * h2, &sn, &cs);
+    const float dphi = 6.283185307179586f * t2;  // rotate by the tail of the angle
+    return make_float2(r * (cs - sn * dphi), r * (sn + cs * dphi));
 }
 
 __global__ void k_philox_normals(uint64_t seed, uint64_t sid, int64_t offset, int64_t n, int dtype,
@@ -147,30 +159,36 @@ __global__ void k_philox_normals(uint64_t seed, uint64_t sid, int64_t offset, in
 
 // ------------------------------------------------------- alm correlation
 
-// Element (l, m) of shells t0..t0+nshell-1, written in HEALPix order.  One
-// thread per HEALPix index (coalesced stores); the thread keeps the window of
-// variates z_{t-k..t} in shared memory so each variate is read or generated
-// once per element.
+// Element (l, m) of shells t0..t0+nshell-1, written in HEALPix order.  A
+// block covers a tile of 16 consecutive l by (blockDim / 16) consecutive m:
+// the w rows of its 16 l values are staged in shared memory once per shell
+// and shared by all m of the tile, and the 16 l of one m are 16 consecutive
+// HEALPix indices, so stores stay coalesced.  Each thread keeps the window of
+// variates z_{t-k..t} of its element in shared memory, so every variate is
+// read or generated once per element.  The sum runs oldest variate first,
+// like the reference's sum over the deque (glass/fields.py:420); the fast
+// form (FP32) accumulates in FP32, the plain form in FP64.
+constexpr int CT_L = 16;
+
 template <typename T2, typename T>
 __global__ void k_alm_correlate(const double *__restrict__ w, const int nshell, const int lmax,
                                 const int k, const int64_t t0, const T2 *__restrict__ z,
                                 const int64_t z_first, const uint64_t seed, const uint64_t sid_base,
                                 T2 *__restrict__ alm, const int window) {
-    extern __shared__ unsigned char zs_raw[];
-    T2 *zs = reinterpret_cast<T2 *>(zs_raw) + (size_t)threadIdx.x * window;
-    const int64_t nalm = glg_nalm(lmax);
-    const int64_t ix = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (ix >= nalm) return;
-    // HEALPix index -> (l, m)
-    const double L2 = 2.0 * lmax + 3.0;
-    int m = (int)floor((L2 - sqrt(L2 * L2 - 8.0 * (double)ix)) * 0.5);
-    while ((int64_t)m * (2 * lmax + 3 - m) / 2 > ix) --m;
-    while ((int64_t)(m + 1) * (2 * lmax + 3 - (m + 1)) / 2 <= ix) ++m;
-    const int l = (int)(ix - (int64_t)m * (2 * lmax + 3 - m) / 2) + m;
-    const int64_t g = (int64_t)l * (l + 1) / 2 + m;  // GLASS index
-    const int L = lmax + 1;
+    extern __shared__ __align__(16) unsigned char sm_raw[];
     const int kp = k + 1;
-    // variates of shells zlo .. t0+nshell-1, ring buffer of size `window` (= k+1)
+    T *ws = reinterpret_cast<T *>(sm_raw);  // [CT_L][kp]
+    const size_t ws_bytes = ((sizeof(T) * CT_L * kp) + 15) & ~(size_t)15;
+    T2 *zs = reinterpret_cast<T2 *>(sm_raw + ws_bytes) + (size_t)threadIdx.x * window;
+    const int ctm = blockDim.x / CT_L;
+    const int l0 = blockIdx.x * CT_L, m0 = blockIdx.y * ctm;
+    if (m0 > l0 + CT_L - 1 || m0 > lmax) return;  // tile entirely above m = l
+    const int l = l0 + (int)(threadIdx.x % CT_L), m = m0 + (int)(threadIdx.x / CT_L);
+    const bool valid = l <= lmax && m <= l;
+    const int64_t nalm = glg_nalm(lmax);
+    const int64_t g = (int64_t)l * (l + 1) / 2 + m;                // GLASS index
+    const int64_t ix = (int64_t)m * (2 * lmax + 1 - m) / 2 + l;    // HEALPix index
+    const int L = lmax + 1;
     const int64_t zlo = t0 - k > 0 ? t0 - k : 0;
     auto fetch = [&](int64_t t) -> T2 {
         if (z != nullptr) return z[(t - z_first) * nalm + g];
@@ -180,26 +198,34 @@ __global__ void k_alm_correlate(const double *__restrict__ w, const int nshell, 
             return philox_cnormal_f32(seed, sid_base + (uint64_t)t, (uint64_t)g);
         }
     };
-    for (int64_t t = zlo; t < t0; ++t) zs[t % window] = fetch(t);
+    if (valid)
+        for (int64_t t = zlo; t < t0; ++t) zs[t % window] = fetch(t);
     for (int s = 0; s < nshell; ++s) {
         const int64_t t = t0 + s;
+        __syncthreads();
+        for (int q = threadIdx.x; q < CT_L * kp; q += blockDim.x) {
+            const int lg = l0 + q / kp;
+            ws[q] = lg <= lmax ? (T)w[((size_t)s * L + lg) * kp + (q % kp)] : (T)0;
+        }
+        __syncthreads();
+        if (!valid) continue;
         zs[t % window] = fetch(t);
-        const double *wt = w + ((size_t)s * L + l) * kp;
-        double re = 0.0, im = 0.0;
+        const T *wt = ws + (l - l0) * kp;
+        T re = 0, im = 0;
         const int dmax = t < k ? (int)t : k;
-        for (int d = dmax; d >= 0; --d) {  // oldest first, like the reference's sum
+        for (int d = dmax; d >= 0; --d) {
             const T2 zz = zs[(t - d) % window];
-            const double c = wt[k - d];
-            re += c * (double)zz.x;
-            im += c * (double)zz.y;
+            const T c = wt[k - d];
+            re += c * zz.x;
+            im += c * zz.y;
         }
         if (m == 0) {
             re = re + im;
-            im = 0.0;
+            im = 0;
         }
         T2 o;
-        o.x = (T)re;
-        o.y = (T)im;
+        o.x = re;
+        o.y = im;
         alm[(int64_t)s * nalm + ix] = o;
     }
 }
@@ -291,25 +317,29 @@ extern "C" int glg_alm_correlate(const double *w, int nshell, int lmax, int k, i
     GLG_REQUIRE(k <= 126, "glg_alm_correlate: k must be <= 126");
     if (z) GLG_REQUIRE(z_first == (t0 - k > 0 ? t0 - k : 0), "glg_alm_correlate: z must start at max(0, t0-k)");
     if (nshell == 0) return GLG_OK;
-    const int64_t n = glg_nalm(lmax);
     const int window = k + 1;
-    const int threads = 64;
     const size_t esz = dtype == GLG_F64 ? sizeof(double2) : sizeof(float2);
-    const size_t smem = esz * (size_t)window * threads;
+    const size_t rsz = dtype == GLG_F64 ? sizeof(double) : sizeof(float);
+    int threads = 128;  // 16 l x 8 m; fewer m per tile when the variate window is long
+    auto smem_for = [&](int th) {
+        return (((rsz * CT_L * (size_t)window) + 15) & ~(size_t)15) + esz * (size_t)window * th;
+    };
+    while (threads > CT_L && smem_for(threads) > 200 * 1024) threads /= 2;
+    const size_t smem = smem_for(threads);
     cudaStream_t st = (cudaStream_t)stream;
-    const unsigned blocks = (unsigned)((n + threads - 1) / threads);
+    dim3 grid((lmax + CT_L) / CT_L, (lmax + threads / CT_L) / (threads / CT_L));
     GLG_LAUNCH_SCOPE("k_alm_correlate", st);
     if (dtype == GLG_F64) {
         if (smem > 48 * 1024)
             cudaFuncSetAttribute(k_alm_correlate<double2, double>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_alm_correlate<double2, double><<<blocks, threads, smem, st>>>(
+        k_alm_correlate<double2, double><<<grid, threads, smem, st>>>(
             w, nshell, lmax, k, t0, (const double2 *)z, z_first, seed, sid_base, (double2 *)alm, window);
     } else {
         if (smem > 48 * 1024)
             cudaFuncSetAttribute(k_alm_correlate<float2, float>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_alm_correlate<float2, float><<<blocks, threads, smem, st>>>(
+        k_alm_correlate<float2, float><<<grid, threads, smem, st>>>(
             w, nshell, lmax, k, t0, (const float2 *)z, z_first, seed, sid_base, (float2 *)alm, window);
     }
     GLG_CHECK_LAUNCH("k_alm_correlate");

@@ -80,8 +80,23 @@ struct glg_plan {
     float4 *coef32;          // [nalm] (A_hi, A_lo, B_hi, B_lo) in FP32
     int64_t *goff;           // [mmax+2] first 16-l group of m: sum_{m'<m} ceil((lmax-m'+1)/16)
     int64_t ngroups;         // total groups
-    float2 *seeds;           // [ngroups][npairs] (lambda_s0, lambda_s0+1) per group
+    float2 *seeds;           // [ngroups][seed_stride] (lambda_s0, lambda_s0+1) per group
+    int64_t seed_stride;     // npairs rounded up to whole 128-pair tiles
     int *lstart;             // [mmax+1][npairs] first l with |lambda| >= 2^-100
+
+    // FP32 ring FFTs of the fast form.  Class 0: ring lengths whose prime
+    // factors are all <= 13 (mixed-radix DIF, output order from pos16).
+    // Class 1: lengths with a larger prime factor (Bluestein with a
+    // power-of-two length M >= 2n - 1 and a precomputed chirp spectrum).
+    int ncls0, ncls1;
+    int *cls0_pairs, *cls1_pairs;  // ring pairs of each class
+    int64_t *pos_ofs;        // [nside+1] offset of the output permutation of n = 4 i
+    uint16_t *pos16;         // DIF output position of every frequency, per length
+    int64_t *blu_ofs;        // [nside+1] offset of the chirp spectrum of n = 4 i (-1: class 0)
+    int *blu_M;              // [nside+1] Bluestein length M of n = 4 i (0: class 0)
+    float2 *blu_H;           // chirp spectra, each in DIF output order of its M
+    int blu_Mmax;
+    float2 *twM;             // [blu_Mmax / 2 + 1] exp(2 pi i t / blu_Mmax)
 };
 
 // l values per group of the fast Legendre contraction (8 even + 8 odd)
@@ -112,7 +127,7 @@ int glg_launch_ring_ana(const glg_plan *P, const double *maps, int nmaps, double
                         cudaStream_t st);
 int glg_launch_leg_ana(const glg_plan *P, const double2 *G, int nmaps, double2 *alm, int accumulate,
                        cudaStream_t st);
-int glg_launch_ring_syn_f32(const glg_plan *P, const float2 *F, int nmaps, float *maps,
+int glg_launch_ring_syn_f32(const glg_plan *P, const float2 *F, float2 *Ft, int nmaps, float *maps,
                             const glg_epilogue *epi, cudaStream_t st);
 size_t glg_leg_tc_pack_bytes(const glg_plan *P, int nmaps);
 int glg_launch_leg_tc(const glg_plan *P, const float2 *alm, int nmaps, float *bpack, float2 *F,

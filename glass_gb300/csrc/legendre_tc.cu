@@ -1,5 +1,5 @@
 // Fast form of the Legendre sums: a shells-batched contraction on the
-// sm_103a tensor cores (tcgen05, split-precision 3xTF32, FP32 accumulation).
+// sm_103a tensor cores (tcgen05, split-precision 3xTF32).
 //
 // For one ring tile (128 ring pairs, one per TMEM lane) and one m:
 //   D_E[p][n] = sum_{l-m even} lambda_lm(x_p) B[l][n],
@@ -8,19 +8,24 @@
 // (lambda_lm(-x) = (-1)^(l+m) lambda_lm(x)).  This is the work healpy does
 // inside alm2map (glass/healpix.py:71, called from glass/fields.py:429).
 //
-// lambda is generated on the fly in FP32 by the producer warps, restarting
-// every 16 l from seeds computed once per plan by an FP64 recurrence, split
-// into TF32 hi + lo parts and written straight into tensor memory (the MMA's
-// A operand).  B (the alm, split the same way) is packed per 16-l group in
-// the canonical no-swizzle K-major layout and streamed into shared memory
-// with 1-D bulk copies.  Each group issues, per parity,
-//   D += A_hi B_hi + A_hi B_lo + A_lo B_hi     (M = 128, N = 2*maps, K = 8).
+// lambda is generated on the fly in FP32 by producer warps, restarting every
+// 16 l (one "group") from seeds computed once per plan by an FP64
+// recurrence, split into TF32 hi + lo parts and written straight into tensor
+// memory as the MMA's A operand.  B (the alm, split the same way), the
+// group's seeds and its recurrence coefficients are streamed into shared
+// memory with 1-D bulk copies.  Each group issues, per parity,
+//   D += A_hi B_hi + A_hi B_lo + A_lo B_hi     (M = 128, N = 2 * maps, K = 8).
+// The tensor core's FP32 accumulation rounds toward zero, so a long chain of
+// MMAs into one accumulator drifts by ~1e-8 per step: the groups of a unit
+// are therefore accumulated in chunks of CHUNK groups into two alternating
+// TMEM accumulator sets, and drain warps add every finished chunk into FP32
+// sums in shared memory (round to nearest).
 //
-// Warp roles (320 threads): warps 0-3 and 4-7 produce lambda for alternate
-// groups (warps 0-3 also drain D after each unit), warp 8 issues the MMAs,
-// warp 9 streams B.  Every wait is bounded; on time-out the kernel records
-// GLG_ERR_TIMEOUT in *err, drains its outstanding MMAs and copies, frees its
-// tensor memory and returns.
+// Warp roles (576 threads): warps 0-11 produce lambda (three sets taking
+// every third group), warps 12-15 drain the accumulators and store F, warp 16
+// issues the MMAs, warp 17 streams B / seeds / coefficients.  Every wait is
+// bounded; on time-out the kernel records GLG_ERR_TIMEOUT in *err, retires
+// its outstanding MMAs and copies, frees its tensor memory and returns.
 #include <cuda_runtime.h>
 
 #include "glg_internal.cuh"
@@ -30,10 +35,13 @@ using namespace glg_tc;
 
 namespace {
 
-constexpr int NST = 8;            // pipeline stages (A in TMEM, B in smem)
-constexpr int A_COL0 = 256;       // first TMEM column of the A stages
+constexpr int NST = 6;            // pipeline stages (A in TMEM, B/seeds/coefs in smem)
+constexpr int NSETS = 3;          // producer warp sets
+constexpr int CHUNK = 4;          // groups accumulated per TMEM accumulator fill
 constexpr int TMEM_COLS = 512;
+constexpr int THREADS = 18 * 32;
 constexpr uint32_t WAIT_LIMIT = 1u << 22;
+constexpr int W_DRAIN = 12, W_MMA = 16, W_LOAD = 17;
 
 struct LegTcArgs {
     int npairs, nrings, lmax, nmaps, ntiles;
@@ -43,6 +51,7 @@ struct LegTcArgs {
     const int64_t *mofs;
     const int64_t *goff;
     const float2 *seeds;
+    int64_t seed_stride;
     const int *lstart;
     const unsigned char *bpack;
     float2 *F;  // [map][m][ring]
@@ -80,20 +89,28 @@ __device__ __forceinline__ int unit_m(int64_t mi, int lmax) {
 
 template <int N>
 struct Smem {
-    unsigned char b[NST][128 * N];
+    static constexpr uint32_t BBYTES = 128 * N;  // 4 tiles of N x 8 tf32
+    struct Stage {
+        unsigned char b[BBYTES];
+        float2 seed[128];      // seeds of the group's 128 ring pairs
+        float4 coef[GLG_GROUP];  // (A_hi, A_lo, B_hi, B_lo) of l = l0 .. l0+15
+    } st[NST];
+    float acc[2 * N][128];     // FP32 sums of drained chunks, [column][lane]
     uint64_t full_a[NST], full_b[NST], empty[NST];
-    uint64_t done, epi_done, drain;
+    uint64_t full_d[2], empty_d[2], drain;
     uint32_t tmem_base;
     int abort;
 };
 
 template <int N>
-__global__ void __launch_bounds__(320, 1) k_leg_tc(const LegTcArgs a) {
+__global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     Smem<N> &S = *reinterpret_cast<Smem<N> *>(smem_raw);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    constexpr uint32_t BBYTES = 128 * N;
     constexpr uint32_t IDESC = idesc_tf32(128, N);
+    constexpr uint32_t STAGE_TX = Smem<N>::BBYTES + 128 * 8 + GLG_GROUP * 16;
+    constexpr int A_COL0 = 4 * N;  // D sets at [0, 2N) and [2N, 4N)
+    static_assert(A_COL0 + 32 * NST <= TMEM_COLS, "tensor memory budget");
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < NST; ++s) {
@@ -101,12 +118,15 @@ __global__ void __launch_bounds__(320, 1) k_leg_tc(const LegTcArgs a) {
             mbar_init(&S.full_b[s], 1);
             mbar_init(&S.empty[s], 1);
         }
-        mbar_init(&S.done, 1);
-        mbar_init(&S.epi_done, 4);
+        for (int d = 0; d < 2; ++d) {
+            mbar_init(&S.full_d[d], 1);
+            mbar_init(&S.empty_d[d], 4);
+        }
         mbar_init(&S.drain, 1);
         S.abort = 0;
         fence_barrier_init();
     }
+    for (int i = threadIdx.x; i < 2 * N * 128; i += THREADS) (&S.acc[0][0])[i] = 0.f;
     if (warp == 0) {
         tmem_alloc(&S.tmem_base, TMEM_COLS);
         tmem_relinquish();
@@ -128,37 +148,35 @@ __global__ void __launch_bounds__(320, 1) k_leg_tc(const LegTcArgs a) {
         fail();
         return false;
     };
-
     const int lmax = a.lmax;
-    if (warp < 8) {
-        // ---------------------------------------------------- lambda producers
+    const uint32_t lane_base = (uint32_t)((warp & 3) << 5) << 16;
+    const int r = ((warp & 3) << 5) + lane;  // TMEM lane = ring pair in tile
+
+    if (warp < W_DRAIN) {
+        // ------------------------------------------------ lambda producers
         const int set = warp >> 2;
-        const int r = ((warp & 3) << 5) + lane;  // TMEM lane = ring pair in tile
-        const uint32_t lane_base = (uint32_t)((warp & 3) << 5) << 16;
-        int64_t gc = 0, ui = 0;
+        int64_t gc = 0;
         bool ok = true;
-        for (int64_t u = blockIdx.x; u < a.nunits && ok; u += gridDim.x, ++ui) {
+        for (int64_t u = blockIdx.x; u < a.nunits && ok; u += gridDim.x) {
             const int tile = (int)(u % a.ntiles);
             const int m = unit_m(u / a.ntiles, lmax);
             const int G = (lmax - m + GLG_GROUP) / GLG_GROUP;
             const int p = tile * 128 + r;
             const bool live = p < a.npairs;
             const int pp = live ? p : a.npairs - 1;
-            const float2 x = a.cth32[pp];  // cos theta as (hi, lo)
+            const float2 x = a.cth32[pp];
             const int ls = live ? a.lstart[(int64_t)m * a.npairs + pp] : lmax + 1;
-            const int64_t mb = a.mofs[m];
-            const int64_t gb = a.goff[m];
-            for (int g = 0; g < G; ++g) {
+            for (int g = (int)((set - gc % NSETS + NSETS) % NSETS); g < G; g += NSETS) {
                 const int64_t gg = gc + g;
-                if ((int)(gg & 1) != set) continue;
                 const int s = (int)(gg % NST);
-                const int64_t use = gg / NST;
-                if (use > 0 && !wait(&S.empty[s], (uint32_t)((use - 1) & 1))) { ok = false; break; }
+                const uint32_t par = (uint32_t)((gg / NST) & 1);
+                if (gg >= NST && !wait(&S.empty[s], par ^ 1u)) { ok = false; break; }
+                if (!wait(&S.full_b[s], par)) { ok = false; break; }
                 fence_after_sync();
+                const typename Smem<N>::Stage &sg = S.st[s];
                 const int l0 = m + g * GLG_GROUP;
                 const int s0 = l0 > ls ? l0 : ls;
-                float2 seed = make_float2(0.f, 0.f);
-                if (s0 <= l0 + GLG_GROUP - 1 && s0 <= lmax) seed = a.seeds[(gb + g) * a.npairs + pp];
+                const float2 seed = sg.seed[r];
                 float lm2 = 0.f, lm1 = 0.f;
                 uint32_t ehi[8], elo[8], ohi[8], olo[8];
 #pragma unroll
@@ -172,7 +190,7 @@ __global__ void __launch_bounds__(320, 1) k_leg_tc(const LegTcArgs a) {
                     } else if (l == s0 + 1) {
                         v = seed.y;
                     } else {
-                        v = rec_step_comp(__ldg(a.coef32 + mb + (l - m)), x, lm1, lm2);
+                        v = rec_step_comp(sg.coef[j], x, lm1, lm2);
                     }
                     lm2 = lm1;
                     lm1 = v;
@@ -197,73 +215,87 @@ __global__ void __launch_bounds__(320, 1) k_leg_tc(const LegTcArgs a) {
                 if (lane == 0) mbar_arrive(&S.full_a[s]);
             }
             gc += G;
-            if (!ok) break;
-            if (set == 0) {
-                // ------------------------------------------------- epilogue
-                if (!wait(&S.done, (uint32_t)(ui & 1))) { ok = false; break; }
+        }
+        if (!ok) fail();
+    } else if (warp < W_MMA) {
+        // --------------------------------- drain: chunk sums -> smem -> F
+        int64_t cc = 0;  // chunk counter across units
+        bool ok = true;
+        for (int64_t u = blockIdx.x; u < a.nunits && ok; u += gridDim.x) {
+            const int tile = (int)(u % a.ntiles);
+            const int m = unit_m(u / a.ntiles, lmax);
+            const int G = (lmax - m + GLG_GROUP) / GLG_GROUP;
+            const int nch = (G + CHUNK - 1) / CHUNK;
+            for (int c = 0; c < nch; ++c, ++cc) {
+                const int d = (int)(cc & 1);
+                if (!wait(&S.full_d[d], (uint32_t)((cc >> 1) & 1))) { ok = false; break; }
                 fence_after_sync();
-                const int rs = a.nrings - 1 - p;
-                for (int c0 = 0; c0 < N; c0 += 16) {
-                    uint32_t e[16], o[16];
-                    tmem_ld16(tb + lane_base + c0, e);
-                    tmem_ld16(tb + lane_base + N + c0, o);
+                for (int c0 = 0; c0 < 2 * N; c0 += 16) {
+                    uint32_t v[16];
+                    tmem_ld16(tb + lane_base + 2 * N * d + c0, v);
                     tmem_wait_ld();
-                    if (live) {
 #pragma unroll
-                        for (int j = 0; j < 16; j += 2) {
-                            const int map = (c0 + j) >> 1;
-                            if (map < a.nmaps) {
-                                const float er = __uint_as_float(e[j]), ei = __uint_as_float(e[j + 1]);
-                                const float orr = __uint_as_float(o[j]), oi = __uint_as_float(o[j + 1]);
-                                float2 *Fm = a.F + ((int64_t)map * (lmax + 1) + m) * a.nrings;
-                                Fm[p] = make_float2(er + orr, ei + oi);
-                                if (rs != p) Fm[rs] = make_float2(er - orr, ei - oi);
-                            }
-                        }
-                    }
+                    for (int j = 0; j < 16; ++j) S.acc[c0 + j][r] += __uint_as_float(v[j]);
                 }
                 fence_before_sync();
                 __syncwarp();
-                if (lane == 0) mbar_arrive(&S.epi_done);
+                if (lane == 0) mbar_arrive(&S.empty_d[d]);
             }
+            if (!ok) break;
+            // unit complete: north = E + O, south = E - O
+            const int p = tile * 128 + r;
+            if (p < a.npairs) {
+                const int rs = a.nrings - 1 - p;
+                for (int map = 0; map < a.nmaps; ++map) {
+                    const float er = S.acc[2 * map][r], ei = S.acc[2 * map + 1][r];
+                    const float orr = S.acc[N + 2 * map][r], oi = S.acc[N + 2 * map + 1][r];
+                    float2 *Fm = a.F + ((int64_t)map * (lmax + 1) + m) * a.nrings;
+                    Fm[p] = make_float2(er + orr, ei + oi);
+                    if (rs != p) Fm[rs] = make_float2(er - orr, ei - oi);
+                }
+            }
+            for (int c0 = 0; c0 < 2 * N; ++c0) S.acc[c0][r] = 0.f;
         }
         if (!ok) fail();
-    } else if (warp == 8) {
+    } else if (warp == W_MMA) {
         // ---------------------------------------------------------- MMA issue
         if (lane == 0) {
-            int64_t gc = 0, ui = 0;
-            bool ok = true;
-            bool issued = false;
-            for (int64_t u = blockIdx.x; u < a.nunits && ok; u += gridDim.x, ++ui) {
+            int64_t gc = 0, cc = 0;
+            bool ok = true, issued = false;
+            for (int64_t u = blockIdx.x; u < a.nunits && ok; u += gridDim.x) {
                 const int m = unit_m(u / a.ntiles, lmax);
                 const int G = (lmax - m + GLG_GROUP) / GLG_GROUP;
-                if (ui > 0 && !wait(&S.epi_done, (uint32_t)((ui - 1) & 1))) { ok = false; break; }
-                fence_after_sync();
-                for (int g = 0; g < G; ++g) {
-                    const int64_t gg = gc + g;
-                    const int s = (int)(gg % NST);
-                    const uint32_t par = (uint32_t)((gg / NST) & 1);
-                    if (!wait(&S.full_a[s], par) || !wait(&S.full_b[s], par)) { ok = false; break; }
+                for (int g = 0; g < G && ok; g += CHUNK, ++cc) {
+                    const int d = (int)(cc & 1);
+                    if (cc >= 2 && !wait(&S.empty_d[d], (uint32_t)(((cc >> 1) - 1) & 1))) { ok = false; break; }
                     fence_after_sync();
-                    const uint32_t acol = tb + A_COL0 + 32 * s;
-                    const uint32_t bb = smem_u32(S.b[s]);
-                    const uint32_t tsz = 32 * N;  // bytes of one B tile
-                    const uint64_t bEh = sdesc_noswz(bb, 128, 256), bEl = sdesc_noswz(bb + tsz, 128, 256);
-                    const uint64_t bOh = sdesc_noswz(bb + 2 * tsz, 128, 256);
-                    const uint64_t bOl = sdesc_noswz(bb + 3 * tsz, 128, 256);
-                    const uint32_t acc = g > 0 ? 1u : 0u;
-                    mma_tf32_ts(tb, acol + 0, bEh, IDESC, acc);
-                    mma_tf32_ts(tb, acol + 0, bEl, IDESC, 1u);
-                    mma_tf32_ts(tb, acol + 8, bEh, IDESC, 1u);
-                    mma_tf32_ts(tb + N, acol + 16, bOh, IDESC, acc);
-                    mma_tf32_ts(tb + N, acol + 16, bOl, IDESC, 1u);
-                    mma_tf32_ts(tb + N, acol + 24, bOh, IDESC, 1u);
-                    mma_commit(&S.empty[s]);
-                    issued = true;
+                    const uint32_t dE = tb + 2 * N * d, dO = dE + N;
+                    const int gend = g + CHUNK < G ? g + CHUNK : G;
+                    for (int q = g; q < gend; ++q) {
+                        const int64_t gg = gc + q;
+                        const int s = (int)(gg % NST);
+                        const uint32_t par = (uint32_t)((gg / NST) & 1);
+                        if (!wait(&S.full_a[s], par) || !wait(&S.full_b[s], par)) { ok = false; break; }
+                        fence_after_sync();
+                        const uint32_t acol = tb + A_COL0 + 32 * s;
+                        const uint32_t bb = smem_u32(S.st[s].b);
+                        constexpr uint32_t tsz = 32 * N;  // bytes of one B tile
+                        const uint64_t bEh = sdesc_noswz(bb, 128, 256), bEl = sdesc_noswz(bb + tsz, 128, 256);
+                        const uint64_t bOh = sdesc_noswz(bb + 2 * tsz, 128, 256);
+                        const uint64_t bOl = sdesc_noswz(bb + 3 * tsz, 128, 256);
+                        const uint32_t acc = q > g ? 1u : 0u;
+                        mma_tf32_ts(dE, acol + 0, bEh, IDESC, acc);
+                        mma_tf32_ts(dE, acol + 0, bEl, IDESC, 1u);
+                        mma_tf32_ts(dE, acol + 8, bEh, IDESC, 1u);
+                        mma_tf32_ts(dO, acol + 16, bOh, IDESC, acc);
+                        mma_tf32_ts(dO, acol + 16, bOl, IDESC, 1u);
+                        mma_tf32_ts(dO, acol + 24, bOh, IDESC, 1u);
+                        mma_commit(&S.empty[s]);
+                        issued = true;
+                    }
+                    if (ok) mma_commit(&S.full_d[d]);
                 }
                 gc += G;
-                if (!ok) break;
-                mma_commit(&S.done);
             }
             if (!ok) fail();
             if (issued) {  // every MMA of this CTA retired before TMEM is freed
@@ -274,23 +306,28 @@ __global__ void __launch_bounds__(320, 1) k_leg_tc(const LegTcArgs a) {
         }
         __syncwarp();
     } else {
-        // -------------------------------------------------------- B streaming
+        // ------------------------------------- B / seeds / coefficient streaming
         if (lane == 0) {
             int64_t gc = 0;
             bool ok = true;
             int64_t last_use[NST];
             for (int s = 0; s < NST; ++s) last_use[s] = -1;
             for (int64_t u = blockIdx.x; u < a.nunits && ok; u += gridDim.x) {
+                const int tile = (int)(u % a.ntiles);
                 const int m = unit_m(u / a.ntiles, lmax);
                 const int G = (lmax - m + GLG_GROUP) / GLG_GROUP;
                 const int64_t gb = a.goff[m];
+                const int64_t cb = a.mofs[m];
                 for (int g = 0; g < G; ++g) {
                     const int64_t gg = gc + g;
                     const int s = (int)(gg % NST);
                     const int64_t use = gg / NST;
                     if (use > 0 && !wait(&S.empty[s], (uint32_t)((use - 1) & 1))) { ok = false; break; }
-                    mbar_arrive_expect_tx(&S.full_b[s], BBYTES);
-                    bulk_g2s(S.b[s], a.bpack + (size_t)(gb + g) * BBYTES, BBYTES, &S.full_b[s]);
+                    typename Smem<N>::Stage &sg = S.st[s];
+                    mbar_arrive_expect_tx(&S.full_b[s], STAGE_TX);
+                    bulk_g2s(sg.b, a.bpack + (size_t)(gb + g) * Smem<N>::BBYTES, Smem<N>::BBYTES, &S.full_b[s]);
+                    bulk_g2s(sg.seed, a.seeds + (gb + g) * a.seed_stride + (int64_t)tile * 128, 128 * 8, &S.full_b[s]);
+                    bulk_g2s(sg.coef, a.coef32 + cb + (int64_t)g * GLG_GROUP, GLG_GROUP * 16, &S.full_b[s]);
                     last_use[s] = use;
                 }
                 gc += G;
@@ -367,6 +404,7 @@ int launch_tc(const glg_plan *P, const float2 *alm, int nmaps, float *bpack, flo
     a.mofs = P->mofs;
     a.goff = P->goff;
     a.seeds = P->seeds;
+    a.seed_stride = P->seed_stride;
     a.lstart = P->lstart;
     a.bpack = reinterpret_cast<const unsigned char *>(bpack);
     a.F = F;
@@ -381,7 +419,7 @@ int launch_tc(const glg_plan *P, const float2 *alm, int nmaps, float *bpack, flo
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     const int64_t grid = a.nunits < nsm ? a.nunits : nsm;
     GLG_LAUNCH_SCOPE("k_leg_tc", st);
-    k_leg_tc<N><<<(unsigned)grid, 320, smem, st>>>(a);
+    k_leg_tc<N><<<(unsigned)grid, THREADS, smem, st>>>(a);
     GLG_CHECK_LAUNCH("k_leg_tc");
     return GLG_OK;
 }
@@ -402,11 +440,8 @@ int glg_launch_leg_tc(const glg_plan *P, const float2 *alm, int nmaps, float *bp
         case 48: return launch_tc<48>(P, alm, nmaps, bpack, F, err, st);
         case 64: return launch_tc<64>(P, alm, nmaps, bpack, F, err, st);
         case 80: return launch_tc<80>(P, alm, nmaps, bpack, F, err, st);
-        case 96: return launch_tc<96>(P, alm, nmaps, bpack, F, err, st);
-        case 112: return launch_tc<112>(P, alm, nmaps, bpack, F, err, st);
-        case 128: return launch_tc<128>(P, alm, nmaps, bpack, F, err, st);
         default:
-            glg_set_error("fast Legendre contraction: at most 64 maps per launch");
+            glg_set_error("fast Legendre contraction: at most 40 maps per launch");
             return GLG_ERR_UNSUPPORTED;
     }
 }

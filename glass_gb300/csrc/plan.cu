@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include <complex>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -201,7 +202,8 @@ extern "C" void glg_plan_destroy(glg_plan *P) {
     void *ptrs[] = {P->cth,   P->sth,       P->nph,     P->half,   P->startN, P->startS,
                     P->mofs,  P->coef,      P->lmm,     P->lmm_scale, P->fft_radix,
                     P->fft_nst, P->tw_ofs,  P->tw,      P->cth32,  P->tw32,   P->coef32,
-                    P->goff,  P->seeds,     P->lstart};
+                    P->goff,  P->seeds,     P->lstart,  P->cls0_pairs, P->cls1_pairs,
+                    P->pos_ofs, P->pos16,   P->blu_ofs, P->blu_M,  P->blu_H,  P->twM};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     delete P;
@@ -218,7 +220,7 @@ __global__ void k_plan_seeds(int lmax, int npairs, const double *__restrict__ ct
                              const int64_t *__restrict__ mofs, const double2 *__restrict__ coef,
                              const double *__restrict__ lmm, const int *__restrict__ lmm_scale,
                              const int64_t *__restrict__ goff, float2 *__restrict__ seeds,
-                             int *__restrict__ lstart) {
+                             int64_t sstride, int *__restrict__ lstart) {
     const int m = blockIdx.y;
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= npairs) return;
@@ -253,7 +255,7 @@ __global__ void k_plan_seeds(int lmax, int npairs, const double *__restrict__ ct
         const int j = (l - m) / GLG_GROUP;
         const int lg0 = m + j * GLG_GROUP;
         if (pend >= 0) {  // l == s0 + 1 of the pending seed
-            seeds[pend * npairs + p] = make_float2(sx, (float)tv);
+            seeds[pend * sstride + p] = make_float2(sx, (float)tv);
             pend = -1;
         }
         if (ls >= 0 && l == (lg0 > ls ? lg0 : ls)) {
@@ -261,9 +263,9 @@ __global__ void k_plan_seeds(int lmax, int npairs, const double *__restrict__ ct
             pend = g0 + j;
         }
         const bool group_end = ((l - m) % GLG_GROUP == GLG_GROUP - 1) || l == lmax;
-        if (group_end && ls < 0) seeds[(g0 + j) * npairs + p] = make_float2(0.f, 0.f);
+        if (group_end && ls < 0) seeds[(g0 + j) * sstride + p] = make_float2(0.f, 0.f);
     }
-    if (pend >= 0) seeds[pend * npairs + p] = make_float2(sx, 0.f);
+    if (pend >= 0) seeds[pend * sstride + p] = make_float2(sx, 0.f);
     lstart[(int64_t)m * npairs + p] = ls < 0 ? lmax + 1 : ls;
 }
 
@@ -290,6 +292,120 @@ __global__ void k_plan_coef32(int64_t n, const double2 *__restrict__ src, float4
     }
 }
 
+// Output position of frequency k after in-place DIF passes with `radix`.
+static int dif_pos_host(const int *radix, int nst, int n, int k) {
+    int pos = 0, span = n;
+    for (int s = 0; s < nst; ++s) {
+        span /= radix[s];
+        pos += (k % radix[s]) * span;
+        k /= radix[s];
+    }
+    return pos;
+}
+
+// In-place iterative radix-2 FFT, sum_t x_t e^{-2 pi i k t / M}, FP64 (host).
+static void fft_pow2_host(std::vector<std::complex<double>> &x) {
+    const size_t M = x.size();
+    for (size_t i = 1, j = 0; i < M; ++i) {
+        size_t bit = M >> 1;
+        for (; j & bit; bit >>= 1) j ^= bit;
+        j ^= bit;
+        if (i < j) std::swap(x[i], x[j]);
+    }
+    for (size_t len = 2; len <= M; len <<= 1) {
+        const double ang = -2.0 * M_PI / (double)len;
+        for (size_t i = 0; i < M; i += len)
+            for (size_t k = 0; k < len / 2; ++k) {
+                const std::complex<double> w(cos(ang * (double)k), sin(ang * (double)k));
+                const std::complex<double> u = x[i + k], v = x[i + k + len / 2] * w;
+                x[i + k] = u + v;
+                x[i + k + len / 2] = u - v;
+            }
+    }
+}
+
+// Host-built tables of the FP32 ring FFTs: ring classes, DIF output orders
+// and the Bluestein chirp spectra H = DFT_M(h), h_t = e^{-i pi t^2 / n} for
+// |t| < n (indices mod M), stored in the DIF output order of M.
+static int build_fft32_tables(glg_plan *P, cudaStream_t st) {
+    const int nside = P->nside;
+    std::vector<int> radix((size_t)(nside + 1) * GLG_MAX_FFT_STAGES), nst(nside + 1, 0);
+    std::vector<int64_t> pos_ofs(nside + 2, 0), blu_ofs(nside + 1, -1);
+    std::vector<int> blu_M(nside + 1, 0);
+    int64_t nblu = 0;
+    int Mmax = 4;
+    for (int i = 1; i <= nside; ++i) {
+        int *r = &radix[(size_t)i * GLG_MAX_FFT_STAGES];
+        factor_ring(4 * i, r, &nst[i]);
+        pos_ofs[i + 1] = pos_ofs[i] + 4LL * i;
+        bool large = false;
+        for (int s = 0; s < nst[i]; ++s) large |= r[s] > 13;
+        if (large) {
+            int M = 1;
+            while (M < 2 * 4 * i - 1) M <<= 1;
+            blu_M[i] = M;
+            blu_ofs[i] = nblu;
+            nblu += M;
+            if (M > Mmax) Mmax = M;
+        }
+    }
+    std::vector<uint16_t> pos16(pos_ofs[nside + 1]);
+    for (int i = 1; i <= nside; ++i)
+        for (int k = 0; k < 4 * i; ++k)
+            pos16[pos_ofs[i] + k] = (uint16_t)dif_pos_host(&radix[(size_t)i * GLG_MAX_FFT_STAGES], nst[i], 4 * i, k);
+    std::vector<float2> H((size_t)(nblu > 0 ? nblu : 1));
+    for (int i = 1; i <= nside; ++i) {
+        const int M = blu_M[i];
+        if (!M) continue;
+        const int n = 4 * i;
+        std::vector<std::complex<double>> h(M, 0.0);
+        for (int t = 0; t < n; ++t) {
+            const double ph = -M_PI * (double)(((int64_t)t * t) % (2LL * n)) / n;
+            h[t] = std::complex<double>(cos(ph), sin(ph));
+            if (t > 0) h[M - t] = h[t];
+        }
+        fft_pow2_host(h);
+        int mr[GLG_MAX_FFT_STAGES], mns = 0;
+        factor_ring(M, mr, &mns);
+        for (int k = 0; k < M; ++k) {
+            const int q = dif_pos_host(mr, mns, M, k);
+            H[blu_ofs[i] + q] = make_float2((float)h[k].real(), (float)h[k].imag());
+        }
+    }
+    std::vector<float2> twM(Mmax / 2 + 1);
+    for (int t = 0; t <= Mmax / 2; ++t)
+        twM[t] = make_float2((float)cos(2.0 * M_PI * t / Mmax), (float)sin(2.0 * M_PI * t / Mmax));
+    std::vector<int> c0, c1;
+    for (int p = 0; p < P->npairs; ++p) {
+        const int i = p + 1 < nside ? p + 1 : nside;
+        (blu_M[i] ? c1 : c0).push_back(p);
+    }
+    P->ncls0 = (int)c0.size();
+    P->ncls1 = (int)c1.size();
+    P->blu_Mmax = Mmax;
+    int rc;
+    if ((rc = dalloc(P, &P->cls0_pairs, c0.size())) || (rc = dalloc(P, &P->cls1_pairs, c1.size())) ||
+        (rc = dalloc(P, &P->pos_ofs, pos_ofs.size())) || (rc = dalloc(P, &P->pos16, pos16.size())) ||
+        (rc = dalloc(P, &P->blu_ofs, blu_ofs.size())) || (rc = dalloc(P, &P->blu_M, blu_M.size())) ||
+        (rc = dalloc(P, &P->blu_H, H.size())) || (rc = dalloc(P, &P->twM, twM.size())))
+        return rc;
+    cudaError_t e = cudaSuccess;
+    auto up = [&](void *dst, const void *src, size_t bytes) {
+        if (e == cudaSuccess && bytes) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st);
+    };
+    up(P->cls0_pairs, c0.data(), sizeof(int) * c0.size());
+    up(P->cls1_pairs, c1.data(), sizeof(int) * c1.size());
+    up(P->pos_ofs, pos_ofs.data(), sizeof(int64_t) * pos_ofs.size());
+    up(P->pos16, pos16.data(), sizeof(uint16_t) * pos16.size());
+    up(P->blu_ofs, blu_ofs.data(), sizeof(int64_t) * blu_ofs.size());
+    up(P->blu_M, blu_M.data(), sizeof(int) * blu_M.size());
+    up(P->blu_H, H.data(), sizeof(float2) * H.size());
+    up(P->twM, twM.data(), sizeof(float2) * twM.size());
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // host vectors go out of scope
+    if (e != cudaSuccess) return glg_cuda_status(e, "glg_plan_prepare_fast: FFT tables");
+    return GLG_OK;
+}
+
 int glg_plan_prepare_fast(glg_plan *P, cudaStream_t st) {
     static std::mutex mu;
     std::lock_guard<std::mutex> lk(mu);
@@ -300,24 +416,31 @@ int glg_plan_prepare_fast(glg_plan *P, cudaStream_t st) {
         goff[m + 1] = goff[m] + (lmax - m + 1 + GLG_GROUP - 1) / GLG_GROUP;
     P->ngroups = goff[lmax + 1];
     const int64_t ntw = 4LL * P->nside * (P->nside + 1);
+    // seed rows padded to whole 128-pair tiles, and 16 spare coefficient
+    // entries: the contraction copies whole tiles / whole groups per stage
+    P->seed_stride = (int64_t)((np + 127) / 128) * 128;
     int rc;
     if ((rc = dalloc(P, &P->cth32, np)) || (rc = dalloc(P, &P->tw32, ntw)) ||
-        (rc = dalloc(P, &P->coef32, P->nalm)) || (rc = dalloc(P, &P->goff, lmax + 2)) ||
-        (rc = dalloc(P, &P->seeds, (size_t)P->ngroups * np)) ||
+        (rc = dalloc(P, &P->coef32, P->nalm + GLG_GROUP)) || (rc = dalloc(P, &P->goff, lmax + 2)) ||
+        (rc = dalloc(P, &P->seeds, (size_t)P->ngroups * P->seed_stride)) ||
         (rc = dalloc(P, &P->lstart, (size_t)(lmax + 1) * np)))
         return rc;
     cudaError_t e = cudaMemcpyAsync(P->goff, goff.data(), sizeof(int64_t) * goff.size(),
                                     cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(P->seeds, 0, sizeof(float2) * (size_t)P->ngroups * P->seed_stride, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(P->coef32, 0, sizeof(float4) * (size_t)(P->nalm + GLG_GROUP), st);
     if (e != cudaSuccess) return glg_cuda_status(e, "glg_plan_prepare_fast: upload");
     k_plan_cth32<<<(np + 255) / 256, 256, 0, st>>>(np, P->cth, P->cth32);
     k_plan_f32<<<1024, 256, 0, st>>>(ntw, P->tw, P->tw32);
     k_plan_coef32<<<1024, 256, 0, st>>>(P->nalm, P->coef, P->coef32);
     dim3 gs((np + 127) / 128, lmax + 1);
     k_plan_seeds<<<gs, 128, 0, st>>>(lmax, np, P->cth, P->mofs, P->coef, P->lmm, P->lmm_scale,
-                                     P->goff, P->seeds, P->lstart);
+                                     P->goff, P->seeds, P->seed_stride, P->lstart);
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return glg_cuda_status(e, "glg_plan_prepare_fast");
+    if ((rc = build_fft32_tables(P, st))) return rc;
     P->fast_ready = true;
     return GLG_OK;
 }

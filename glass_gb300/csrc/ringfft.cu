@@ -363,12 +363,6 @@ int glg_launch_ring_syn(const glg_plan *P, const double2 *F, int nmaps, double *
     return launch_ring_syn<double>(P, P->tw, F, fl, nmaps, maps, epi, st);
 }
 
-// FP32 synthesis from F laid out [map][m][ring] (the fast contraction's output).
-int glg_launch_ring_syn_f32(const glg_plan *P, const float2 *F, int nmaps, float *maps,
-                            const glg_epilogue *epi, cudaStream_t st) {
-    const FLayout fl{(int64_t)P->nrings * (P->mmax + 1), 1, (int64_t)P->nrings};
-    return launch_ring_syn<float>(P, P->tw32, F, fl, nmaps, maps, epi, st);
-}
 
 int glg_launch_ring_ana(const glg_plan *P, const double *maps, int nmaps, double2 *G,
                         cudaStream_t st) {

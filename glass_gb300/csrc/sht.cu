@@ -29,9 +29,9 @@ static size_t fast_pack_bytes(const glg_plan *P, int nmaps) {
 
 extern "C" size_t glg_alm2map_workspace(const glg_plan *P, int nmaps, int form) {
     if (!P || nmaps <= 0) return 0;
-    if (form == GLG_FORM_FAST)
+    if (form == GLG_FORM_FAST)  // status | B pack | F [map][m][ring] | F [map][ring][m]
         return GLG_WS_STATUS_BYTES + fast_pack_bytes(P, nmaps) +
-               sizeof(float2) * (size_t)nmaps * P->nrings * (P->mmax + 1);
+               2 * sizeof(float2) * (size_t)nmaps * P->nrings * (P->mmax + 1);
     return ring_coef_bytes(P, nmaps);
 }
 
@@ -46,7 +46,7 @@ extern "C" int glg_alm2map(const glg_plan *P, const void *alm, int nmaps, int fo
                 "glg_alm2map: workspace too small");
     cudaStream_t st = (cudaStream_t)stream;
     if (form == GLG_FORM_FAST) {
-        GLG_REQUIRE(nmaps <= 64, "glg_alm2map: the fast form takes at most 64 maps per call");
+        GLG_REQUIRE(nmaps <= 40, "glg_alm2map: the fast form takes at most 40 maps per call");
         int rc = glg_plan_prepare_fast(const_cast<glg_plan *>(P), st);
         if (rc) return rc;
         int *err = (int *)ws;
@@ -54,9 +54,10 @@ extern "C" int glg_alm2map(const glg_plan *P, const void *alm, int nmaps, int fo
         float2 *F = (float2 *)((char *)ws + GLG_WS_STATUS_BYTES + fast_pack_bytes(P, nmaps));
         cudaError_t e = cudaMemsetAsync(err, 0, GLG_WS_STATUS_BYTES, st);
         if (e != cudaSuccess) return glg_cuda_status(e, "glg_alm2map: status reset");
+        float2 *Ft = F + (size_t)nmaps * P->nrings * (P->mmax + 1);
         rc = glg_launch_leg_tc(P, (const float2 *)alm, nmaps, bpack, F, err, st);
         if (rc) return rc;
-        return glg_launch_ring_syn_f32(P, F, nmaps, (float *)maps, epi, st);
+        return glg_launch_ring_syn_f32(P, F, Ft, nmaps, (float *)maps, epi, st);
     }
     double2 *F = (double2 *)ws;
     int rc = glg_launch_leg_syn(P, (const double2 *)alm, nmaps, F, st);

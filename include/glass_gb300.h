@@ -130,7 +130,7 @@ typedef struct glg_epilogue {
  *   the tensor cores as split-precision 3xTF32 with FP32 accumulation,
  *   lambda_lm from an FP32 recurrence restarted every 16 l from FP64 seeds
  *   (built once per plan on first use; that first call synchronises the
- *   stream); at most 64 maps per call.
+ *   stream); at most 40 maps per call; nside <= 2048.
  * workspace: device scratch of glg_alm2map_workspace() bytes.  For the fast
  * form its first int receives GLG_ERR_TIMEOUT if a bounded device wait gave
  * up; glg_workspace_status() reads it.
