@@ -63,6 +63,7 @@ _SIGNATURES = {
     "glg_alm2map_workspace": ([c_p, c_i, c_i], c_sz),
     "glg_alm2map": ([c_p, c_p, c_i, c_i, c_p, ctypes.POINTER(Epilogue), c_p, c_sz, c_p], c_i),
     "glg_workspace_status": ([c_p, c_p], c_i),
+    "glg_alm2map_noalloc": ([c_i, c_i, c_p, c_i, c_p, c_p], c_i),
     "glg_alm2map_spin_workspace": ([c_p], c_sz),
     "glg_alm2map_spin": ([c_p, c_p, c_p, c_i, c_p, c_p, c_p, c_sz, c_p], c_i),
     "glg_map2alm_workspace": ([c_p, c_i], c_sz),

@@ -164,6 +164,25 @@ int glg_map2alm(const glg_plan *plan, const void *maps, int nmaps, int niter, vo
                 void *workspace, size_t workspace_bytes, void *stream);
 
 /*
+ * Spin-0 synthesis that allocates nothing.  No counterpart in the reference:
+ * it exists for callers that cannot call cudaMalloc where they need a map --
+ * code inside CUDA stream capture (allocation cannot be captured), loops
+ * whose device memory is fixed at start-up, or programs whose device memory
+ * belongs to an allocator that must not be bypassed.  It needs no plan and no
+ * workspace: alm complex128 [nmaps][nalm] (HEALPix order, lmax), maps float64
+ * [nmaps][npix]; FP64 throughout, same result as glg_alm2map's plain form.
+ * Its scratch is one fixed array of GLG_NOALLOC_SCRATCH_BYTES in the
+ * library's device memory, held by every GPU that loads the library until
+ * the process exits.  Limits: nside <= 256 and
+ * nmaps * (4 nside - 1) * (lmax + 1) * 16 <= GLG_NOALLOC_SCRATCH_BYTES, else
+ * GLG_ERR_UNSUPPORTED.  All calls share that array: calls that overlap on the
+ * GPU race, so serialise them.  The first call on each device looks up the
+ * array's address; make it before any stream capture begins.
+ */
+#define GLG_NOALLOC_SCRATCH_BYTES (16u << 20)
+int glg_alm2map_noalloc(int nside, int lmax, const void *alm, int nmaps, void *maps, void *stream);
+
+/*
  * Launch accounting (no counterpart in the reference, which has no GPU
  * code): every kernel launch of this library is counted; with timing
  * enabled each launch is bracketed by CUDA events on its own stream and
