@@ -57,6 +57,7 @@ _SIGNATURES = {
                        ctypes.POINTER(c_i64), ctypes.POINTER(c_i64)], c_i),
     "glg_iternorm": ([c_p, c_i64, c_i64, c_i, c_p, c_p, c_p], c_i),
     "glg_philox_normals": ([c_u64, c_u64, c_i64, c_i64, c_i, c_p, c_p], c_i),
+    "glg_cls2cov": ([c_p, c_p, c_i, c_i, c_i, c_p, c_p, c_p, c_p], c_i),
     "glg_alm_correlate": ([c_p, c_i, c_i, c_i, c_i64, c_p, c_i64, c_u64, c_u64, c_i, c_p, c_p], c_i),
     "glg_multalm": ([c_p, c_p, c_i, c_i, c_p, c_p], c_i),
     "glg_almxfl": ([c_p, c_p, c_i, c_i, c_i, c_i, c_p, c_p], c_i),

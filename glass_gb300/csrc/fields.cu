@@ -81,6 +81,54 @@ k_iternorm(const double *__restrict__ cov, const int64_t nrows, const int64_t nl
     }
 }
 
+// ----------------------------------------------------------------- cls2cov
+
+// cov[j][l][i] = C^{j,j-i}_l / 2 for i <= min(j, nc) and l < len(C^{j,j-i}),
+// else 0 (glass/fields.py:191-236); spectra in GLASS order, concatenated in
+// `flat` with offsets `offs` (spectrum q = offs[q] .. offs[q+1]-1).
+__global__ void k_cls2cov(const double *__restrict__ flat, const int64_t *__restrict__ offs, int nf,
+                          int nl, int nc, double *__restrict__ cov) {
+    const int j = blockIdx.y;
+    const int l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= nl) return;
+    double *row = cov + ((int64_t)j * nl + l) * (nc + 1);
+    const int64_t base = (int64_t)j * (j + 1) / 2;
+    for (int i = 0; i <= nc; ++i) {
+        double v = 0.0;
+        if (i <= j) {
+            const int64_t o = offs[base + i], len = offs[base + i + 1] - o;
+            if (l < len) v = flat[o + l] / 2;
+        }
+        row[i] = v;
+    }
+}
+
+// var[j] = sum_l (2l+1)/(4 pi) C^{jj}_l (the variance transformcl.cltovar
+// gives, glass/fields.py:890); *status = first field whose auto-spectrum has a
+// negative value ("negative values in cl", glass/fields.py:229-231).
+__global__ void k_cltovar(const double *__restrict__ flat, const int64_t *__restrict__ offs,
+                          double *__restrict__ var, unsigned long long *__restrict__ status) {
+    __shared__ double part[256];
+    const int j = blockIdx.x;
+    const int64_t q = (int64_t)j * (j + 1) / 2;
+    const int64_t o = offs[q], len = offs[q + 1] - o;
+    double s = 0.0;
+    bool neg = false;
+    for (int64_t l = threadIdx.x; l < len; l += blockDim.x) {
+        const double c = flat[o + l];
+        neg |= c < 0;
+        s += (2.0 * l + 1.0) * c;
+    }
+    if (neg) atomicMin(status, (unsigned long long)j);
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) part[threadIdx.x] += part[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) var[j] = part[0] / (4.0 * 3.14159265358979323846);
+}
+
 // ------------------------------------------------------------------ philox
 
 struct U4 {
@@ -293,6 +341,27 @@ extern "C" int glg_iternorm(const double *cov, int64_t nrows, int64_t nl, int k,
     GLG_LAUNCH_SCOPE("k_iternorm", st);
     k_iternorm<<<(unsigned)nl, 32, smem, st>>>(cov, nrows, nl, k, w, (int64_t *)status);
     GLG_CHECK_LAUNCH("k_iternorm");
+    return GLG_OK;
+}
+
+extern "C" int glg_cls2cov(const double *flat, const int64_t *offs, int nf, int nl, int nc,
+                           double *cov, double *var, uint64_t *status, void *stream) {
+    GLG_REQUIRE(flat && offs && cov && var && status, "glg_cls2cov: null pointer");
+    GLG_REQUIRE(nf >= 0 && nl >= 0 && nc >= 0, "glg_cls2cov: negative size");
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e = cudaMemsetAsync(status, 0xff, sizeof(uint64_t), st);
+    if (e != cudaSuccess) return glg_cuda_status(e, "glg_cls2cov: status reset");
+    if (nf == 0) return GLG_OK;
+    if (nl > 0) {
+        GLG_LAUNCH_SCOPE("k_cls2cov", st);
+        k_cls2cov<<<dim3((nl + 255) / 256, nf), 256, 0, st>>>(flat, offs, nf, nl, nc, cov);
+        GLG_CHECK_LAUNCH("k_cls2cov");
+    }
+    {
+        GLG_LAUNCH_SCOPE("k_cltovar", st);
+        k_cltovar<<<nf, 256, 0, st>>>(flat, offs, var, (unsigned long long *)status);
+        GLG_CHECK_LAUNCH("k_cltovar");
+    }
     return GLG_OK;
 }
 

@@ -37,7 +37,10 @@ namespace {
 
 constexpr int NST = 6;            // pipeline stages (A in TMEM, B/seeds/coefs in smem)
 constexpr int NSETS = 3;          // producer warp sets
-constexpr int CHUNK = 4;          // groups accumulated per TMEM accumulator fill
+#ifndef GLG_TC_CHUNK
+#define GLG_TC_CHUNK 4
+#endif
+constexpr int CHUNK = GLG_TC_CHUNK;  // groups accumulated per TMEM accumulator fill
 constexpr int TMEM_COLS = 512;
 constexpr int THREADS = 18 * 32;
 constexpr uint32_t WAIT_LIMIT = 1u << 22;

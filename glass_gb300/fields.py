@@ -246,14 +246,37 @@ class _FieldBatcher:
         self.cdtype = torch.complex128 if form == "plain" else torch.complex64
         self.code = _lib.GLG_F64 if form == "plain" else _lib.GLG_F32
         self.z_size = n * (n + 1) // 2
-        gls_dev = [_lib.to_device(g, torch.float64, self.device) if g is not None else None for g in gls]
-        covs = [c.clone() for c in cls2cov(gls_dev, n, self.ngrf, self.ncorr)]
         k = self.ncorr
-        stack = torch.stack(covs) if covs else torch.zeros((0, n, k + 1), dtype=torch.float64,
-                                                              device=self.device)
         self.k = k
-        self.w, status = _iternorm_device(stack.contiguous())
-        self.bad = _first_bad(status)
+        # cls2cov + variances of every field in one launch from the
+        # concatenated spectra, then iternorm of every field in one launch
+        lens = [0 if g is None else int(g.shape[0]) for g in gls]
+        offs = np.concatenate([[0], np.cumsum(lens)]).astype(np.int64)
+        if self.numpy_out:
+            flat_h = np.concatenate([np.asarray(g, dtype=np.float64).reshape(-1) for g in gls if g is not None])
+            flat = torch.from_numpy(flat_h).to(self.device)
+        else:
+            flat = torch.cat([_lib.to_device(g, torch.float64, self.device).reshape(-1)
+                              for g in gls if g is not None])
+        offs_d = torch.from_numpy(offs).to(self.device)
+        cov = torch.empty((self.ngrf, n, k + 1), dtype=torch.float64, device=self.device)
+        self.var_dev = torch.empty(self.ngrf, dtype=torch.float64, device=self.device)
+        status = torch.empty(2, dtype=torch.int64, device=self.device)
+        check(lib().glg_cls2cov(c_p(ptr(flat)), c_p(ptr(offs_d)), self.ngrf, n, k, c_p(ptr(cov)),
+                                c_p(ptr(self.var_dev)), c_p(ptr(status)), c_p(stream_ptr(self.device))),
+              "glg_cls2cov")
+        self.w, st_it = _iternorm_device(cov)
+        status[1:2].copy_(st_it)
+        host = torch.cat([status.double(), self.var_dev]).cpu().numpy()  # one sync
+        neg, nonpd = int(host[0]), int(host[1])
+        self.variances = [float(v) for v in host[2:]]
+        # the reference raises at the first failing field, after the earlier maps
+        self.bad_msg = None
+        self.bad = -1
+        if neg >= 0:
+            self.bad, self.bad_msg = neg, "negative values in cl"
+        if nonpd >= 0 and (self.bad < 0 or nonpd < self.bad):
+            self.bad, self.bad_msg = nonpd, "covariance matrix is not positive definite"
         # variate source
         if rng is None:
             rng = grng.default_rng()
@@ -318,10 +341,25 @@ def _generate_grf(gls, nside: int, *, ncorr=None, rng=None, form: str | None = N
         if b.bad >= 0 and b.bad < t0 + cnt:
             cnt = b.bad - t0
         maps = b.maps(t0, cnt) if cnt > 0 else None
+        if b.numpy_out and cnt > 0:
+            maps = _to_host(maps)
         for s in range(cnt):
-            yield maps[s].cpu().numpy() if b.numpy_out else maps[s]
+            yield maps[s]
         if b.bad >= 0 and b.bad < t0 + g:
-            raise ValueError("covariance matrix is not positive definite")
+            raise ValueError(b.bad_msg)
+
+
+def _to_host(maps: torch.Tensor) -> list[np.ndarray]:
+    """Device maps -> numpy arrays backed by page-locked host memory.
+
+    One asynchronous copy per map into pinned buffers (recycled by torch's
+    caching host allocator) and a single synchronisation.
+    """
+    out = [torch.empty(m.shape, dtype=m.dtype, pin_memory=True) for m in maps]
+    for h, m in zip(out, maps):
+        h.copy_(m, non_blocking=True)
+    torch.cuda.current_stream(maps.device).synchronize()
+    return [h.numpy() for h in out]
 
 
 def _cltovar(cl) -> float:
@@ -346,7 +384,7 @@ def generate(fields: Sequence, gls, nside: int, *, ncorr: int | None = None, rng
 
 def _generate(fields, gls, nside, ncorr, rng, form):
     b = _FieldBatcher(gls, nside, ncorr, rng, form)
-    variances = [_cltovar(getcl(gls, i, i)) for i in range(b.ngrf)]
+    variances = b.variances
     kinds = [grf.fused_kind(t) for t in fields]
     g = _group_size(b.ngrf, nside, b.lmax, form, b.np_rng is not None)
     for t0 in range(0, b.ngrf, g):
@@ -359,16 +397,16 @@ def _generate(fields, gls, nside, ncorr, rng, form):
             epi = (epi_kind, [variances[t] for t in range(t0, t0 + cnt)],
                    [kinds[t][1] if fused[s] else 1.0 for s, t in enumerate(range(t0, t0 + cnt))])
             maps = b.maps(t0, cnt, epi=epi)
+            if b.numpy_out:
+                maps = _to_host(maps)
         for s in range(cnt):
             t = t0 + s
             x = maps[s]
-            if b.numpy_out:
-                x = x.cpu().numpy()
             if kinds[t] is None:
                 x = fields[t](x, variances[t])
             yield x
         if b.bad >= 0 and b.bad < t0 + g:
-            raise ValueError("covariance matrix is not positive definite")
+            raise ValueError(b.bad_msg)
 
 
 @_deprecated("use glass.generate() instead")

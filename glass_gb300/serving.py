@@ -27,7 +27,7 @@ import torch
 
 from . import _lib, grf
 from . import healpix as hp
-from .fields import _FieldBatcher, _cltovar, getcl
+from .fields import _FieldBatcher
 from .rng import Generator
 
 __all__ = ["Request", "Server"]
@@ -86,9 +86,11 @@ class _Active:
         fields = [grf.Lognormal(float(s)) for s in req.shifts]
         self.kinds = [_lib.EPI_LOGNORMAL] * req.nshell
         self.lam = [f.lamda for f in fields]
-        self.var = [_cltovar(getcl(req.gls, i, i)) for i in range(req.nshell)]
         self.batcher = _FieldBatcher(req.gls, req.nside, req.ncorr, Generator(req.seed), "fast",
                                      device=device)
+        if self.batcher.bad >= 0:
+            raise ValueError(f"request {req.id}: {self.batcher.bad_msg}")
+        self.var = self.batcher.variances
         self.alm = self.batcher.alm(0, req.nshell)  # [nshell][nalm] complex64, device
         self.next_shell = 0
         self.maps: list[torch.Tensor | None] = [None] * req.nshell

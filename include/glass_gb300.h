@@ -80,6 +80,18 @@ int glg_iternorm(const double *cov, int64_t nrows, int64_t nl, int k, double *w,
                  uint64_t *status, void *stream);
 
 /*
+ * Covariance rows of every field at once, glass/fields.py:191-236 (cls2cov),
+ * and the variances of glass/fields.py:890 (transformcl.cltovar of each
+ * auto-spectrum).  flat: the nf(nf+1)/2 spectra in GLASS order, float64,
+ * concatenated; offs: int64 [nspec+1] offsets into flat.  cov: float64
+ * [nf][nl][nc+1] (= C^{j,j-i}_l / 2, zero-padded); var: float64 [nf].
+ * status: one uint64 of device memory, UINT64_MAX, or the first field whose
+ * auto-spectrum has a negative value ("negative values in cl").
+ */
+int glg_cls2cov(const double *flat, const int64_t *offs, int nf, int nl, int nc, double *cov,
+                double *var, uint64_t *status, void *stream);
+
+/*
  * Standard complex normals of the counter-based stream that replaces the
  * reference's numpy draw standard_normal((z_size, 2)) @ [1, 1j]
  * (glass/fields.py:407; generator seam glass/rng.py:21-55).  Element e of

@@ -98,3 +98,15 @@ def test_no_cpu_fallback_without_gpu():
 
     with pytest.raises(RuntimeError, match="no CPU fallback"):
         _lib.lib()
+
+
+def test_serving_memory_model():
+    from glass_gb300 import serving
+
+    a = serving.request_bytes(128, 256, 3)
+    b = serving.request_bytes(128, 256, 6)
+    assert 0 < a < b
+    assert serving.request_bytes(1024, 2048, 20) > 20 * 12 * 1024 * 1024 * 4
+    r = serving.Request(gls=[np.ones(9)], nside=4, shifts=[1.0], arrival=1.0)
+    r.finished = 3.5
+    assert r.latency == 2.5 and r.nshell == 1 and r.lmax == 8
