@@ -11,7 +11,7 @@ computed by hand-written CUDA kernels for sm_103a behind the C ABI of
 
 from __future__ import annotations
 
-from . import grf, harmonics, healpix, rng
+from . import grf, harmonics, healpix, points, rng
 from .fields import (
     cls2cov,
     enumerate_spectra,
@@ -37,6 +37,7 @@ __all__ = [
     "grf",
     "harmonics",
     "healpix",
+    "points",
     "iternorm",
     "multalm",
     "nfields_from_nspectra",

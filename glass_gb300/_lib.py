@@ -61,6 +61,8 @@ _SIGNATURES = {
     "glg_alm_correlate": ([c_p, c_i, c_i, c_i, c_i64, c_p, c_i64, c_u64, c_u64, c_i, c_p, c_p], c_i),
     "glg_multalm": ([c_p, c_p, c_i, c_i, c_p, c_p], c_i),
     "glg_almxfl": ([c_p, c_p, c_i, c_i, c_i, c_i, c_p, c_p], c_i),
+    "glg_poisson_counts": ([c_p, c_i, c_i64, ctypes.c_double, ctypes.c_double, ctypes.c_double, c_p,
+                            c_u64, c_u64, c_p, c_p], c_i),
     "glg_alm2map_workspace": ([c_p, c_i, c_i], c_sz),
     "glg_alm2map": ([c_p, c_p, c_i, c_i, c_p, ctypes.POINTER(Epilogue), c_p, c_sz, c_p], c_i),
     "glg_workspace_status": ([c_p, c_p], c_i),

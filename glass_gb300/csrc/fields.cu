@@ -6,6 +6,10 @@
 #include <vector>
 
 #include "glg_internal.cuh"
+#include "philox.cuh"
+
+using glg_rng::U4;
+using glg_rng::philox4x32_10;
 
 namespace {
 
@@ -131,27 +135,6 @@ __global__ void k_cltovar(const double *__restrict__ flat, const int64_t *__rest
 
 // ------------------------------------------------------------------ philox
 
-struct U4 {
-    uint32_t x, y, z, w;
-};
-
-__device__ __forceinline__ U4 philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
-                                            uint32_t k0, uint32_t k1) {
-#pragma unroll
-    for (int r = 0; r < 10; ++r) {
-        const uint32_t lo0 = 0xD2511F53u * c0, hi0 = __umulhi(0xD2511F53u, c0);
-        const uint32_t lo1 = 0xCD9E8D57u * c2, hi1 = __umulhi(0xCD9E8D57u, c2);
-        const uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
-        c0 = n0;
-        c1 = lo1;
-        c2 = n2;
-        c3 = lo0;
-        k0 += 0x9E3779B9u;
-        k1 += 0xBB67AE85u;
-    }
-    return {c0, c1, c2, c3};
-}
-
 // Complex standard normal: element e of stream sid (see orc_philox_normals).
 __device__ __forceinline__ double2 philox_cnormal_f64(uint64_t seed, uint64_t sid, uint64_t e) {
     const U4 x = philox4x32_10((uint32_t)e, (uint32_t)(e >> 32), (uint32_t)sid,
@@ -225,10 +208,13 @@ __global__ void k_alm_correlate(const double *__restrict__ w, const int nshell, 
                                 T2 *__restrict__ alm, const int window) {
     extern __shared__ __align__(16) unsigned char sm_raw[];
     const int kp = k + 1;
-    T *ws = reinterpret_cast<T *>(sm_raw);  // [CT_L][kp]
-    const size_t ws_bytes = ((sizeof(T) * CT_L * kp) + 15) & ~(size_t)15;
-    T2 *zs = reinterpret_cast<T2 *>(sm_raw + ws_bytes) + (size_t)threadIdx.x * window;
-    const int ctm = blockDim.x / CT_L;
+    const int wst = kp | 1;  // odd row stride: the 16 l rows sit in distinct banks
+    T *ws = reinterpret_cast<T *>(sm_raw);  // [CT_L][wst]
+    const size_t ws_bytes = ((sizeof(T) * CT_L * wst) + 15) & ~(size_t)15;
+    // variate window, slot-major ([slot][thread]) so a warp's accesses are contiguous
+    T2 *zs = reinterpret_cast<T2 *>(sm_raw + ws_bytes) + threadIdx.x;
+    const int B = blockDim.x;
+    const int ctm = B / CT_L;
     const int l0 = blockIdx.x * CT_L, m0 = blockIdx.y * ctm;
     if (m0 > l0 + CT_L - 1 || m0 > lmax) return;  // tile entirely above m = l
     const int l = l0 + (int)(threadIdx.x % CT_L), m = m0 + (int)(threadIdx.x / CT_L);
@@ -246,35 +232,48 @@ __global__ void k_alm_correlate(const double *__restrict__ w, const int nshell, 
             return philox_cnormal_f32(seed, sid_base + (uint64_t)t, (uint64_t)g);
         }
     };
-    if (valid)
-        for (int64_t t = zlo; t < t0; ++t) zs[t % window] = fetch(t);
+    // shell t lives in slot t mod window; head = slot of the current shell
+    int head = (int)(t0 % window);
+    if (valid) {
+        int slot = (int)(zlo % window);
+        for (int64_t t = zlo; t < t0; ++t) {
+            zs[slot * B] = fetch(t);
+            if (++slot == window) slot = 0;
+        }
+    }
     for (int s = 0; s < nshell; ++s) {
         const int64_t t = t0 + s;
         __syncthreads();
-        for (int q = threadIdx.x; q < CT_L * kp; q += blockDim.x) {
-            const int lg = l0 + q / kp;
-            ws[q] = lg <= lmax ? (T)w[((size_t)s * L + lg) * kp + (q % kp)] : (T)0;
+        for (int q = threadIdx.x; q < CT_L * kp; q += B) {
+            const int r = q / kp, c = q - r * kp;
+            const int lg = l0 + r;
+            ws[r * wst + c] = lg <= lmax ? (T)w[((size_t)s * L + lg) * kp + c] : (T)0;
         }
         __syncthreads();
-        if (!valid) continue;
-        zs[t % window] = fetch(t);
-        const T *wt = ws + (l - l0) * kp;
-        T re = 0, im = 0;
-        const int dmax = t < k ? (int)t : k;
-        for (int d = dmax; d >= 0; --d) {
-            const T2 zz = zs[(t - d) % window];
-            const T c = wt[k - d];
-            re += c * zz.x;
-            im += c * zz.y;
+        if (valid) {
+            zs[head * B] = fetch(t);
+            const T *wt = ws + (l - l0) * wst;
+            T re = 0, im = 0;
+            const int dmax = t < k ? (int)t : k;
+            int j = head - dmax;
+            if (j < 0) j += window;
+            for (int d = dmax; d >= 0; --d) {
+                const T2 zz = zs[j * B];
+                const T c = wt[k - d];
+                re += c * zz.x;
+                im += c * zz.y;
+                if (++j == window) j = 0;
+            }
+            if (m == 0) {
+                re = re + im;
+                im = 0;
+            }
+            T2 o;
+            o.x = re;
+            o.y = im;
+            alm[(int64_t)s * nalm + ix] = o;
         }
-        if (m == 0) {
-            re = re + im;
-            im = 0;
-        }
-        T2 o;
-        o.x = re;
-        o.y = im;
-        alm[(int64_t)s * nalm + ix] = o;
+        if (++head == window) head = 0;
     }
 }
 
@@ -391,7 +390,7 @@ extern "C" int glg_alm_correlate(const double *w, int nshell, int lmax, int k, i
     const size_t rsz = dtype == GLG_F64 ? sizeof(double) : sizeof(float);
     int threads = 128;  // 16 l x 8 m; fewer m per tile when the variate window is long
     auto smem_for = [&](int th) {
-        return (((rsz * CT_L * (size_t)window) + 15) & ~(size_t)15) + esz * (size_t)window * th;
+        return (((rsz * CT_L * (size_t)(window | 1)) + 15) & ~(size_t)15) + esz * (size_t)window * th;
     };
     while (threads > CT_L && smem_for(threads) > 200 * 1024) threads /= 2;
     const size_t smem = smem_for(threads);

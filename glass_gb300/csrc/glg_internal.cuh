@@ -47,6 +47,15 @@ struct glg_launch_scope {
 // Maximum number of radix passes of one ring FFT (n = 4 i <= 4 * 8192).
 #define GLG_MAX_FFT_STAGES 20
 
+// One launch of the FP32 ring FFTs: `count` ring pairs of one kind
+// (0: mixed radix, 1: Bluestein) starting at bucket_pairs[first].
+#define GLG_MAX_RING_BUCKETS 24
+struct glg_ring_bucket {
+    int kind, count, threads;
+    int64_t first;
+    size_t smem;
+};
+
 struct glg_plan {
     int nside, lmax, mmax;
     int nrings, npairs;
@@ -88,16 +97,45 @@ struct glg_plan {
     // factors are all <= 13 (mixed-radix DIF, output order from pos16).
     // Class 1: lengths with a larger prime factor (Bluestein with a
     // power-of-two length M >= 2n - 1 and a precomputed chirp spectrum).
-    int ncls0, ncls1;
-    int *cls0_pairs, *cls1_pairs;  // ring pairs of each class
+    // Ring pairs are launched in size buckets (one launch per bucket, every
+    // map of the call in the same grid), each with its own shared memory.
+    int nbuckets;
+    glg_ring_bucket buckets[GLG_MAX_RING_BUCKETS];
+    int *bucket_pairs;       // ring pairs of all buckets, bucket after bucket
     int64_t *pos_ofs;        // [nside+1] offset of the output permutation of n = 4 i
     uint16_t *pos16;         // DIF output position of every frequency, per length
     int64_t *blu_ofs;        // [nside+1] offset of the chirp spectrum of n = 4 i (-1: class 0)
     int *blu_M;              // [nside+1] Bluestein length M of n = 4 i (0: class 0)
     float2 *blu_H;           // chirp spectra, each in DIF output order of its M
+    int64_t *chirp_ofs;      // [nside+1] offset of the chirp of n = 4 i (-1: class 0)
+    float2 *chirp;           // exp(i pi k^2 / n), k < n, per Bluestein length
     int blu_Mmax;
     float2 *twM;             // [blu_Mmax / 2 + 1] exp(2 pi i t / blu_Mmax)
 };
+
+// Radix passes of an FP32 ring FFT of length n (DIF order: 16s, then one 8,
+// 4 or 2, then the odd primes up to 13).  Returns the pass count, or -1 when
+// n has a prime factor above 13 (those lengths go through Bluestein).
+__host__ __device__ inline int glg_fft32_radices(int n, int *r) {
+    int k = 0;
+    while (n % 16 == 0) { r[k++] = 16; n /= 16; }
+    if (n % 8 == 0) { r[k++] = 8; n /= 8; }
+    else if (n % 4 == 0) { r[k++] = 4; n /= 4; }
+    else if (n % 2 == 0) { r[k++] = 2; n /= 2; }
+    for (int p = 3; p <= 13; p += 2)
+        while (n % p == 0) { r[k++] = p; n /= p; }
+    return n == 1 ? k : -1;
+}
+
+// Shared-memory index of complex element e of a ring FFT buffer: one spare
+// slot per 16 values keeps every power-of-two stride free of bank conflicts.
+__host__ __device__ inline int glg_zi(int e) { return e + (e >> 4); }
+
+// Dynamic shared memory of one ring FFT block: the padded transform buffer
+// of length n (kind 0) or M (kind 1), a second padded buffer for the south
+// ring's fold (kind 0 with n <= mmax), 2 x threads partial sums and the half
+// twiddle table.
+size_t glg_ring32_smem(int kind, int n_or_M, int threads, bool fold);
 
 // l values per group of the fast Legendre contraction (8 even + 8 odd)
 #define GLG_GROUP 16

@@ -21,9 +21,10 @@
 // TMEM accumulator sets, and drain warps add every finished chunk into FP32
 // sums in shared memory (round to nearest).
 //
-// Warp roles (576 threads): warps 0-11 produce lambda (three sets taking
+// Warp roles (608 threads): warps 0-11 produce lambda (three sets taking
 // every third group), warps 12-15 drain the accumulators and store F, warp 16
-// issues the MMAs, warp 17 streams B / seeds / coefficients.  Every wait is
+// issues the MMAs, warp 17 streams B through NB stages and warp 18 streams
+// seeds / coefficients through a deeper ring of NSEED slots.  Every wait is
 // bounded; on time-out the kernel records GLG_ERR_TIMEOUT in *err, retires
 // its outstanding MMAs and copies, frees its tensor memory and returns.
 #include <cuda_runtime.h>
@@ -35,16 +36,18 @@ using namespace glg_tc;
 
 namespace {
 
-constexpr int NST = 6;            // pipeline stages (A in TMEM, B/seeds/coefs in smem)
+constexpr int NST = 6;            // lambda stages in tensor memory (A operands)
 constexpr int NSETS = 3;          // producer warp sets
 #ifndef GLG_TC_CHUNK
 #define GLG_TC_CHUNK 4
 #endif
 constexpr int CHUNK = GLG_TC_CHUNK;  // groups accumulated per TMEM accumulator fill
+constexpr int NSEED = 16;         // slots of the seed / coefficient ring
 constexpr int TMEM_COLS = 512;
-constexpr int THREADS = 18 * 32;
+constexpr int THREADS = 19 * 32;
 constexpr uint32_t WAIT_LIMIT = 1u << 22;
-constexpr int W_DRAIN = 12, W_MMA = 16, W_LOAD = 17;
+constexpr int W_DRAIN = 12, W_MMA = 16, W_LOAD = 17, W_SEED = 18;
+static_assert((W_SEED + 1) * 32 == THREADS, "one warp per role after the producers and drains");
 
 struct LegTcArgs {
     int npairs, nrings, lmax, nmaps, ntiles;
@@ -90,16 +93,30 @@ __device__ __forceinline__ int unit_m(int64_t mi, int lmax) {
     return (mi & 1) ? lmax - (int)(mi >> 1) : (int)(mi >> 1);
 }
 
+// B stages in shared memory: as many as fit beside the accumulators and the
+// seed ring (up to 16), so that the alm of a group are requested well before
+// the MMA that reads them.
+template <int N>
+constexpr int nb_stages() {
+    constexpr int room = (220 * 1024 - 1024 * N - NSEED * 1280 - 1024) / (128 * N);
+    return room > 16 ? 16 : room;
+}
+
 template <int N>
 struct Smem {
     static constexpr uint32_t BBYTES = 128 * N;  // 4 tiles of N x 8 tf32
+    static constexpr int NB = nb_stages<N>();
+    static_assert(NB >= NST, "B ring shallower than the lambda stages");
     struct Stage {
         unsigned char b[BBYTES];
-        float2 seed[128];      // seeds of the group's 128 ring pairs
+    } st[NB];
+    struct SeedSlot {
+        float2 seed[128];        // seeds of the group's 128 ring pairs
         float4 coef[GLG_GROUP];  // (A_hi, A_lo, B_hi, B_lo) of l = l0 .. l0+15
-    } st[NST];
+    } sd[NSEED];
     float acc[2 * N][128];     // FP32 sums of drained chunks, [column][lane]
-    uint64_t full_a[NST], full_b[NST], empty[NST];
+    uint64_t full_a[NST], empty[NST], full_b[NB], bempty[NB];
+    uint64_t sfull[NSEED], sempty[NSEED];
     uint64_t full_d[2], empty_d[2], drain;
     uint32_t tmem_base;
     int abort;
@@ -111,15 +128,22 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
     Smem<N> &S = *reinterpret_cast<Smem<N> *>(smem_raw);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     constexpr uint32_t IDESC = idesc_tf32(128, N);
-    constexpr uint32_t STAGE_TX = Smem<N>::BBYTES + 128 * 8 + GLG_GROUP * 16;
+    constexpr uint32_t SEED_TX = 128 * 8 + GLG_GROUP * 16;
     constexpr int A_COL0 = 4 * N;  // D sets at [0, 2N) and [2N, 4N)
     static_assert(A_COL0 + 32 * NST <= TMEM_COLS, "tensor memory budget");
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < NST; ++s) {
             mbar_init(&S.full_a[s], 4);
-            mbar_init(&S.full_b[s], 1);
             mbar_init(&S.empty[s], 1);
+        }
+        for (int s = 0; s < Smem<N>::NB; ++s) {
+            mbar_init(&S.full_b[s], 1);
+            mbar_init(&S.bempty[s], 1);
+        }
+        for (int q = 0; q < NSEED; ++q) {
+            mbar_init(&S.sfull[q], 1);
+            mbar_init(&S.sempty[q], 4);
         }
         for (int d = 0; d < 2; ++d) {
             mbar_init(&S.full_d[d], 1);
@@ -173,40 +197,63 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
                 const int64_t gg = gc + g;
                 const int s = (int)(gg % NST);
                 const uint32_t par = (uint32_t)((gg / NST) & 1);
+                const int q = (int)(gg % NSEED);
+                if (!wait(&S.sfull[q], (uint32_t)((gg / NSEED) & 1))) { ok = false; break; }
                 if (gg >= NST && !wait(&S.empty[s], par ^ 1u)) { ok = false; break; }
-                if (!wait(&S.full_b[s], par)) { ok = false; break; }
                 fence_after_sync();
-                const typename Smem<N>::Stage &sg = S.st[s];
+                const typename Smem<N>::SeedSlot &sd = S.sd[q];
                 const int l0 = m + g * GLG_GROUP;
                 const int s0 = l0 > ls ? l0 : ls;
-                const float2 seed = sg.seed[r];
+                const float2 seed = sd.seed[r];
                 float lm2 = 0.f, lm1 = 0.f;
                 uint32_t ehi[8], elo[8], ohi[8], olo[8];
+                // every lane starts at l0 and the group ends inside lmax: no per-step tests
+                const bool regular = __all_sync(0xffffffffu, s0 == l0) && l0 + GLG_GROUP - 1 <= lmax;
+                if (regular) {
 #pragma unroll
-                for (int j = 0; j < GLG_GROUP; ++j) {
-                    const int l = l0 + j;
-                    float v;
-                    if (l < s0 || l > lmax) {
-                        v = 0.f;
-                    } else if (l == s0) {
-                        v = seed.x;
-                    } else if (l == s0 + 1) {
-                        v = seed.y;
-                    } else {
-                        v = rec_step_comp(sg.coef[j], x, lm1, lm2);
+                    for (int j = 0; j < GLG_GROUP; ++j) {
+                        const float v = j == 0 ? seed.x : j == 1 ? seed.y : rec_step_comp(sd.coef[j], x, lm1, lm2);
+                        lm2 = lm1;
+                        lm1 = v;
+                        const uint32_t hi = tf32_rna(v);
+                        const uint32_t lo = tf32_rna(v - __uint_as_float(hi));
+                        if (j & 1) {
+                            ohi[j >> 1] = hi;
+                            olo[j >> 1] = lo;
+                        } else {
+                            ehi[j >> 1] = hi;
+                            elo[j >> 1] = lo;
+                        }
                     }
-                    lm2 = lm1;
-                    lm1 = v;
-                    const uint32_t hi = tf32_rna(v);
-                    const uint32_t lo = tf32_rna(v - __uint_as_float(hi));
-                    if (j & 1) {
-                        ohi[j >> 1] = hi;
-                        olo[j >> 1] = lo;
-                    } else {
-                        ehi[j >> 1] = hi;
-                        elo[j >> 1] = lo;
+                } else {
+#pragma unroll
+                    for (int j = 0; j < GLG_GROUP; ++j) {
+                        const int l = l0 + j;
+                        float v;
+                        if (l < s0 || l > lmax) {
+                            v = 0.f;
+                        } else if (l == s0) {
+                            v = seed.x;
+                        } else if (l == s0 + 1) {
+                            v = seed.y;
+                        } else {
+                            v = rec_step_comp(sd.coef[j], x, lm1, lm2);
+                        }
+                        lm2 = lm1;
+                        lm1 = v;
+                        const uint32_t hi = tf32_rna(v);
+                        const uint32_t lo = tf32_rna(v - __uint_as_float(hi));
+                        if (j & 1) {
+                            ohi[j >> 1] = hi;
+                            olo[j >> 1] = lo;
+                        } else {
+                            ehi[j >> 1] = hi;
+                            elo[j >> 1] = lo;
+                        }
                     }
                 }
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&S.sempty[q]);  // slot read: the seed loader may refill it
                 const uint32_t col = tb + lane_base + A_COL0 + 32 * s;
                 tmem_st8(col + 0, ehi);
                 tmem_st8(col + 8, elo);
@@ -277,11 +324,15 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
                     for (int q = g; q < gend; ++q) {
                         const int64_t gg = gc + q;
                         const int s = (int)(gg % NST);
-                        const uint32_t par = (uint32_t)((gg / NST) & 1);
-                        if (!wait(&S.full_a[s], par) || !wait(&S.full_b[s], par)) { ok = false; break; }
+                        const int sb = (int)(gg % Smem<N>::NB);
+                        if (!wait(&S.full_b[sb], (uint32_t)((gg / Smem<N>::NB) & 1)) ||
+                            !wait(&S.full_a[s], (uint32_t)((gg / NST) & 1))) {
+                            ok = false;
+                            break;
+                        }
                         fence_after_sync();
                         const uint32_t acol = tb + A_COL0 + 32 * s;
-                        const uint32_t bb = smem_u32(S.st[s].b);
+                        const uint32_t bb = smem_u32(S.st[sb].b);
                         constexpr uint32_t tsz = 32 * N;  // bytes of one B tile
                         const uint64_t bEh = sdesc_noswz(bb, 128, 256), bEl = sdesc_noswz(bb + tsz, 128, 256);
                         const uint64_t bOh = sdesc_noswz(bb + 2 * tsz, 128, 256);
@@ -294,6 +345,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
                         mma_tf32_ts(dO, acol + 16, bOl, IDESC, 1u);
                         mma_tf32_ts(dO, acol + 24, bOh, IDESC, 1u);
                         mma_commit(&S.empty[s]);
+                        mma_commit(&S.bempty[sb]);
                         issued = true;
                     }
                     if (ok) mma_commit(&S.full_d[d]);
@@ -308,13 +360,46 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
             }
         }
         __syncwarp();
-    } else {
-        // ------------------------------------- B / seeds / coefficient streaming
+    } else if (warp == W_LOAD) {
+        // ------------------------------------------------------- B streaming
         if (lane == 0) {
             int64_t gc = 0;
             bool ok = true;
-            int64_t last_use[NST];
-            for (int s = 0; s < NST; ++s) last_use[s] = -1;
+            constexpr int NB = Smem<N>::NB;
+            int64_t last_use[NB];
+            for (int s = 0; s < NB; ++s) last_use[s] = -1;
+            for (int64_t u = blockIdx.x; u < a.nunits && ok; u += gridDim.x) {
+                const int m = unit_m(u / a.ntiles, lmax);
+                const int G = (lmax - m + GLG_GROUP) / GLG_GROUP;
+                const int64_t gb = a.goff[m];
+                for (int g = 0; g < G; ++g) {
+                    const int64_t gg = gc + g;
+                    const int s = (int)(gg % NB);
+                    const int64_t use = gg / NB;
+                    if (use > 0 && !wait(&S.bempty[s], (uint32_t)((use - 1) & 1))) { ok = false; break; }
+                    mbar_arrive_expect_tx(&S.full_b[s], Smem<N>::BBYTES);
+                    bulk_g2s(S.st[s].b, a.bpack + (size_t)(gb + g) * Smem<N>::BBYTES, Smem<N>::BBYTES, &S.full_b[s]);
+                    last_use[s] = use;
+                }
+                gc += G;
+            }
+            if (!ok) fail();
+            // outstanding copies land before the CTA exits
+            for (int s = 0; s < NB; ++s)
+                if (last_use[s] >= 0)
+                    for (uint32_t i = 0; i < WAIT_LIMIT && !mbar_try_wait(&S.full_b[s], (uint32_t)(last_use[s] & 1)); ++i) {
+                    }
+        }
+        __syncwarp();
+    } else {
+        // ----------------------------------- seed / coefficient streaming
+        // A deeper ring than the B stages, so that a producer set finds the
+        // seeds of its next group already resident when it finishes one.
+        if (lane == 0) {
+            int64_t gc = 0;
+            bool ok = true;
+            int64_t last_use[NSEED];
+            for (int q = 0; q < NSEED; ++q) last_use[q] = -1;
             for (int64_t u = blockIdx.x; u < a.nunits && ok; u += gridDim.x) {
                 const int tile = (int)(u % a.ntiles);
                 const int m = unit_m(u / a.ntiles, lmax);
@@ -323,23 +408,21 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
                 const int64_t cb = a.mofs[m];
                 for (int g = 0; g < G; ++g) {
                     const int64_t gg = gc + g;
-                    const int s = (int)(gg % NST);
-                    const int64_t use = gg / NST;
-                    if (use > 0 && !wait(&S.empty[s], (uint32_t)((use - 1) & 1))) { ok = false; break; }
-                    typename Smem<N>::Stage &sg = S.st[s];
-                    mbar_arrive_expect_tx(&S.full_b[s], STAGE_TX);
-                    bulk_g2s(sg.b, a.bpack + (size_t)(gb + g) * Smem<N>::BBYTES, Smem<N>::BBYTES, &S.full_b[s]);
-                    bulk_g2s(sg.seed, a.seeds + (gb + g) * a.seed_stride + (int64_t)tile * 128, 128 * 8, &S.full_b[s]);
-                    bulk_g2s(sg.coef, a.coef32 + cb + (int64_t)g * GLG_GROUP, GLG_GROUP * 16, &S.full_b[s]);
-                    last_use[s] = use;
+                    const int q = (int)(gg % NSEED);
+                    const int64_t use = gg / NSEED;
+                    if (use > 0 && !wait(&S.sempty[q], (uint32_t)((use - 1) & 1))) { ok = false; break; }
+                    typename Smem<N>::SeedSlot &sd = S.sd[q];
+                    mbar_arrive_expect_tx(&S.sfull[q], SEED_TX);
+                    bulk_g2s(sd.seed, a.seeds + (gb + g) * a.seed_stride + (int64_t)tile * 128, 128 * 8, &S.sfull[q]);
+                    bulk_g2s(sd.coef, a.coef32 + cb + (int64_t)g * GLG_GROUP, GLG_GROUP * 16, &S.sfull[q]);
+                    last_use[q] = use;
                 }
                 gc += G;
             }
             if (!ok) fail();
-            // outstanding copies land before the CTA exits
-            for (int s = 0; s < NST; ++s)
-                if (last_use[s] >= 0)
-                    for (uint32_t i = 0; i < WAIT_LIMIT && !mbar_try_wait(&S.full_b[s], (uint32_t)(last_use[s] & 1)); ++i) {
+            for (int q = 0; q < NSEED; ++q)
+                if (last_use[q] >= 0)
+                    for (uint32_t i = 0; i < WAIT_LIMIT && !mbar_try_wait(&S.sfull[q], (uint32_t)(last_use[q] & 1)); ++i) {
                     }
         }
         __syncwarp();

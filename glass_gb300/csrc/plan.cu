@@ -8,6 +8,7 @@
 #include <math.h>
 
 #include <complex>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -202,8 +203,8 @@ extern "C" void glg_plan_destroy(glg_plan *P) {
     void *ptrs[] = {P->cth,   P->sth,       P->nph,     P->half,   P->startN, P->startS,
                     P->mofs,  P->coef,      P->lmm,     P->lmm_scale, P->fft_radix,
                     P->fft_nst, P->tw_ofs,  P->tw,      P->cth32,  P->tw32,   P->coef32,
-                    P->goff,  P->seeds,     P->lstart,  P->cls0_pairs, P->cls1_pairs,
-                    P->pos_ofs, P->pos16,   P->blu_ofs, P->blu_M,  P->blu_H,  P->twM};
+                    P->goff,  P->seeds,     P->lstart,  P->bucket_pairs, P->chirp_ofs,
+                    P->chirp, P->pos_ofs, P->pos16,   P->blu_ofs, P->blu_M,  P->blu_H,  P->twM};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     delete P;
@@ -324,49 +325,59 @@ static void fft_pow2_host(std::vector<std::complex<double>> &x) {
     }
 }
 
-// Host-built tables of the FP32 ring FFTs: ring classes, DIF output orders
-// and the Bluestein chirp spectra H = DFT_M(h), h_t = e^{-i pi t^2 / n} for
-// |t| < n (indices mod M), stored in the DIF output order of M.
+// Host-built tables of the FP32 ring FFTs: launch buckets, DIF output
+// orders, the Bluestein chirps c_k = e^{i pi k^2 / n} and chirp spectra
+// H = DFT_M(h), h_t = e^{-i pi t^2 / n} for |t| < n (indices mod M), stored
+// in the DIF output order of M.
+size_t glg_ring32_smem(int kind, int n_or_M, int threads, bool fold) {
+    const size_t zs = (size_t)n_or_M + n_or_M / 16 + 1;
+    size_t slots = zs + 2 * (size_t)threads + n_or_M / 2 + 1;
+    if (kind == 0 && fold) slots += zs;
+    return slots * sizeof(float2);
+}
+
 static int build_fft32_tables(glg_plan *P, cudaStream_t st) {
-    const int nside = P->nside;
-    std::vector<int> radix((size_t)(nside + 1) * GLG_MAX_FFT_STAGES), nst(nside + 1, 0);
-    std::vector<int64_t> pos_ofs(nside + 2, 0), blu_ofs(nside + 1, -1);
+    const int nside = P->nside, mmax = P->mmax;
+    std::vector<int64_t> pos_ofs(nside + 2, 0), blu_ofs(nside + 1, -1), chirp_ofs(nside + 1, -1);
     std::vector<int> blu_M(nside + 1, 0);
-    int64_t nblu = 0;
+    int64_t nblu = 0, nchirp = 0;
     int Mmax = 4;
     for (int i = 1; i <= nside; ++i) {
-        int *r = &radix[(size_t)i * GLG_MAX_FFT_STAGES];
-        factor_ring(4 * i, r, &nst[i]);
+        int r[GLG_MAX_FFT_STAGES];
         pos_ofs[i + 1] = pos_ofs[i] + 4LL * i;
-        bool large = false;
-        for (int s = 0; s < nst[i]; ++s) large |= r[s] > 13;
-        if (large) {
+        if (glg_fft32_radices(4 * i, r) < 0) {
             int M = 1;
             while (M < 2 * 4 * i - 1) M <<= 1;
             blu_M[i] = M;
             blu_ofs[i] = nblu;
             nblu += M;
+            chirp_ofs[i] = nchirp;
+            nchirp += 4 * i;
             if (M > Mmax) Mmax = M;
         }
     }
     std::vector<uint16_t> pos16(pos_ofs[nside + 1]);
-    for (int i = 1; i <= nside; ++i)
-        for (int k = 0; k < 4 * i; ++k)
-            pos16[pos_ofs[i] + k] = (uint16_t)dif_pos_host(&radix[(size_t)i * GLG_MAX_FFT_STAGES], nst[i], 4 * i, k);
-    std::vector<float2> H((size_t)(nblu > 0 ? nblu : 1));
+    for (int i = 1; i <= nside; ++i) {
+        int r[GLG_MAX_FFT_STAGES];
+        const int ns = glg_fft32_radices(4 * i, r);
+        if (ns < 0) continue;
+        for (int k = 0; k < 4 * i; ++k) pos16[pos_ofs[i] + k] = (uint16_t)dif_pos_host(r, ns, 4 * i, k);
+    }
+    std::vector<float2> H((size_t)(nblu > 0 ? nblu : 1)), chirp((size_t)(nchirp > 0 ? nchirp : 1));
     for (int i = 1; i <= nside; ++i) {
         const int M = blu_M[i];
         if (!M) continue;
         const int n = 4 * i;
         std::vector<std::complex<double>> h(M, 0.0);
         for (int t = 0; t < n; ++t) {
-            const double ph = -M_PI * (double)(((int64_t)t * t) % (2LL * n)) / n;
-            h[t] = std::complex<double>(cos(ph), sin(ph));
+            const double ph = M_PI * (double)(((int64_t)t * t) % (2LL * n)) / n;
+            chirp[chirp_ofs[i] + t] = make_float2((float)cos(ph), (float)sin(ph));
+            h[t] = std::complex<double>(cos(ph), -sin(ph));
             if (t > 0) h[M - t] = h[t];
         }
         fft_pow2_host(h);
-        int mr[GLG_MAX_FFT_STAGES], mns = 0;
-        factor_ring(M, mr, &mns);
+        int mr[GLG_MAX_FFT_STAGES];
+        const int mns = glg_fft32_radices(M, mr);
         for (int k = 0; k < M; ++k) {
             const int q = dif_pos_host(mr, mns, M, k);
             H[blu_ofs[i] + q] = make_float2((float)h[k].real(), (float)h[k].imag());
@@ -375,32 +386,62 @@ static int build_fft32_tables(glg_plan *P, cudaStream_t st) {
     std::vector<float2> twM(Mmax / 2 + 1);
     for (int t = 0; t <= Mmax / 2; ++t)
         twM[t] = make_float2((float)cos(2.0 * M_PI * t / Mmax), (float)sin(2.0 * M_PI * t / Mmax));
-    std::vector<int> c0, c1;
+
+    // buckets: Bluestein rings by M, mixed-radix rings by (next power of two
+    // of n, whether m folds onto the ring); largest work first
+    struct Key {
+        int kind, size, fold;
+        bool operator<(const Key &o) const {
+            if (size != o.size) return size > o.size;
+            if (kind != o.kind) return kind > o.kind;
+            return fold > o.fold;
+        }
+    };
+    std::map<Key, std::vector<int>> groups;
     for (int p = 0; p < P->npairs; ++p) {
         const int i = p + 1 < nside ? p + 1 : nside;
-        (blu_M[i] ? c1 : c0).push_back(p);
+        const int n = 4 * i;
+        if (blu_M[i]) {
+            groups[{1, blu_M[i], 0}].push_back(p);
+        } else {
+            int nb = 1;
+            while (nb < n) nb <<= 1;
+            groups[{0, nb, n <= mmax ? 1 : 0}].push_back(p);
+        }
     }
-    P->ncls0 = (int)c0.size();
-    P->ncls1 = (int)c1.size();
+    GLG_REQUIRE((int)groups.size() <= GLG_MAX_RING_BUCKETS, "fast ring FFT: too many ring buckets");
+    std::vector<int> bpairs;
+    P->nbuckets = 0;
+    for (auto &kv : groups) {
+        glg_ring_bucket &b = P->buckets[P->nbuckets++];
+        b.kind = kv.first.kind;
+        b.threads = kv.first.size >= 4096 ? 512 : 256;
+        b.smem = glg_ring32_smem(b.kind, kv.first.size, b.threads, kv.first.fold != 0);
+        b.count = (int)kv.second.size();
+        b.first = (int64_t)bpairs.size();
+        bpairs.insert(bpairs.end(), kv.second.begin(), kv.second.end());
+    }
     P->blu_Mmax = Mmax;
     int rc;
-    if ((rc = dalloc(P, &P->cls0_pairs, c0.size())) || (rc = dalloc(P, &P->cls1_pairs, c1.size())) ||
+    if ((rc = dalloc(P, &P->bucket_pairs, bpairs.size())) ||
         (rc = dalloc(P, &P->pos_ofs, pos_ofs.size())) || (rc = dalloc(P, &P->pos16, pos16.size())) ||
         (rc = dalloc(P, &P->blu_ofs, blu_ofs.size())) || (rc = dalloc(P, &P->blu_M, blu_M.size())) ||
-        (rc = dalloc(P, &P->blu_H, H.size())) || (rc = dalloc(P, &P->twM, twM.size())))
+        (rc = dalloc(P, &P->blu_H, H.size())) || (rc = dalloc(P, &P->twM, twM.size())) ||
+        (rc = dalloc(P, &P->chirp_ofs, chirp_ofs.size())) || (rc = dalloc(P, &P->chirp, chirp.size())))
         return rc;
     cudaError_t e = cudaSuccess;
     auto up = [&](void *dst, const void *src, size_t bytes) {
         if (e == cudaSuccess && bytes) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st);
     };
-    up(P->cls0_pairs, c0.data(), sizeof(int) * c0.size());
-    up(P->cls1_pairs, c1.data(), sizeof(int) * c1.size());
+    up(P->bucket_pairs, bpairs.data(), sizeof(int) * bpairs.size());
     up(P->pos_ofs, pos_ofs.data(), sizeof(int64_t) * pos_ofs.size());
     up(P->pos16, pos16.data(), sizeof(uint16_t) * pos16.size());
     up(P->blu_ofs, blu_ofs.data(), sizeof(int64_t) * blu_ofs.size());
     up(P->blu_M, blu_M.data(), sizeof(int) * blu_M.size());
     up(P->blu_H, H.data(), sizeof(float2) * H.size());
     up(P->twM, twM.data(), sizeof(float2) * twM.size());
+    up(P->chirp_ofs, chirp_ofs.data(), sizeof(int64_t) * chirp_ofs.size());
+    up(P->chirp, chirp.data(), sizeof(float2) * chirp.size());
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // host vectors go out of scope
     if (e != cudaSuccess) return glg_cuda_status(e, "glg_plan_prepare_fast: FFT tables");
     return GLG_OK;

@@ -185,13 +185,6 @@ __device__ __forceinline__ double apply_epi(double v, int kind, double var, doub
     }
     return v;
 }
-__device__ __forceinline__ float apply_epi(float v, int kind, double var, double lam) {
-    if (kind == GLG_EPI_LOGNORMAL) {
-        v = expm1f(v - (float)(var * 0.5));
-        if (lam != 1.0) v = (float)lam * v;
-    }
-    return v;
-}
 
 struct EpiArgs {
     int kind[8];  // per map of this launch chunk

@@ -7,21 +7,37 @@
 // inverse DFT of length n and stores both rings with the fused field
 // transform (glass/grf/_transformations.py:83-89).
 //
-// Ring lengths n = 4 i whose prime factors are all <= 13 use an in-place
-// mixed-radix decimation-in-frequency FFT whose twiddles come from a
-// shared-memory table.  Lengths with a larger prime factor use Bluestein's
-// algorithm: the DFT becomes a cyclic convolution of length M (a power of
-// two, M >= 2n - 1) with the chirp h_t = e^{-i pi t^2 / n}, computed as a
-// forward DIF FFT, a product with the precomputed chirp spectrum (stored in
-// the DIF output order) and the adjoint of the DIF FFT, so that no
-// permutation pass is needed.
+// Fold.  With G_m = F_m e^{i m phi0} and phi0 = h pi / n (h = 1 on rings
+// whose first pixel sits half a step off phi = 0),
+//   B_k = sum_{m = k mod n} c_m G_m + sum_{m = -k mod n} c_m conj(G_m),
+// c_0 = 1/2, c_m = 1 otherwise.  Since e^{i pi (k + n j) / n} =
+// e^{i pi k / n} (-1)^j, both sums come from one signed fold per residue,
+//   S_k = sum_j (-1)^{h j} c_{k+nj} F_{k+nj},
+//   B_k = w_k S_k + conj(w_k' S_k'),  w_k = e^{i pi h k / n}, k' = -k mod n,
+// so every F_m is read once and the phases cost one table value per k.
+//
+// Transforms.  Lengths n = 4 i whose prime factors are all <= 13 use an
+// in-place mixed-radix decimation-in-frequency FFT (radix 16 and 8
+// butterflies in registers, then 4 or 2, then odd primes); the output order is
+// undone through a per-length position table.  Lengths with a larger prime
+// factor use Bluestein's algorithm: the DFT becomes a cyclic convolution of
+// power-of-two length M >= 2n - 1 with the chirp h_t = e^{-i pi t^2 / n},
+// computed as a forward DIF FFT, a product with the chirp spectrum (stored in
+// DIF output order) and the adjoint of the DIF FFT, so no permutation pass is
+// needed.  Shared-memory buffers are padded one slot per 16 values
+// (glg_zi) so that every power-of-two stride is free of bank conflicts.
+//
+// Rings are launched in size buckets built with the plan (one launch per
+// bucket, all maps of the call in one grid with the map index fastest, so the
+// blocks that share a ring's tables run together).
 #include <cuda_runtime.h>
 
 #include "glg_internal.cuh"
 
 namespace {
 
-constexpr int T32 = 256;
+constexpr int TMAX = 512;
+constexpr int EPI_MAX = 40;
 
 struct c32 {
     float x, y;
@@ -30,133 +46,207 @@ __device__ __forceinline__ c32 cmul(c32 a, c32 b) { return {a.x * b.x - a.y * b.
 __device__ __forceinline__ c32 cadd(c32 a, c32 b) { return {a.x + b.x, a.y + b.y}; }
 __device__ __forceinline__ c32 csub(c32 a, c32 b) { return {a.x - b.x, a.y - b.y}; }
 __device__ __forceinline__ c32 cconj(c32 a) { return {a.x, -a.y}; }
-__device__ __forceinline__ c32 ld(const float2 *p) {
-    const float2 v = *p;
+__device__ __forceinline__ c32 cscale(c32 a, float s) { return {a.x * s, a.y * s}; }
+__device__ __forceinline__ c32 ldg(const float2 *p) {
+    const float2 v = __ldg(p);
     return {v.x, v.y};
 }
+__device__ __forceinline__ int zi(int e) { return glg_zi(e); }
 
-// e^{dir 2 pi i t / n} from a half table wh[t] = e^{2 pi i t / n}, t <= n/2.
-__device__ __forceinline__ c32 tw(const c32 *wh, int n, int t, int dir) {
-    c32 w = t <= (n >> 1) ? wh[t] : cconj(wh[n - t]);
-    if (dir < 0) w.y = -w.y;
+// e^{DIR 2 pi i t / n}, 0 <= t < n, from the half table wh[t] = e^{2 pi i t / n}, t <= n/2.
+template <int DIR>
+__device__ __forceinline__ c32 tw(const c32 *wh, int n, int t) {
+    const bool lo = t <= (n >> 1);
+    c32 w = wh[lo ? t : n - t];
+    if (lo != (DIR > 0)) w.y = -w.y;
     return w;
 }
 
-struct FftDesc {
-    int n, nst, dir;
-    int radix[GLG_MAX_FFT_STAGES];
-    const c32 *wh;
-};
+// ------------------------------------------------------- register DFTs
+// y_k = sum_j v_j e^{DIR 2 pi i j k / R}, natural order in and out.
 
-// One radix-RD DIF butterfly: y_k = sum_j v_j w_RD^{jk}, then twiddle w_L^{j1 k}.
-template <int RD>
-__device__ __forceinline__ void dif_bfly(c32 *Z, const FftDesc &f, int base, int msub, int L, int j1) {
-    c32 v[RD], y[RD];
-#pragma unroll
-    for (int j = 0; j < RD; ++j) v[j] = Z[base + msub * j];
-    if (RD == 2) {
-        y[0] = cadd(v[0], v[1]);
-        y[1] = csub(v[0], v[1]);
-    } else if (RD == 4) {
-        const c32 a = cadd(v[0], v[2]), b = csub(v[0], v[2]);
-        const c32 cc = cadd(v[1], v[3]), d = csub(v[1], v[3]);
-        const c32 id = f.dir > 0 ? c32{-d.y, d.x} : c32{d.y, -d.x};
-        y[0] = cadd(a, cc);
-        y[2] = csub(a, cc);
-        y[1] = cadd(b, id);
-        y[3] = csub(b, id);
-    } else {
-        const int step = f.n / RD;
-#pragma unroll
-        for (int k = 0; k < RD; ++k) {
-            c32 acc = v[0];
-#pragma unroll
-            for (int j = 1; j < RD; ++j) acc = cadd(acc, cmul(v[j], tw(f.wh, f.n, ((j * k) % RD) * step, f.dir)));
-            y[k] = acc;
-        }
-    }
-    const int ts = (f.n / L) * j1;
-    Z[base] = y[0];
-#pragma unroll
-    for (int k = 1; k < RD; ++k) Z[base + msub * k] = cmul(y[k], tw(f.wh, f.n, ts * k, f.dir));
+template <int DIR>
+__device__ __forceinline__ c32 mul_i(c32 a) {  // a * (DIR i)
+    return DIR > 0 ? c32{-a.y, a.x} : c32{a.y, -a.x};
 }
 
-// Adjoint of dif_bfly: undo the twiddle (conjugate), then the opposite-direction DFT_RD.
-template <int RD>
-__device__ __forceinline__ void adj_bfly(c32 *Z, const FftDesc &f, int base, int msub, int L, int j1) {
-    c32 v[RD], y[RD];
-    const int ts = (f.n / L) * j1;
-    v[0] = Z[base];
-#pragma unroll
-    for (int k = 1; k < RD; ++k) v[k] = cmul(Z[base + msub * k], tw(f.wh, f.n, ts * k, -f.dir));
-    if (RD == 2) {
-        y[0] = cadd(v[0], v[1]);
-        y[1] = csub(v[0], v[1]);
-    } else if (RD == 4) {
-        const c32 a = cadd(v[0], v[2]), b = csub(v[0], v[2]);
-        const c32 cc = cadd(v[1], v[3]), d = csub(v[1], v[3]);
-        const c32 id = f.dir > 0 ? c32{d.y, -d.x} : c32{-d.y, d.x};
-        y[0] = cadd(a, cc);
-        y[2] = csub(a, cc);
-        y[1] = cadd(b, id);
-        y[3] = csub(b, id);
-    } else {
-        const int step = f.n / RD;
-#pragma unroll
-        for (int j = 0; j < RD; ++j) {
-            c32 acc = v[0];
-#pragma unroll
-            for (int k = 1; k < RD; ++k) acc = cadd(acc, cmul(v[k], tw(f.wh, f.n, ((j * k) % RD) * step, -f.dir)));
-            y[j] = acc;
-        }
-    }
-#pragma unroll
-    for (int j = 0; j < RD; ++j) Z[base + msub * j] = y[j];
+template <int DIR>
+__device__ __forceinline__ void dft4(c32 &v0, c32 &v1, c32 &v2, c32 &v3) {
+    const c32 a = cadd(v0, v2), b = csub(v0, v2), c = cadd(v1, v3), d = mul_i<DIR>(csub(v1, v3));
+    v0 = cadd(a, c);
+    v2 = csub(a, c);
+    v1 = cadd(b, d);
+    v3 = csub(b, d);
 }
 
-template <bool ADJ, bool POW2>
-__device__ __forceinline__ void stage(c32 *Z, const FftDesc &f, int RD, int L) {
-    const int msub = L / RD, nbf = f.n / RD;
+constexpr float R2 = 0.70710678118654752440f;   // cos(pi/4)
+constexpr float C8 = 0.92387953251128675613f;   // cos(pi/8)
+constexpr float S8 = 0.38268343236508977173f;   // sin(pi/8)
+
+template <int DIR>
+__device__ __forceinline__ void dft8(c32 *v) {
+    c32 e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
+    c32 o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
+    dft4<DIR>(e0, e1, e2, e3);
+    dft4<DIR>(o0, o1, o2, o3);
+    // o_k *= e^{DIR 2 pi i k / 8}
+    o1 = c32{R2 * (o1.x - DIR * o1.y), R2 * (o1.y + DIR * o1.x)};
+    o2 = mul_i<DIR>(o2);
+    o3 = c32{R2 * (-o3.x - DIR * o3.y), R2 * (DIR * o3.x - o3.y)};
+    v[0] = cadd(e0, o0);
+    v[4] = csub(e0, o0);
+    v[1] = cadd(e1, o1);
+    v[5] = csub(e1, o1);
+    v[2] = cadd(e2, o2);
+    v[6] = csub(e2, o2);
+    v[3] = cadd(e3, o3);
+    v[7] = csub(e3, o3);
+}
+
+template <int DIR>
+__device__ __forceinline__ void dft16(c32 *v) {
+    // j = j2 + 4 j1: length-4 DFTs over j1, twiddles w16^(j2 k1), length-4
+    // DFTs over j2; y[k1 + 4 k2] lands in u[4 k1 + k2].
+    c32 u[16];
+#pragma unroll
+    for (int j2 = 0; j2 < 4; ++j2) {
+        c32 a = v[j2], b = v[j2 + 4], c = v[j2 + 8], d = v[j2 + 12];
+        dft4<DIR>(a, b, c, d);
+        u[4 * 0 + j2] = a;
+        u[4 * 1 + j2] = b;
+        u[4 * 2 + j2] = c;
+        u[4 * 3 + j2] = d;
+    }
+    const float D = (float)DIR;
+    // u[4 k1 + j2] *= e^{DIR 2 pi i j2 k1 / 16}
+    const c32 w1 = {C8, D * S8}, w2 = {R2, D * R2}, w3 = {S8, D * C8};
+    const c32 w6 = {-R2, D * R2}, w9 = {-C8, -D * S8};
+    u[5] = cmul(u[5], w1);
+    u[6] = cmul(u[6], w2);
+    u[7] = cmul(u[7], w3);
+    u[9] = cmul(u[9], w2);
+    u[10] = mul_i<DIR>(u[10]);
+    u[11] = cmul(u[11], w6);
+    u[13] = cmul(u[13], w3);
+    u[14] = cmul(u[14], w6);
+    u[15] = cmul(u[15], w9);
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1) dft4<DIR>(u[4 * k1], u[4 * k1 + 1], u[4 * k1 + 2], u[4 * k1 + 3]);
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1)
+#pragma unroll
+        for (int k2 = 0; k2 < 4; ++k2) v[k1 + 4 * k2] = u[4 * k1 + k2];
+}
+
+// Odd prime radix with table twiddles e^{DIR 2 pi i (j k mod R) / R}.
+template <int R, int DIR>
+__device__ __forceinline__ void dft_odd(c32 *v, const c32 *wh, int n) {
+    c32 y[R];
+    const int step = n / R;
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        c32 acc = v[0];
+#pragma unroll
+        for (int j = 1; j < R; ++j) acc = cadd(acc, cmul(v[j], tw<DIR>(wh, n, ((j * k) % R) * step)));
+        y[k] = acc;
+    }
+#pragma unroll
+    for (int k = 0; k < R; ++k) v[k] = y[k];
+}
+
+template <int R, int DIR>
+__device__ __forceinline__ void dft(c32 *v, const c32 *wh, int n) {
+    if constexpr (R == 2) {
+        const c32 a = v[0];
+        v[0] = cadd(a, v[1]);
+        v[1] = csub(a, v[1]);
+    } else if constexpr (R == 4) {
+        dft4<DIR>(v[0], v[1], v[2], v[3]);
+    } else if constexpr (R == 8) {
+        dft8<DIR>(v);
+    } else if constexpr (R == 16) {
+        dft16<DIR>(v);
+    } else {
+        dft_odd<R, DIR>(v, wh, n);
+    }
+}
+
+// One in-place DIF pass of radix R (sub-length L) of a length-n transform,
+// or its adjoint.  DIF: y = DFT_R(v), then y_k *= w_L^(DIR j1 k).  Adjoint:
+// v_k *= w_L^(-DIR j1 k), then y = DFT_R^(-DIR)(v).
+template <int R, int DIR, bool ADJ>
+__device__ __forceinline__ void pass(c32 *Z, const c32 *wh, int n, int L) {
+    const int msub = L / R, nbf = n / R, tsc = n / L;
     for (int bf = threadIdx.x; bf < nbf; bf += blockDim.x) {
         const int blk = bf / msub, j1 = bf - blk * msub;
         const int base = blk * L + j1;
-        switch (RD) {
-#define GLG_CASE(R)                                          \
-    case R:                                                  \
-        if (ADJ) adj_bfly<R>(Z, f, base, msub, L, j1);       \
-        else dif_bfly<R>(Z, f, base, msub, L, j1);           \
-        break;
-            GLG_CASE(2) GLG_CASE(4)
-            default:
-                if constexpr (!POW2) {
-                    switch (RD) { GLG_CASE(3) GLG_CASE(5) GLG_CASE(7) GLG_CASE(11) GLG_CASE(13) default: break; }
-                }
-                break;
-#undef GLG_CASE
+        const int ts = tsc * j1;
+        c32 v[R];
+        if constexpr (!ADJ) {
+#pragma unroll
+            for (int j = 0; j < R; ++j) v[j] = Z[zi(base + msub * j)];
+            dft<R, DIR>(v, wh, n);
+            Z[zi(base)] = v[0];
+#pragma unroll
+            for (int k = 1; k < R; ++k) Z[zi(base + msub * k)] = cmul(v[k], tw<DIR>(wh, n, ts * k));
+        } else {
+            v[0] = Z[zi(base)];
+#pragma unroll
+            for (int k = 1; k < R; ++k) v[k] = cmul(Z[zi(base + msub * k)], tw<-DIR>(wh, n, ts * k));
+            dft<R, -DIR>(v, wh, n);
+#pragma unroll
+            for (int j = 0; j < R; ++j) Z[zi(base + msub * j)] = v[j];
         }
     }
     __syncthreads();
 }
 
-template <bool POW2>
-__device__ void fft_dif(c32 *Z, const FftDesc &f) {
-    int L = f.n;
-    for (int s = 0; s < f.nst; ++s) {
-        stage<false, POW2>(Z, f, f.radix[s], L);
-        L /= f.radix[s];
+template <int DIR, bool ADJ, bool POW2>
+__device__ __forceinline__ void pass_any(c32 *Z, const c32 *wh, int n, int R, int L) {
+    switch (R) {
+        case 16: pass<16, DIR, ADJ>(Z, wh, n, L); break;
+        case 8: pass<8, DIR, ADJ>(Z, wh, n, L); break;
+        case 4: pass<4, DIR, ADJ>(Z, wh, n, L); break;
+        case 2: pass<2, DIR, ADJ>(Z, wh, n, L); break;
+        default:
+            if constexpr (!POW2) {
+                switch (R) {
+                    case 3: pass<3, DIR, ADJ>(Z, wh, n, L); break;
+                    case 5: pass<5, DIR, ADJ>(Z, wh, n, L); break;
+                    case 7: pass<7, DIR, ADJ>(Z, wh, n, L); break;
+                    case 11: pass<11, DIR, ADJ>(Z, wh, n, L); break;
+                    case 13: pass<13, DIR, ADJ>(Z, wh, n, L); break;
+                    default: break;
+                }
+            }
+            break;
     }
 }
 
-template <bool POW2>
-__device__ void fft_dif_adjoint(c32 *Z, const FftDesc &f) {
-    int Ls[GLG_MAX_FFT_STAGES];
-    int L = f.n;
-    for (int s = 0; s < f.nst; ++s) {
-        Ls[s] = L;
-        L /= f.radix[s];
+template <int DIR, bool POW2>
+__device__ void fft_dif(c32 *Z, const c32 *wh, int n) {
+    int r[GLG_MAX_FFT_STAGES];
+    const int ns = glg_fft32_radices(n, r);
+    int L = n;
+    for (int s = 0; s < ns; ++s) {
+        pass_any<DIR, false, POW2>(Z, wh, n, r[s], L);
+        L /= r[s];
     }
-    for (int s = f.nst - 1; s >= 0; --s) stage<true, POW2>(Z, f, f.radix[s], Ls[s]);
 }
+
+template <int DIR, bool POW2>
+__device__ void fft_dif_adjoint(c32 *Z, const c32 *wh, int n) {
+    int r[GLG_MAX_FFT_STAGES], Ls[GLG_MAX_FFT_STAGES];
+    const int ns = glg_fft32_radices(n, r);
+    int L = n;
+    for (int s = 0; s < ns; ++s) {
+        Ls[s] = L;
+        L /= r[s];
+    }
+    for (int s = ns - 1; s >= 0; --s) pass_any<DIR, true, POW2>(Z, wh, n, r[s], Ls[s]);
+}
+
+// ------------------------------------------------------------- epilogue
 
 __device__ __forceinline__ float epi(float v, int kind, float hv, float lam) {
     if (kind == GLG_EPI_LOGNORMAL) {
@@ -167,140 +257,193 @@ __device__ __forceinline__ float epi(float v, int kind, float hv, float lam) {
 }
 
 struct Epi32 {
-    int kind[8];
-    float hvar[8], lam[8];  // var / 2 and lambda per map of the launch
+    int kind[EPI_MAX];
+    float hvar[EPI_MAX], lam[EPI_MAX];  // var / 2 and lambda per map
 };
 
 struct RingArgs {
-    int nrings, mmax, nside;
-    const int *pairs;
+    int nrings, mmax, nmaps;
+    const int *pairs;  // ring pairs of this launch
     const int *nph, *half;
     const int64_t *startN, *startS;
-    const int *fft_radix, *fft_nst;
     const int64_t *tw_ofs;
-    const float2 *tw32;
+    const float2 *tw32;  // e^{i pi t / n}, t < 2n, per length
     const int64_t *pos_ofs;
     const uint16_t *pos16;
-    const int64_t *blu_ofs;
+    const int64_t *blu_ofs, *chirp_ofs;
     const int *blu_M;
-    const float2 *blu_H;
-    const float2 *twM;
+    const float2 *blu_H, *chirp, *twM;
     int Mmax;
     const float2 *Ft;  // [map][ring][m]
     float *maps;
     int64_t npix;
-    int map0;
 };
 
-// Fold F_m (m = 0..mmax) of both rings onto n bins, packed as B^N + i B^S:
-// B_k = 1/2 sum_{m = k} c_m G_m + 1/2 sum_{m = -k} c_m conj(G_m), G_m = F_m e^{i m phi0}.
-__device__ __forceinline__ c32 fold(const RingArgs &a, const float2 *FN, const float2 *FS, const float2 *tw2n,
-                                    int n, int h, bool equator, int k) {
-    c32 bn = {0.f, 0.f}, bs = {0.f, 0.f};
-    for (int m = k; m <= a.mmax; m += n) {
-        const float cm = m == 0 ? 0.5f : 1.0f;
-        const c32 ph = h ? ld(tw2n + (m % (2 * n))) : c32{1.f, 0.f};
-        const c32 gn = cmul(ld(FN + m), ph), gs = cmul(ld(FS + m), ph);
-        bn = cadd(bn, c32{cm * gn.x, cm * gn.y});
-        bs = cadd(bs, c32{cm * gs.x, cm * gs.y});
+__device__ __forceinline__ c32 pack(c32 bn, c32 bs) { return {bn.x - bs.y, bn.y + bs.x}; }
+
+// Z[zi(k)] = B^N_k + i B^S_k for k < n (times chirp[k] when chirp != null).
+// SS: scratch of the south fold, element k at SS[zi(soff + k)] (may alias Z
+// beyond n); X: 2 x blockDim partial sums.  Ends with __syncthreads().
+__device__ void fold(const float2 *FN, const float2 *FS, bool equator, int n, int mmax, int h,
+                     const float2 *w2n, const float2 *chirp, c32 *Z, c32 *SS, int soff, c32 *X) {
+    const int T = blockDim.x, t = threadIdx.x;
+    const c32 one = {1.f, 0.f};
+    if (n > mmax) {
+        // at most one term per residue: read F directly
+#pragma unroll 4
+        for (int k = t; k < n; k += T) {
+            const int k2 = k ? n - k : 0;
+            const float ck = k ? 1.f : 0.5f;
+            c32 an = {0.f, 0.f}, as = an, bn = an, bs = an;
+            if (k <= mmax) {
+                an = cscale(ldg(FN + k), ck);
+                as = cscale(ldg(FS + k), ck);
+            }
+            if (k2 <= mmax) {
+                bn = cscale(ldg(FN + k2), ck);
+                bs = cscale(ldg(FS + k2), ck);
+            }
+            const c32 wk = h ? ldg(w2n + k) : one, wk2 = h ? ldg(w2n + k2) : one;
+            const c32 BN = cadd(cmul(wk, an), cconj(cmul(wk2, bn)));
+            c32 BS = cadd(cmul(wk, as), cconj(cmul(wk2, bs)));
+            if (equator) BS = {0.f, 0.f};
+            c32 z = pack(BN, BS);
+            if (chirp) z = cmul(z, ldg(chirp + k));
+            Z[zi(k)] = z;
+        }
+        __syncthreads();
+        return;
     }
-    for (int m = (n - k) % n; m <= a.mmax; m += n) {
-        const float cm = m == 0 ? 0.5f : 1.0f;
-        const c32 ph = h ? ld(tw2n + (m % (2 * n))) : c32{1.f, 0.f};
-        const c32 gn = cconj(cmul(ld(FN + m), ph)), gs = cconj(cmul(ld(FS + m), ph));
-        bn = cadd(bn, c32{cm * gn.x, cm * gn.y});
-        bs = cadd(bs, c32{cm * gs.x, cm * gs.y});
+    // signed fold S_k: one thread per residue, or C threads per residue
+    // (fixed slices, summed in order) when n < blockDim
+    const float sgn = h ? -1.f : 1.f;
+    if (n >= T) {
+        for (int k = t; k < n; k += T) {
+            c32 sn = {0.f, 0.f}, ss = sn;
+            float s = 1.f;
+            for (int m = k; m <= mmax; m += n, s *= sgn) {
+                const float c = m ? s : 0.5f * s;
+                const c32 fn = ldg(FN + m), fs = ldg(FS + m);
+                sn = {fmaf(c, fn.x, sn.x), fmaf(c, fn.y, sn.y)};
+                ss = {fmaf(c, fs.x, ss.x), fmaf(c, fs.y, ss.y)};
+            }
+            Z[zi(k)] = sn;
+            SS[zi(soff + k)] = ss;
+        }
+    } else {
+        const int C = T / n;
+        if (t < C * n) {
+            const int k = t % n, c = t / n;
+            c32 sn = {0.f, 0.f}, ss = sn;
+            const float sC = (h && (C & 1)) ? -1.f : 1.f;  // sign step over C folds
+            float s = (h && (c & 1)) ? -1.f : 1.f;
+            for (int m = k + c * n; m <= mmax; m += C * n, s *= sC) {
+                const float cc = m ? s : 0.5f * s;
+                const c32 fn = ldg(FN + m), fs = ldg(FS + m);
+                sn = {fmaf(cc, fn.x, sn.x), fmaf(cc, fn.y, sn.y)};
+                ss = {fmaf(cc, fs.x, ss.x), fmaf(cc, fs.y, ss.y)};
+            }
+            X[t] = sn;
+            X[T + t] = ss;
+        }
+        __syncthreads();
+        if (t < n) {
+            c32 sn = X[t], ss = X[T + t];
+            for (int c = 1; c < C; ++c) {
+                sn = cadd(sn, X[c * n + t]);
+                ss = cadd(ss, X[T + c * n + t]);
+            }
+            Z[zi(t)] = sn;
+            SS[zi(soff + t)] = ss;
+        }
     }
-    if (equator) bs = {0.f, 0.f};
-    return {bn.x - bs.y, bn.y + bs.x};
+    __syncthreads();
+    // combine the residue pair (k, n - k)
+    for (int k = t; k <= (n >> 1); k += T) {
+        const int k2 = k ? n - k : 0;
+        const c32 an = Z[zi(k)], bn = Z[zi(k2)];
+        c32 as = SS[zi(soff + k)], bs = SS[zi(soff + k2)];
+        if (equator) as = bs = {0.f, 0.f};
+        const c32 wk = h ? ldg(w2n + k) : one, wk2 = h ? ldg(w2n + k2) : one;
+        const c32 pa = cmul(wk, an), pb = cmul(wk2, bn), qa = cmul(wk, as), qb = cmul(wk2, bs);
+        c32 z = pack(cadd(pa, cconj(pb)), cadd(qa, cconj(qb)));
+        if (chirp) z = cmul(z, ldg(chirp + k));
+        Z[zi(k)] = z;
+        if (k2 != k) {
+            c32 z2 = pack(cadd(pb, cconj(pa)), cadd(qb, cconj(qa)));
+            if (chirp) z2 = cmul(z2, ldg(chirp + k2));
+            Z[zi(k2)] = z2;
+        }
+    }
+    __syncthreads();
 }
 
-// Class 0: mixed-radix DIF in shared memory.  smem: Z[n], wh[n/2 + 1].
-__global__ void __launch_bounds__(T32) k_ring32(const RingArgs a, const Epi32 e) {
+// Class 0: mixed-radix DIF.  smem: Z | SS (n <= mmax) | X[2T] | wh[n/2 + 1].
+__global__ void __launch_bounds__(TMAX) k_ring32(const RingArgs a, const Epi32 e) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int p = a.pairs[blockIdx.x];
-    const int slot = blockIdx.y, map = a.map0 + slot;
-    const int n = a.nph[p], i4 = n / 4;
+    const int map = blockIdx.x % a.nmaps;
+    const int p = a.pairs[blockIdx.x / a.nmaps];
+    const int n = a.nph[p], i4 = n / 4, T = blockDim.x;
+    const bool folds = n <= a.mmax;
+    const int zs = n + n / 16 + 1;
     c32 *Z = reinterpret_cast<c32 *>(smem_raw);
-    c32 *wh = Z + n;
-    const float2 *tw2n = a.tw32 + a.tw_ofs[i4];  // e^{i pi t / n}, t < 2n
-    for (int t = threadIdx.x; t <= n / 2; t += blockDim.x) wh[t] = ld(tw2n + 2 * t);
-    FftDesc f;
-    f.n = n;
-    f.nst = a.fft_nst[i4];
-    f.dir = 1;
-    f.wh = wh;
-    for (int s = 0; s < GLG_MAX_FFT_STAGES; ++s) f.radix[s] = a.fft_radix[i4 * GLG_MAX_FFT_STAGES + s];
+    c32 *SS = Z + zs;
+    c32 *X = SS + (folds ? zs : 0);
+    c32 *wh = X + 2 * T;
+    const float2 *w2n = a.tw32 + a.tw_ofs[i4];  // e^{i pi t / n}, t < 2n
+    for (int t = threadIdx.x; t <= n / 2; t += T) wh[t] = ldg(w2n + 2 * t);
     const int rn = p, rs = a.nrings - 1 - p;
     const bool equator = rn == rs;
     const float2 *FN = a.Ft + ((int64_t)map * a.nrings + rn) * (a.mmax + 1);
     const float2 *FS = a.Ft + ((int64_t)map * a.nrings + rs) * (a.mmax + 1);
-    const int h = a.half[p];
-    for (int k = threadIdx.x; k < n; k += blockDim.x) Z[k] = fold(a, FN, FS, tw2n, n, h, equator, k);
-    __syncthreads();
-    fft_dif<false>(Z, f);
+    fold(FN, FS, equator, n, a.mmax, a.half[p], w2n, nullptr, Z, SS, 0, X);
+    fft_dif<1, false>(Z, wh, n);
     const uint16_t *pos = a.pos16 + a.pos_ofs[i4];
     float *mp = a.maps + (int64_t)map * a.npix;
     const int64_t sN = a.startN[p], sS = a.startS[p];
-    const int kind = e.kind[slot];
-    const float hv = e.hvar[slot], lam = e.lam[slot];
-    for (int j = threadIdx.x; j < n; j += blockDim.x) {
-        const c32 v = Z[pos[j]];
+    const int kind = e.kind[map];
+    const float hv = e.hvar[map], lam = e.lam[map];
+    for (int j = threadIdx.x; j < n; j += T) {
+        const c32 v = Z[zi(pos[j])];
         mp[sN + j] = epi(v.x, kind, hv, lam);
         if (!equator) mp[sS + j] = epi(v.y, kind, hv, lam);
     }
 }
 
-// Class 1: Bluestein.  smem: Z[M], wh[M/2 + 1].
-__global__ void __launch_bounds__(T32) k_ring32_blu(const RingArgs a, const Epi32 e) {
+// Class 1: Bluestein.  smem: Z[M] (the south fold scratch sits at n..2n-1) |
+// X[2T] | wh[M/2 + 1].
+__global__ void __launch_bounds__(TMAX) k_ring32_blu(const RingArgs a, const Epi32 e) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int p = a.pairs[blockIdx.x];
-    const int slot = blockIdx.y, map = a.map0 + slot;
-    const int n = a.nph[p], i4 = n / 4;
+    const int map = blockIdx.x % a.nmaps;
+    const int p = a.pairs[blockIdx.x / a.nmaps];
+    const int n = a.nph[p], i4 = n / 4, T = blockDim.x;
     const int M = a.blu_M[i4];
     c32 *Z = reinterpret_cast<c32 *>(smem_raw);
-    c32 *wh = Z + M;
+    c32 *X = Z + (M + M / 16 + 1);
+    c32 *wh = X + 2 * T;
     const int stride = a.Mmax / M;
-    for (int t = threadIdx.x; t <= M / 2; t += blockDim.x) wh[t] = ld(a.twM + (int64_t)t * stride);
-    FftDesc f;
-    f.n = M;
-    f.dir = -1;
-    f.wh = wh;
-    {
-        int r = M, s = 0;
-        while (r % 4 == 0 && r > 1) { f.radix[s++] = 4; r /= 4; }
-        while (r % 2 == 0) { f.radix[s++] = 2; r /= 2; }
-        f.nst = s;
-    }
-    const float2 *tw2n = a.tw32 + a.tw_ofs[i4];  // e^{i pi t / n}: the chirp b_t = tw2n[t^2 mod 2n]
+    for (int t = threadIdx.x; t <= M / 2; t += T) wh[t] = ldg(a.twM + (int64_t)t * stride);
+    const float2 *w2n = a.tw32 + a.tw_ofs[i4];
+    const float2 *chirp = a.chirp + a.chirp_ofs[i4];  // e^{i pi k^2 / n}
     const int rn = p, rs = a.nrings - 1 - p;
     const bool equator = rn == rs;
     const float2 *FN = a.Ft + ((int64_t)map * a.nrings + rn) * (a.mmax + 1);
     const float2 *FS = a.Ft + ((int64_t)map * a.nrings + rs) * (a.mmax + 1);
-    const int h = a.half[p];
-    for (int k = threadIdx.x; k < M; k += blockDim.x) {
-        c32 v = {0.f, 0.f};
-        if (k < n) {
-            const c32 x = fold(a, FN, FS, tw2n, n, h, equator, k);
-            v = cmul(x, ld(tw2n + (int)(((int64_t)k * k) % (2 * n))));
-        }
-        Z[k] = v;
-    }
+    fold(FN, FS, equator, n, a.mmax, a.half[p], w2n, chirp, Z, Z, n, X);
+    for (int k = n + threadIdx.x; k < M; k += T) Z[zi(k)] = {0.f, 0.f};
     __syncthreads();
-    fft_dif<true>(Z, f);
+    fft_dif<-1, true>(Z, wh, M);
     const float2 *H = a.blu_H + a.blu_ofs[i4];
-    for (int k = threadIdx.x; k < M; k += blockDim.x) Z[k] = cmul(Z[k], ld(H + k));
+    for (int k = threadIdx.x; k < M; k += T) Z[zi(k)] = cmul(Z[zi(k)], ldg(H + k));
     __syncthreads();
-    fft_dif_adjoint<true>(Z, f);
+    fft_dif_adjoint<-1, true>(Z, wh, M);
     float *mp = a.maps + (int64_t)map * a.npix;
     const int64_t sN = a.startN[p], sS = a.startS[p];
-    const int kind = e.kind[slot];
-    const float hv = e.hvar[slot], lam = e.lam[slot];
+    const int kind = e.kind[map];
+    const float hv = e.hvar[map], lam = e.lam[map];
     const float invM = 1.0f / (float)M;
-    for (int j = threadIdx.x; j < n; j += blockDim.x) {
-        c32 v = cmul(Z[j], ld(tw2n + (int)(((int64_t)j * j) % (2 * n))));
-        v.x *= invM;
-        v.y *= invM;
+    for (int j = threadIdx.x; j < n; j += T) {
+        const c32 v = cscale(cmul(Z[zi(j)], ldg(chirp + j)), invM);
         mp[sN + j] = epi(v.x, kind, hv, lam);
         if (!equator) mp[sS + j] = epi(v.y, kind, hv, lam);
     }
@@ -328,63 +471,64 @@ __global__ void k_transpose32(const float2 *__restrict__ F, float2 *__restrict__
 
 int glg_launch_ring_syn_f32(const glg_plan *P, const float2 *F, float2 *Ft, int nmaps, float *maps,
                             const glg_epilogue *epi_in, cudaStream_t st) {
+    if (nmaps > EPI_MAX) {
+        glg_set_error("fast ring FFT: at most 40 maps per call");
+        return GLG_ERR_UNSUPPORTED;
+    }
     const int nm = P->mmax + 1, nr = P->nrings;
+    for (int b = 0; b < P->nbuckets; ++b)
+        if (P->buckets[b].smem > 227 * 1024) {
+            glg_set_error("fast ring FFT: ring length too large for shared memory (nside <= 2048)");
+            return GLG_ERR_UNSUPPORTED;
+        }
     {
         dim3 grid((nr + 31) / 32, (nm + 31) / 32, nmaps);
         GLG_LAUNCH_SCOPE("k_transpose32", st);
         k_transpose32<<<grid, dim3(32, 8), 0, st>>>(F, Ft, nm, nr);
         GLG_CHECK_LAUNCH("k_transpose32");
     }
-    const size_t smem0 = sizeof(c32) * ((size_t)4 * P->nside + 2 * P->nside + 1);
-    const size_t smem1 = sizeof(c32) * ((size_t)P->blu_Mmax + P->blu_Mmax / 2 + 1);
-    if (smem0 > 227 * 1024 || (P->ncls1 > 0 && smem1 > 227 * 1024)) {
-        glg_set_error("fast ring FFT: ring length too large for shared memory (nside <= 2048)");
-        return GLG_ERR_UNSUPPORTED;
-    }
-    cudaFuncSetAttribute(k_ring32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem0);
-    cudaFuncSetAttribute(k_ring32_blu, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
     RingArgs a;
     a.nrings = nr;
     a.mmax = P->mmax;
-    a.nside = P->nside;
+    a.nmaps = nmaps;
     a.nph = P->nph;
     a.half = P->half;
     a.startN = P->startN;
     a.startS = P->startS;
-    a.fft_radix = P->fft_radix;
-    a.fft_nst = P->fft_nst;
     a.tw_ofs = P->tw_ofs;
     a.tw32 = P->tw32;
     a.pos_ofs = P->pos_ofs;
     a.pos16 = P->pos16;
     a.blu_ofs = P->blu_ofs;
+    a.chirp_ofs = P->chirp_ofs;
     a.blu_M = P->blu_M;
     a.blu_H = P->blu_H;
+    a.chirp = P->chirp;
     a.twM = P->twM;
     a.Mmax = P->blu_Mmax;
     a.Ft = Ft;
     a.maps = maps;
     a.npix = P->npix;
-    for (int m0 = 0; m0 < nmaps; m0 += 8) {
-        const int cnt = nmaps - m0 < 8 ? nmaps - m0 : 8;
-        Epi32 e;
-        for (int k = 0; k < 8; ++k) {
-            const bool on = epi_in && k < cnt;
-            e.kind[k] = !on ? GLG_EPI_NONE : (epi_in->kinds ? epi_in->kinds[m0 + k] : epi_in->kind);
-            e.hvar[k] = (on && epi_in->var) ? (float)(0.5 * epi_in->var[m0 + k]) : 0.f;
-            e.lam[k] = (on && epi_in->lamda) ? (float)epi_in->lamda[m0 + k] : 1.f;
-        }
-        a.map0 = m0;
-        if (P->ncls1 > 0) {
-            a.pairs = P->cls1_pairs;
+    Epi32 e;
+    for (int k = 0; k < EPI_MAX; ++k) {
+        const bool on = epi_in && k < nmaps;
+        e.kind[k] = !on ? GLG_EPI_NONE : (epi_in->kinds ? epi_in->kinds[k] : epi_in->kind);
+        e.hvar[k] = (on && epi_in->var) ? (float)(0.5 * epi_in->var[k]) : 0.f;
+        e.lam[k] = (on && epi_in->lamda) ? (float)epi_in->lamda[k] : 1.f;
+    }
+    for (int b = 0; b < P->nbuckets; ++b) {
+        const glg_ring_bucket &B = P->buckets[b];
+        a.pairs = P->bucket_pairs + B.first;
+        const unsigned grid = (unsigned)B.count * (unsigned)nmaps;
+        if (B.kind == 1) {
+            cudaFuncSetAttribute(k_ring32_blu, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)B.smem);
             GLG_LAUNCH_SCOPE("k_ring32_blu", st);
-            k_ring32_blu<<<dim3(P->ncls1, cnt), T32, smem1, st>>>(a, e);
+            k_ring32_blu<<<grid, B.threads, B.smem, st>>>(a, e);
             GLG_CHECK_LAUNCH("k_ring32_blu");
-        }
-        if (P->ncls0 > 0) {
-            a.pairs = P->cls0_pairs;
+        } else {
+            cudaFuncSetAttribute(k_ring32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)B.smem);
             GLG_LAUNCH_SCOPE("k_ring32", st);
-            k_ring32<<<dim3(P->ncls0, cnt), T32, smem0, st>>>(a, e);
+            k_ring32<<<grid, B.threads, B.smem, st>>>(a, e);
             GLG_CHECK_LAUNCH("k_ring32");
         }
     }

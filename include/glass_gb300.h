@@ -125,6 +125,22 @@ int glg_multalm(const void *alm, const double *bl, int lmax, int dtype, void *ou
 int glg_almxfl(const void *alm, const double *fl, int nfl, int lmax, int nmaps, int dtype,
                void *out, void *stream);
 
+/*
+ * Per-pixel Poisson galaxy counts, replacing glass/points.py:252-348
+ * (_compute_expected_count, _apply_visibility, _sample_number_galaxies):
+ *   n_e = ((bias * delta_e - offset) + 1) * scale  [* vis_e],  clipped at 0,
+ *   counts_e ~ Poisson(n_e)
+ * with scale = ARCMIN2_SPHERE / npix * ngal and offset the monopole that
+ * remove_monopole subtracts (0 otherwise).  delta: float64 or float32
+ * [npix] (dtype); vis: float64 [npix] or NULL; counts: int64 [npix].  The
+ * draw uses the Philox stream (key seed, stream sid < 2^32, element = pixel)
+ * and is reproducible bit for bit from the same delta values, whatever their
+ * producer (plain or fast form).
+ */
+int glg_poisson_counts(const void *delta, int dtype, int64_t npix, double bias, double offset,
+                       double scale, const double *vis, uint64_t seed, uint64_t sid,
+                       int64_t *counts, void *stream);
+
 /* Fused epilogue applied while maps are stored. */
 typedef struct glg_epilogue {
     int kind;             /* GLG_EPI_* for every map, unless `kinds` is set  */

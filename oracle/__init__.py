@@ -82,6 +82,11 @@ def _declare(L: ctypes.CDLL) -> None:
     L.orc_philox4x32_10.restype = None
     L.orc_philox_normals.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int64, ctypes.c_int64, dp, u32p]
     L.orc_philox_normals.restype = None
+    L.orc_poisson_counts.argtypes = [dp, ctypes.c_int64, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                     dp, ctypes.c_uint64, ctypes.c_uint32, i64p]
+    L.orc_poisson_counts.restype = None
+    L.orc_exp_neg.argtypes = [ctypes.c_double]
+    L.orc_exp_neg.restype = ctypes.c_double
     L.orc_num_threads.argtypes = []
     L.orc_num_threads.restype = ctypes.c_int
 

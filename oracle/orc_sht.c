@@ -18,7 +18,9 @@
  *     checked bit for bit;
  *   - the Philox4x32-10 counter-based generator (Salmon et al., SC'11) and
  *     the Box-Muller map that the GPU path uses in place of numpy's PCG64
- *     (the RNG seam is glass/rng.py:21-55).
+ *     (the RNG seam is glass/rng.py:21-55);
+ *   - the per-pixel Poisson galaxy counts of glass/points.py:252-348, with
+ *     the GPU kernel's exact operation order so counts agree bit for bit.
  *
  * Conventions (HEALPix, with the Condon-Shortley phase):
  *   Y_lm(theta, phi) = lambda_lm(cos theta) exp(i m phi),
@@ -498,6 +500,79 @@ void orc_philox_normals(uint64_t seed, uint64_t sid, int64_t offset, int64_t n,
         double r = sqrt(-2.0 * log(u1));
         z[2 * i] = r * cos(2.0 * M_PI * u2);
         z[2 * i + 1] = r * sin(2.0 * M_PI * u2);
+    }
+}
+
+/* ---------------------------------------------------------- poisson */
+
+/*
+ * Per-pixel Poisson counts of glass/points.py:252-348 (expected count
+ * n = ((b delta - offset) + 1) scale [* vis], clipped at 0, one Poisson draw
+ * per pixel), restating the GPU kernel's exact operation sequence so the
+ * counts agree bit for bit.  e^{-x} is a Cody-Waite reduction plus a degree-13
+ * Taylor polynomial (no libm), every step a single rounded FP64 operation
+ * (this file is built with -ffp-contract=off).  Poisson(n) is a sum of
+ * pieces of mean <= 256 (Poisson additivity), each drawn by sequential
+ * inversion from one 53-bit uniform; piece c of pixel e uses words
+ * 2(c&1), 2(c&1)+1 of the Philox block with counter (e_lo, e_hi, sid, c>>1).
+ */
+double orc_exp_neg(double x)
+{
+    const double inv_ln2 = 0x1.71547652b82fep+0;
+    const double ln2_hi = 0x1.62e42fee00000p-1, ln2_lo = 0x1.a39ef35793c76p-33;
+    static const double c[14] = {
+        0x1.0000000000000p+0, 0x1.0000000000000p+0, 0x1.0000000000000p-1, 0x1.5555555555555p-3,
+        0x1.5555555555555p-5, 0x1.1111111111111p-7, 0x1.6c16c16c16c17p-10, 0x1.a01a01a01a01ap-13,
+        0x1.a01a01a01a01ap-16, 0x1.71de3a556c734p-19, 0x1.27e4fb7789f5cp-22, 0x1.ae64567f544e4p-26,
+        0x1.1eed8eff8d898p-29, 0x1.6124613a86d09p-33};
+    double kd = floor(x * inv_ln2 + 0.5);
+    double r = (x - kd * ln2_hi) - kd * ln2_lo;
+    double y = -r;
+    double p = c[13];
+    for (int i = 12; i >= 0; --i) p = p * y + c[i];
+    return ldexp(p, -(int)kd);
+}
+
+static int64_t orc_poisson_piece(double lam, double u)
+{
+    double p = orc_exp_neg(lam), F = p;
+    int64_t k = 0;
+    while (u > F && p > 0.0 && k < (1 << 20)) {
+        k += 1;
+        p = (p * lam) / (double)k;
+        F = F + p;
+    }
+    return k;
+}
+
+static double orc_u53(uint32_t a, uint32_t b)
+{
+    return ((double)(a >> 5) * 67108864.0 + (double)(b >> 6) + 0.5) * 1.1102230246251565e-16;
+}
+
+void orc_poisson_counts(const double *delta, int64_t npix, double bias, double offset, double scale,
+                        const double *vis, uint64_t seed, uint32_t sid, int64_t *counts)
+{
+    const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+#pragma omp parallel for schedule(dynamic, 4096)
+    for (int64_t e = 0; e < npix; ++e) {
+        double n = ((bias * delta[e]) - offset) + 1.0;
+        n = n * scale;
+        if (vis) n = n * vis[e];
+        double rest = n > 0.0 ? n : 0.0;
+        int64_t total = 0;
+        uint32_t x[4] = {0, 0, 0, 0};
+        for (uint32_t c = 0; rest > 0.0; ++c) {
+            double lam = rest > 256.0 ? 256.0 : rest;
+            rest = rest - lam;
+            if ((c & 1u) == 0u) {
+                uint32_t ctr[4] = {(uint32_t)e, (uint32_t)((uint64_t)e >> 32), sid, c >> 1};
+                orc_philox4x32_10(ctr, key, x);
+            }
+            double u = (c & 1u) ? orc_u53(x[2], x[3]) : orc_u53(x[0], x[1]);
+            total += orc_poisson_piece(lam, u);
+        }
+        counts[e] = total;
     }
 }
 

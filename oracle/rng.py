@@ -35,3 +35,17 @@ def complex_normals(seed: int, stream: int, offset: int, n: int, raw: bool = Fal
         None if r is None else r.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)),
     )
     return (z, r) if raw else z
+
+
+def poisson_counts(delta, *, bias: float = 1.0, offset: float = 0.0, scale: float = 1.0, vis=None,
+                   seed: int = 42, stream: int = 0) -> np.ndarray:
+    """Per-pixel Poisson counts of the GPU stream (bit-exact restatement)."""
+    d = np.ascontiguousarray(delta, dtype=np.float64)
+    v = None if vis is None else np.ascontiguousarray(vis, dtype=np.float64)
+    out = np.empty(d.size, dtype=np.int64)
+    dp = ctypes.POINTER(ctypes.c_double)
+    lib().orc_poisson_counts(
+        d.ctypes.data_as(dp), ctypes.c_int64(d.size), ctypes.c_double(bias), ctypes.c_double(offset),
+        ctypes.c_double(scale), None if v is None else v.ctypes.data_as(dp), ctypes.c_uint64(seed),
+        ctypes.c_uint32(stream), out.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)))
+    return out

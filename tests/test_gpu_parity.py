@@ -329,3 +329,40 @@ def test_generate_fast_vs_plain(g):
     assert fast.dtype == np.float32
     for s in range(6):
         assert rel_rms(fast[s], plain[s]) < FAST_RMS
+
+
+# ------------------------------------------------------- Poisson counts
+
+
+def test_poisson_counts_bit_exact_vs_oracle(g):
+    """Counts of glass/points.py:252-348 from the Philox stream: bit-exact
+    with the host restatement, for float64 and float32 delta (same values),
+    with bias, visibility, clipped and NaN pixels and means far above 256."""
+    import torch
+
+    rng = np.random.default_rng(11)
+    npix = 12 * 64 * 64
+    d = np.exp(rng.normal(0.0, 1.2, npix)) - 1.0
+    d[:50] = -5.0
+    d[50:60] = np.nan
+    d[60:80] = 2000.0  # expected counts of ~10^4: forty pieces
+    vis = rng.uniform(0.0, 1.0, npix)
+    ngal = 5.0 * npix / g.points.ARCMIN2_SPHERE  # 5 per pixel
+    scale = g.points.ARCMIN2_SPHERE / npix * ngal
+    got = g.points.counts_from_delta(ngal, d, 1.3, vis, rng=g.rng.Generator(7))
+    ref = orng.poisson_counts(d, bias=1.3, scale=scale, vis=vis, seed=7, stream=0)
+    assert got.dtype == np.int64
+    np.testing.assert_array_equal(got, ref)
+    assert np.all(got[:60] == 0) and got[60:80].min() > 5000
+    d32 = d.astype(np.float32)
+    got32 = g.points.counts_from_delta(ngal, torch.as_tensor(d32, device="cuda"), rng=g.rng.Generator(7))
+    assert isinstance(got32, torch.Tensor) and got32.dtype == torch.int64
+    np.testing.assert_array_equal(got32.cpu().numpy(),
+                                  orng.poisson_counts(d32.astype(np.float64), scale=scale, seed=7, stream=0))
+    # remove_monopole subtracts the mean of the biased delta
+    got_m = g.points.counts_from_delta(ngal, d[80:], remove_monopole=True, rng=g.rng.Generator(2))
+    n2 = d.size - 80
+    ref_m = orng.poisson_counts(d[80:], offset=float(np.mean(d[80:])), scale=g.points.ARCMIN2_SPHERE / n2 * ngal,
+                                seed=2, stream=0)
+    assert np.mean(got_m == ref_m) > 0.999  # the offset is a device mean: may differ in the last bit
+    assert g.points.counts_from_delta(ngal, np.zeros(0)).size == 0

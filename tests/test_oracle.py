@@ -139,3 +139,38 @@ def test_multalm_and_reorder_match_reference(golden):
     inp = np.array([0, 10, 11, 20, 21, 22, 30, 31, 32, 33], dtype=complex)
     np.testing.assert_array_equal(of.glass_to_healpix_alm(inp),
                                   np.array([0, 10, 20, 30, 11, 21, 31, 22, 32, 33], dtype=complex))
+
+
+def test_poisson_exp_accuracy():
+    """The library-free e^{-x} of the count sampler is within a few ulp of exp."""
+    from oracle import lib
+
+    xs = np.concatenate([np.linspace(0.0, 256.0, 20001), [1e-300, 0.5 * np.log(2.0), 255.999]])
+    got = np.array([lib().orc_exp_neg(float(x)) for x in xs])
+    ref = np.exp(-xs)
+    assert np.max(np.abs(got - ref) / ref) < 5e-16
+
+
+def test_poisson_counts_statistics_and_streams():
+    rng = np.random.default_rng(0)
+    d = rng.normal(0.0, 0.4, 400_000)
+    c1 = orng.poisson_counts(d, scale=5.0, seed=1, stream=2)
+    assert c1.dtype == np.int64
+    np.testing.assert_array_equal(c1, orng.poisson_counts(d, scale=5.0, seed=1, stream=2))
+    assert np.mean(c1 != orng.poisson_counts(d, scale=5.0, seed=1, stream=3)) > 0.5
+    lam = np.clip((d + 1.0) * 5.0, 0.0, None)
+    n = d.size
+    assert abs(c1.mean() - lam.mean()) < 5 * np.sqrt(lam.mean() / n)
+    # Var[N] = E[lam] + Var[lam] for a Poisson mixture
+    assert abs(c1.var() / (lam.mean() + lam.var()) - 1.0) < 0.02
+    # pieces of mean 256: large means keep mean and variance
+    big = orng.poisson_counts(np.zeros(100_000), scale=1000.0, seed=5)
+    assert abs(big.mean() - 1000.0) < 5 * np.sqrt(1000.0 / 1e5)
+    assert abs(big.var() / 1000.0 - 1.0) < 0.03
+    # clipping, NaN and the visibility / bias / offset arithmetic
+    z = orng.poisson_counts(np.array([-3.0, np.nan, -1.0]), scale=5.0)
+    np.testing.assert_array_equal(z, [0, 0, 0])
+    vis = rng.uniform(0.0, 1.0, 1000)
+    a = orng.poisson_counts(d[:1000], bias=1.5, offset=0.1, scale=2.0, vis=vis, seed=9)
+    b = orng.poisson_counts(((1.5 * d[:1000] - 0.1) + 1.0) * 2.0 * vis, scale=1.0, bias=1.0, offset=1.0, seed=9)
+    assert np.mean(a == b) > 0.99  # same uniforms, expected counts equal up to rounding
