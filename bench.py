@@ -14,7 +14,12 @@ Printed JSON (one line, rank 0):
             (numpy) maps, copies inside the timed region,
   plain  -- the FP64 drop-in form on the same workload, and the fast form's
             relative RMS map error against it,
-  roofline / gpu_launches / clocks / cpu_baseline as described in DESIGN.md.
+  roofline / gpu_launches / clocks / cpu_baseline as described in DESIGN.md,
+  serving -- p50/p99 latency and shell-maps/s of the serving workload: a
+            Poisson stream of 2000 requests (nside in {128, 256, 512, 1024},
+            lmax = 2 nside, 3-20 lognormal shells each) at 70% of the
+            measured capacity, continuous batching within a 120 GB HBM
+            budget; beside it the FP64 form without batching on a sample.
 
 ``--impl reference`` times the CPU restatement of the reference's path
 (oracle/: GLASS glue + FP64 ring SHT with all host threads) on a bounded
@@ -53,6 +58,96 @@ def spectra_cfg3(nshell: int, lmax: int, seed: int = 0):
     gls = [np.exp(-abs(i - j) / 3.0) * np.sqrt(auto[i] * auto[j])
            for i in range(nshell) for j in range(i, -1, -1)]
     return gls, lam
+
+
+def spectra_cfg2(nshell: int, lmax: int, seed: int = 0):
+    """Request spectra of the serving workload: A_i (l+1)^-1.2 e^{-(l/800)^2},
+    A_i log-uniform in [1e-3, 1e-1], correlation exp(-|i-j|/1.5), shifts
+    uniform in [0.5, 2]."""
+    rng = np.random.default_rng(seed)
+    amp = 10 ** rng.uniform(-3, -1, nshell)
+    lam = rng.uniform(0.5, 2.0, nshell)
+    ell = np.arange(lmax + 1)
+    auto = [a * (ell + 1.0) ** -1.2 * np.exp(-((ell / 800.0) ** 2)) for a in amp]
+    gls = [np.exp(-abs(i - j) / 1.5) * np.sqrt(auto[i] * auto[j])
+           for i in range(nshell) for j in range(i, -1, -1)]
+    return gls, lam
+
+
+def _serving_requests(n: int, seed: int):
+    """Requests of the serving workload: nside uniform over {128, 256, 512,
+    1024}, lmax = 2 nside, 3-20 shells, per-request spectra seed."""
+    from glass_gb300 import serving
+
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for i in range(n):
+        nside = int(rng.choice([128, 256, 512, 1024]))
+        nshell = int(rng.integers(3, 21))
+        gls, lam = spectra_cfg2(nshell, 2 * nside, seed=seed * 100003 + i)
+        reqs.append(serving.Request(gls=gls, nside=nside, shifts=[float(x) for x in lam], seed=1000 + i))
+    return reqs
+
+
+def _serve(reqs, rate: float | None, form: str, batching: bool) -> dict:
+    """Serve `reqs` arriving as a Poisson stream of `rate` requests/s (all at
+    once when rate is None); finished maps are dropped as they complete."""
+    import torch
+
+    from glass_gb300 import serving
+
+    srv = serving.Server(hbm_budget=120 << 30, form=form, batching=batching)
+    gaps = np.random.default_rng(7).exponential(1.0 / rate, len(reqs)) if rate else np.zeros(len(reqs))
+    t0 = time.perf_counter() + 0.05
+    arrivals = t0 + np.cumsum(gaps)
+    for r, t in zip(reqs, arrivals):
+        r.arrival = float(t)
+        r.maps, r.finished, r.admitted = [], None, None
+
+    def feeder():
+        for r in reqs:
+            dt = r.arrival - time.perf_counter()
+            if dt > 0:
+                time.sleep(dt)
+            srv.submit(r)
+
+    th = threading.Thread(target=feeder, daemon=True)
+    th.start()
+    done = 0
+    while done < len(reqs):
+        srv.step()
+        while srv.finished:
+            r = srv.finished.pop()
+            r.maps = []  # the client has taken the maps
+            done += 1
+        if not srv.active:
+            time.sleep(0.0002)
+    th.join()
+    torch.cuda.synchronize()
+    lat = np.array([r.latency for r in reqs])
+    shells = sum(r.nshell for r in reqs)
+    span = max(r.finished for r in reqs) - min(r.arrival for r in reqs)
+    return {"requests": len(reqs), "p50_s": float(np.percentile(lat, 50)),
+            "p99_s": float(np.percentile(lat, 99)), "mean_s": float(lat.mean()),
+            "shell_maps_per_s": shells / span, "span_s": span,
+            "arrival_rate_per_s": rate, "form": form, "batching": batching}
+
+
+def run_serving(args) -> dict:
+    """Serving workload: calibrate capacity on a closed batch, then serve a
+    Poisson arrival stream at 70% of it; the FP64 form without batching on a
+    smaller sample for comparison."""
+    out = {}
+    for form, batching, n, ncal in (("fast", True, args.serving, min(200, args.serving)),
+                                    ("plain", False, args.serving_plain, min(20, args.serving_plain))):
+        if n <= 0:
+            continue
+        cal = _serve(_serving_requests(ncal, seed=91), None, form, batching)
+        cap = cal["requests"] / cal["span_s"]
+        res = _serve(_serving_requests(n, seed=3), 0.7 * cap, form, batching)
+        res["capacity_req_per_s"] = cap
+        out[f"{form}{'_batched' if batching else '_unbatched'}"] = res
+    return out
 
 
 class ClockSampler:
@@ -230,6 +325,7 @@ def run_ours(args, rank: int, world: int) -> dict | None:
                "h2d_bytes_per_step": int(sum(c.nbytes for c in gls_np)),
                "d2h_bytes_per_step": d2h}
 
+    serving = run_serving(args) if (args.serving > 0 or args.serving_plain > 0) else None
     cpu = cpu_baseline(args) if args.cpu_baseline else None
     res = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -241,7 +337,7 @@ def run_ours(args, rank: int, world: int) -> dict | None:
         "pixels_per_sec": value * npix, "e2e": e2e, "plain_fp64": plain, "roofline": roofline,
         "kernel_ms_per_step": {k: v[0] for k, v in kt.items()},
         "kernel_launches_per_step": {k: v[1] for k, v in kt.items()}, "gpu_launches": launches,
-        "clocks": clk.summary(), "cpu_baseline": cpu,
+        "clocks": clk.summary(), "cpu_baseline": cpu, "serving": serving,
     }
     return res
 
@@ -289,6 +385,23 @@ def run_reference(args, rank: int, world: int) -> dict | None:
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def ncu_case() -> None:
+    """Small profiling case (no JSON): two fast `generate` calls of 8
+    lognormal shells of the serving spectra at nside 1024, lmax 2048 (the
+    Legendre sums, 0.54 GB, exceed L2); profilers capture the first call."""
+    import torch
+
+    import glass_gb300 as g
+
+    gls, lam = spectra_cfg2(8, 2048, seed=1)
+    gls = [torch.as_tensor(c, device="cuda") for c in gls]
+    fields = [g.grf.Lognormal(float(x)) for x in lam]
+    for _ in range(2):
+        maps = list(g.generate(fields, gls, 1024, rng=g.rng.Generator(42), form="fast"))
+        torch.cuda.synchronize()
+    print("ncu case done", float(maps[0].abs().max()))
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
@@ -301,8 +414,15 @@ def main() -> None:
     ap.add_argument("--plain-steps", type=int, default=1)
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-shells", type=int, default=1)
+    ap.add_argument("--serving", type=int, default=2000, help="requests of the serving workload (0: off)")
+    ap.add_argument("--serving-plain", type=int, default=60,
+                    help="requests of the FP64 unbatched serving comparison (0: off)")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--ncu-case", action="store_true", help="run the small profiling case and exit")
     args = ap.parse_args()
+    if args.ncu_case:
+        ncu_case()
+        return
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -19,7 +19,9 @@
 // MMAs into one accumulator drifts by ~1e-8 per step: the groups of a unit
 // are therefore accumulated in chunks of CHUNK groups into two alternating
 // TMEM accumulator sets, and drain warps add every finished chunk into FP32
-// sums in shared memory (round to nearest).
+// sums in shared memory (round to nearest).  Within a chunk the small cross
+// terms of all its groups go first and the large A_hi B_hi terms last, so
+// the truncation never falls on a small term added to a large sum.
 //
 // Warp roles (608 threads): warps 0-11 produce lambda (three sets taking
 // every third group), warps 12-15 drain the accumulators and store F, warp 16
@@ -131,6 +133,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
     constexpr uint32_t SEED_TX = 128 * 8 + GLG_GROUP * 16;
     constexpr int A_COL0 = 4 * N;  // D sets at [0, 2N) and [2N, 4N)
     static_assert(A_COL0 + 32 * NST <= TMEM_COLS, "tensor memory budget");
+    static_assert(CHUNK <= NST, "a chunk holds all of its lambda stages until its last MMA");
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < NST; ++s) {
@@ -321,6 +324,11 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
                     fence_after_sync();
                     const uint32_t dE = tb + 2 * N * d, dO = dE + N;
                     const int gend = g + CHUNK < G ? g + CHUNK : G;
+                    constexpr uint32_t tsz = 32 * N;  // bytes of one B tile
+                    // The accumulator rounds toward zero: add every small
+                    // cross term (A_hi B_lo, A_lo B_hi) of the chunk first,
+                    // while D is still small, then the large A_hi B_hi terms,
+                    // so each group costs one truncation of the running sum.
                     for (int q = g; q < gend; ++q) {
                         const int64_t gg = gc + q;
                         const int s = (int)(gg % NST);
@@ -333,20 +341,27 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
                         fence_after_sync();
                         const uint32_t acol = tb + A_COL0 + 32 * s;
                         const uint32_t bb = smem_u32(S.st[sb].b);
-                        constexpr uint32_t tsz = 32 * N;  // bytes of one B tile
                         const uint64_t bEh = sdesc_noswz(bb, 128, 256), bEl = sdesc_noswz(bb + tsz, 128, 256);
                         const uint64_t bOh = sdesc_noswz(bb + 2 * tsz, 128, 256);
                         const uint64_t bOl = sdesc_noswz(bb + 3 * tsz, 128, 256);
                         const uint32_t acc = q > g ? 1u : 0u;
-                        mma_tf32_ts(dE, acol + 0, bEh, IDESC, acc);
-                        mma_tf32_ts(dE, acol + 0, bEl, IDESC, 1u);
+                        mma_tf32_ts(dE, acol + 0, bEl, IDESC, acc);
                         mma_tf32_ts(dE, acol + 8, bEh, IDESC, 1u);
-                        mma_tf32_ts(dO, acol + 16, bOh, IDESC, acc);
-                        mma_tf32_ts(dO, acol + 16, bOl, IDESC, 1u);
+                        mma_tf32_ts(dO, acol + 16, bOl, IDESC, acc);
                         mma_tf32_ts(dO, acol + 24, bOh, IDESC, 1u);
+                        issued = true;
+                    }
+                    if (!ok) break;
+                    for (int q = g; q < gend; ++q) {
+                        const int64_t gg = gc + q;
+                        const int s = (int)(gg % NST);
+                        const int sb = (int)(gg % Smem<N>::NB);
+                        const uint32_t acol = tb + A_COL0 + 32 * s;
+                        const uint32_t bb = smem_u32(S.st[sb].b);
+                        mma_tf32_ts(dE, acol + 0, sdesc_noswz(bb, 128, 256), IDESC, 1u);
+                        mma_tf32_ts(dO, acol + 16, sdesc_noswz(bb + 2 * tsz, 128, 256), IDESC, 1u);
                         mma_commit(&S.empty[s]);
                         mma_commit(&S.bempty[sb]);
-                        issued = true;
                     }
                     if (ok) mma_commit(&S.full_d[d]);
                 }

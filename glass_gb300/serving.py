@@ -63,11 +63,13 @@ class Request:
         return None if self.finished is None else self.finished - self.arrival
 
 
-def request_bytes(nside: int, lmax: int, nshell: int) -> int:
-    """Device bytes a request holds: alm (complex64), maps (float32), w/cov."""
+def request_bytes(nside: int, lmax: int, nshell: int, form: str = "fast") -> int:
+    """Device bytes a request holds: alm, maps and w/cov (twice as many alm
+    and map bytes in the FP64 form)."""
     nalm = (lmax + 1) * (lmax + 2) // 2
     npix = 12 * nside * nside
-    return nshell * (8 * nalm + 4 * npix) + 2 * 8 * nshell * (lmax + 1) * nshell
+    f = 2 if form == "plain" else 1
+    return nshell * f * (8 * nalm + 4 * npix) + 2 * 8 * nshell * (lmax + 1) * nshell
 
 
 def launch_bytes(nside: int, lmax: int, nmaps: int) -> int:
@@ -81,12 +83,12 @@ def launch_bytes(nside: int, lmax: int, nmaps: int) -> int:
 class _Active:
     """Per-request state while it is being served."""
 
-    def __init__(self, req: Request, device: torch.device):
+    def __init__(self, req: Request, device: torch.device, form: str = "fast"):
         self.req = req
         fields = [grf.Lognormal(float(s)) for s in req.shifts]
         self.kinds = [_lib.EPI_LOGNORMAL] * req.nshell
         self.lam = [f.lamda for f in fields]
-        self.batcher = _FieldBatcher(req.gls, req.nside, req.ncorr, Generator(req.seed), "fast",
+        self.batcher = _FieldBatcher(req.gls, req.nside, req.ncorr, Generator(req.seed), form,
                                      device=device)
         if self.batcher.bad >= 0:
             raise ValueError(f"request {req.id}: {self.batcher.bad_msg}")
@@ -98,13 +100,22 @@ class _Active:
 
 
 class Server:
-    """Continuous batching of simulation requests within an HBM budget."""
+    """Continuous batching of simulation requests within an HBM budget.
+
+    ``form="fast"`` with ``batching=True`` is the serving configuration;
+    ``form="plain", batching=False`` (one map per transform launch, no
+    sharing across requests) is the comparison point of the FP64 form.
+    """
 
     def __init__(self, hbm_budget: int = 120 << 30, max_maps_per_launch: int = 40,
-                 device: torch.device | None = None):
+                 device: torch.device | None = None, form: str = "fast", batching: bool = True):
+        if form not in ("fast", "plain"):
+            raise ValueError(f"form must be 'plain' or 'fast', not {form!r}")
         self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else device
         self.budget = int(hbm_budget)
-        self.max_maps = int(max_maps_per_launch)
+        self.form = form
+        self.batching = bool(batching)
+        self.max_maps = int(max_maps_per_launch) if batching else 1
         self.used = 0
         self.queue: collections.deque[Request] = collections.deque()
         self.active: list[_Active] = []
@@ -121,7 +132,7 @@ class Server:
             self._next_id += 1
             if req.arrival == 0.0:
                 req.arrival = time.perf_counter()
-            need = request_bytes(req.nside, req.lmax, req.nshell)
+            need = request_bytes(req.nside, req.lmax, req.nshell, self.form)
             if need > self.budget:
                 raise MemoryError(f"request {req.id} needs {need} bytes, over the HBM budget {self.budget}")
             self.queue.append(req)
@@ -130,7 +141,7 @@ class Server:
     def _admit(self) -> None:
         while self.queue:
             req = self.queue[0]
-            need = request_bytes(req.nside, req.lmax, req.nshell)
+            need = request_bytes(req.nside, req.lmax, req.nshell, self.form)
             if self.used + need > self.budget:
                 break
             self.queue.popleft()
@@ -139,7 +150,7 @@ class Server:
             req.admitted = time.perf_counter()
             stream = self._stream(req.nside, req.lmax)
             with torch.cuda.stream(stream):
-                self.active.append(_Active(req, self.device))
+                self.active.append(_Active(req, self.device, self.form))
 
     def _stream(self, nside: int, lmax: int) -> torch.cuda.Stream:
         key = (nside, lmax)
@@ -151,12 +162,14 @@ class Server:
 
     def _launch_batches(self) -> bool:
         """One launch per (nside, lmax) group from the shells ready now."""
-        groups: dict[tuple[int, int], list[tuple[_Active, int]]] = collections.defaultdict(list)
+        groups: dict[tuple, list[tuple[_Active, int]]] = collections.defaultdict(list)
         for a in self.active:
+            key = (a.req.nside, a.req.lmax) if self.batching else (a.req.nside, a.req.lmax, a.req.id)
             for s in range(a.next_shell, a.req.nshell):
-                groups[(a.req.nside, a.req.lmax)].append((a, s))
+                groups[key].append((a, s))
         launched = False
-        for (nside, lmax), items in groups.items():
+        for key, items in groups.items():
+            nside, lmax = key[0], key[1]
             stream = self._stream(nside, lmax)
             for c0 in range(0, len(items), self.max_maps):
                 chunk = items[c0:c0 + self.max_maps]
@@ -164,7 +177,7 @@ class Server:
                     alm = torch.stack([a.alm[s] for a, s in chunk])
                     epi = ([a.kinds[s] for a, s in chunk], [a.var[s] for a, s in chunk],
                            [a.lam[s] for a, s in chunk])
-                    maps = hp.synth(alm, nside, lmax, epilogue=epi, form="fast")
+                    maps = hp.synth(alm, nside, lmax, epilogue=epi, form=self.form)
                 for k, (a, s) in enumerate(chunk):
                     a.maps[s] = maps[k]
                     a.next_shell = max(a.next_shell, s + 1)
