@@ -14,21 +14,27 @@
 // memory as the MMA's A operand.  B (the alm, split the same way), the
 // group's seeds and its recurrence coefficients are streamed into shared
 // memory with 1-D bulk copies.  Each group issues, per parity,
-//   D += A_hi B_hi + A_hi B_lo + A_lo B_hi     (M = 128, N = 2 * maps, K = 8).
-// The tensor core's FP32 accumulation rounds toward zero, so a long chain of
-// MMAs into one accumulator drifts by ~1e-8 per step: the groups of a unit
-// are therefore accumulated in chunks of CHUNK groups into two alternating
-// TMEM accumulator sets, and drain warps add every finished chunk into FP32
-// sums in shared memory (round to nearest).  Within a chunk the small cross
-// terms of all its groups go first and the large A_hi B_hi terms last, so
-// the truncation never falls on a small term added to a large sum.
+//   D += A_hi B_lo + A_lo B_hi + A_hi B_hi     (M = 128, N = 2 * maps, K = 8).
 //
-// Warp roles (608 threads): warps 0-11 produce lambda (three sets taking
-// every third group), warps 12-15 drain the accumulators and store F, warp 16
-// issues the MMAs, warp 17 streams B through NB stages and warp 18 streams
-// seeds / coefficients through a deeper ring of NSEED slots.  Every wait is
-// bounded; on time-out the kernel records GLG_ERR_TIMEOUT in *err, retires
-// its outstanding MMAs and copies, frees its tensor memory and returns.
+// Pipeline.  The groups of a (tile, m) unit are processed in chunks of
+// CH = 3 groups, one per producer warp set; a chunk is the unit of every
+// hand-off: its lambda goes to one of two TMEM chunk slots, its B tiles come
+// in one bulk copy into one of NBC shared-memory chunk slots, its MMAs
+// accumulate into one of two TMEM accumulator sets, and one commit per chunk
+// both frees the lambda slot and hands the accumulator to the drain warps,
+// which add it into FP32 sums in shared memory (round to nearest).  The
+// tensor core's FP32 accumulation rounds toward zero, so accumulating only a
+// chunk in TMEM bounds that drift, and within a chunk the small cross terms
+// of its groups go first and the large A_hi B_hi terms last, so the
+// truncation never falls on a small term added to a large sum.
+//
+// Warp roles (608 threads): warps 0-11 produce lambda (set k = warps
+// 4k..4k+3 makes group k of every chunk), warps 12-15 drain the
+// accumulators and store F, warp 16 issues the MMAs, warp 17 streams B and
+// warp 18 streams seeds / coefficients through a ring of NSEED group slots.
+// Every wait is bounded; on time-out the kernel records GLG_ERR_TIMEOUT in
+// *err, retires its outstanding MMAs and copies, frees its tensor memory and
+// returns.
 #include <cuda_runtime.h>
 
 #include "glg_internal.cuh"
@@ -38,17 +44,13 @@ using namespace glg_tc;
 
 namespace {
 
-constexpr int NST = 6;            // lambda stages in tensor memory (A operands)
-constexpr int NSETS = 3;          // producer warp sets
-#ifndef GLG_TC_CHUNK
-#define GLG_TC_CHUNK 4
-#endif
-constexpr int CHUNK = GLG_TC_CHUNK;  // groups accumulated per TMEM accumulator fill
-constexpr int NSEED = 16;         // slots of the seed / coefficient ring
+constexpr int CH = 3;             // groups per chunk = producer warp sets
+constexpr int NSEED = 16;         // slots of the seed / coefficient ring (groups)
 constexpr int TMEM_COLS = 512;
 constexpr int THREADS = 19 * 32;
 constexpr uint32_t WAIT_LIMIT = 1u << 22;
 constexpr int W_DRAIN = 12, W_MMA = 16, W_LOAD = 17, W_SEED = 18;
+static_assert(W_DRAIN == 4 * CH, "one producer warp set per group of a chunk");
 static_assert((W_SEED + 1) * 32 == THREADS, "one warp per role after the producers and drains");
 
 struct LegTcArgs {
@@ -95,31 +97,32 @@ __device__ __forceinline__ int unit_m(int64_t mi, int lmax) {
     return (mi & 1) ? lmax - (int)(mi >> 1) : (int)(mi >> 1);
 }
 
-// B stages in shared memory: as many as fit beside the accumulators and the
-// seed ring (up to 16), so that the alm of a group are requested well before
-// the MMA that reads them.
+// B chunk slots in shared memory: as many as fit beside the accumulators and
+// the seed ring (up to 6), so the alm of a chunk are requested several chunks
+// before the MMAs that read them.
 template <int N>
-constexpr int nb_stages() {
-    constexpr int room = (220 * 1024 - 1024 * N - NSEED * 1280 - 1024) / (128 * N);
-    return room > 16 ? 16 : room;
+constexpr int nbc_slots() {
+    constexpr int room = (226 * 1024 - 1024 * N - NSEED * 1280 - 1024) / (CH * 128 * N);
+    return room > 6 ? 6 : room;
 }
 
 template <int N>
 struct Smem {
-    static constexpr uint32_t BBYTES = 128 * N;  // 4 tiles of N x 8 tf32
-    static constexpr int NB = nb_stages<N>();
-    static_assert(NB >= NST, "B ring shallower than the lambda stages");
-    struct Stage {
-        unsigned char b[BBYTES];
-    } st[NB];
+    static constexpr uint32_t BBYTES = 128 * N;  // one group: 4 tiles of N x 8 tf32
+    static constexpr int NBC = nbc_slots<N>();
+    static_assert(NBC >= 2, "at least two B chunk slots");
+    struct BSlot {
+        unsigned char b[CH * BBYTES];
+    } bs[NBC];
     struct SeedSlot {
         float2 seed[128];        // seeds of the group's 128 ring pairs
         float4 coef[GLG_GROUP];  // (A_hi, A_lo, B_hi, B_lo) of l = l0 .. l0+15
     } sd[NSEED];
     float acc[2 * N][128];     // FP32 sums of drained chunks, [column][lane]
-    uint64_t full_a[NST], empty[NST], full_b[NB], bempty[NB];
+    uint64_t full_a[2], cdone[2], empty_d[2];
+    uint64_t full_b[NBC], bempty[NBC];
     uint64_t sfull[NSEED], sempty[NSEED];
-    uint64_t full_d[2], empty_d[2], drain;
+    uint64_t drain;
     uint32_t tmem_base;
     int abort;
 };
@@ -128,29 +131,28 @@ template <int N>
 __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     Smem<N> &S = *reinterpret_cast<Smem<N> *>(smem_raw);
+    constexpr int NBC = Smem<N>::NBC;
+    constexpr uint32_t BBYTES = Smem<N>::BBYTES;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     constexpr uint32_t IDESC = idesc_tf32(128, N);
     constexpr uint32_t SEED_TX = 128 * 8 + GLG_GROUP * 16;
-    constexpr int A_COL0 = 4 * N;  // D sets at [0, 2N) and [2N, 4N)
-    static_assert(A_COL0 + 32 * NST <= TMEM_COLS, "tensor memory budget");
-    static_assert(CHUNK <= NST, "a chunk holds all of its lambda stages until its last MMA");
+    constexpr int A_COL0 = 4 * N;     // D sets at [0, 2N) and [2N, 4N)
+    constexpr int A_SLOT = CH * 32;   // columns of one lambda chunk slot
+    static_assert(A_COL0 + 2 * A_SLOT <= TMEM_COLS, "tensor memory budget");
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < NST; ++s) {
-            mbar_init(&S.full_a[s], 4);
-            mbar_init(&S.empty[s], 1);
+        for (int k = 0; k < 2; ++k) {
+            mbar_init(&S.full_a[k], 4 * CH);  // every producer warp, once per chunk
+            mbar_init(&S.cdone[k], 1);        // the chunk's commit
+            mbar_init(&S.empty_d[k], 4);      // the drain warps
         }
-        for (int s = 0; s < Smem<N>::NB; ++s) {
-            mbar_init(&S.full_b[s], 1);
-            mbar_init(&S.bempty[s], 1);
+        for (int k = 0; k < NBC; ++k) {
+            mbar_init(&S.full_b[k], 1);
+            mbar_init(&S.bempty[k], 1);
         }
         for (int q = 0; q < NSEED; ++q) {
             mbar_init(&S.sfull[q], 1);
             mbar_init(&S.sempty[q], 4);
-        }
-        for (int d = 0; d < 2; ++d) {
-            mbar_init(&S.full_d[d], 1);
-            mbar_init(&S.empty_d[d], 4);
         }
         mbar_init(&S.drain, 1);
         S.abort = 0;
@@ -182,10 +184,14 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
     const uint32_t lane_base = (uint32_t)((warp & 3) << 5) << 16;
     const int r = ((warp & 3) << 5) + lane;  // TMEM lane = ring pair in tile
 
+    // Chunk cc (counted over the CTA's units) uses lambda slot and
+    // accumulator set cc & 1 (phase cc >> 1 of their barriers) and B slot
+    // cc % NBC (phase cc / NBC); group gg (counted likewise) uses seed slot
+    // gg % NSEED (phase gg / NSEED).
     if (warp < W_DRAIN) {
         // ------------------------------------------------ lambda producers
         const int set = warp >> 2;
-        int64_t gc = 0;
+        uint32_t cc = 0, gc = 0;
         bool ok = true;
         for (int64_t u = blockIdx.x; u < a.nunits && ok; u += gridDim.x) {
             const int tile = (int)(u % a.ntiles);
@@ -196,92 +202,94 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
             const int pp = live ? p : a.npairs - 1;
             const float2 x = a.cth32[pp];
             const int ls = live ? a.lstart[(int64_t)m * a.npairs + pp] : lmax + 1;
-            for (int g = (int)((set - gc % NSETS + NSETS) % NSETS); g < G; g += NSETS) {
-                const int64_t gg = gc + g;
-                const int s = (int)(gg % NST);
-                const uint32_t par = (uint32_t)((gg / NST) & 1);
-                const int q = (int)(gg % NSEED);
-                if (!wait(&S.sfull[q], (uint32_t)((gg / NSEED) & 1))) { ok = false; break; }
-                if (gg >= NST && !wait(&S.empty[s], par ^ 1u)) { ok = false; break; }
-                fence_after_sync();
-                const typename Smem<N>::SeedSlot &sd = S.sd[q];
-                const int l0 = m + g * GLG_GROUP;
-                const int s0 = l0 > ls ? l0 : ls;
-                const float2 seed = sd.seed[r];
-                float lm2 = 0.f, lm1 = 0.f;
-                uint32_t ehi[8], elo[8], ohi[8], olo[8];
-                // every lane starts at l0 and the group ends inside lmax: no per-step tests
-                const bool regular = __all_sync(0xffffffffu, s0 == l0) && l0 + GLG_GROUP - 1 <= lmax;
-                if (regular) {
+            for (int g0 = 0; g0 < G; g0 += CH, ++cc) {
+                const uint32_t slot = cc & 1u;
+                // lambda slot free: chunk cc - 2 has retired
+                if (cc >= 2 && !wait(&S.cdone[slot], ((cc >> 1) - 1) & 1u)) { ok = false; break; }
+                const int g = g0 + set;
+                if (g < G) {
+                    const uint32_t gg = gc + (uint32_t)g;
+                    const int q = (int)(gg % NSEED);
+                    if (!wait(&S.sfull[q], (gg / NSEED) & 1u)) { ok = false; break; }
+                    fence_after_sync();
+                    const typename Smem<N>::SeedSlot &sd = S.sd[q];
+                    const int l0 = m + g * GLG_GROUP;
+                    const int s0 = l0 > ls ? l0 : ls;
+                    const float2 seed = sd.seed[r];
+                    float lm2 = 0.f, lm1 = 0.f;
+                    uint32_t ehi[8], elo[8], ohi[8], olo[8];
+                    // every lane starts at l0 and the group ends inside lmax: no per-step tests
+                    const bool regular = __all_sync(0xffffffffu, s0 == l0) && l0 + GLG_GROUP - 1 <= lmax;
+                    if (regular) {
 #pragma unroll
-                    for (int j = 0; j < GLG_GROUP; ++j) {
-                        const float v = j == 0 ? seed.x : j == 1 ? seed.y : rec_step_comp(sd.coef[j], x, lm1, lm2);
-                        lm2 = lm1;
-                        lm1 = v;
-                        const uint32_t hi = tf32_rna(v);
-                        const uint32_t lo = tf32_rna(v - __uint_as_float(hi));
-                        if (j & 1) {
-                            ohi[j >> 1] = hi;
-                            olo[j >> 1] = lo;
-                        } else {
-                            ehi[j >> 1] = hi;
-                            elo[j >> 1] = lo;
+                        for (int j = 0; j < GLG_GROUP; ++j) {
+                            const float v = j == 0 ? seed.x : j == 1 ? seed.y : rec_step_comp(sd.coef[j], x, lm1, lm2);
+                            lm2 = lm1;
+                            lm1 = v;
+                            const uint32_t hi = tf32_rna(v);
+                            const uint32_t lo = tf32_rna(v - __uint_as_float(hi));
+                            if (j & 1) {
+                                ohi[j >> 1] = hi;
+                                olo[j >> 1] = lo;
+                            } else {
+                                ehi[j >> 1] = hi;
+                                elo[j >> 1] = lo;
+                            }
+                        }
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < GLG_GROUP; ++j) {
+                            const int l = l0 + j;
+                            float v;
+                            if (l < s0 || l > lmax) {
+                                v = 0.f;
+                            } else if (l == s0) {
+                                v = seed.x;
+                            } else if (l == s0 + 1) {
+                                v = seed.y;
+                            } else {
+                                v = rec_step_comp(sd.coef[j], x, lm1, lm2);
+                            }
+                            lm2 = lm1;
+                            lm1 = v;
+                            const uint32_t hi = tf32_rna(v);
+                            const uint32_t lo = tf32_rna(v - __uint_as_float(hi));
+                            if (j & 1) {
+                                ohi[j >> 1] = hi;
+                                olo[j >> 1] = lo;
+                            } else {
+                                ehi[j >> 1] = hi;
+                                elo[j >> 1] = lo;
+                            }
                         }
                     }
-                } else {
-#pragma unroll
-                    for (int j = 0; j < GLG_GROUP; ++j) {
-                        const int l = l0 + j;
-                        float v;
-                        if (l < s0 || l > lmax) {
-                            v = 0.f;
-                        } else if (l == s0) {
-                            v = seed.x;
-                        } else if (l == s0 + 1) {
-                            v = seed.y;
-                        } else {
-                            v = rec_step_comp(sd.coef[j], x, lm1, lm2);
-                        }
-                        lm2 = lm1;
-                        lm1 = v;
-                        const uint32_t hi = tf32_rna(v);
-                        const uint32_t lo = tf32_rna(v - __uint_as_float(hi));
-                        if (j & 1) {
-                            ohi[j >> 1] = hi;
-                            olo[j >> 1] = lo;
-                        } else {
-                            ehi[j >> 1] = hi;
-                            elo[j >> 1] = lo;
-                        }
-                    }
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(&S.sempty[q]);  // seed slot read
+                    const uint32_t col = tb + lane_base + A_COL0 + slot * A_SLOT + 32 * set;
+                    tmem_st8(col + 0, ehi);
+                    tmem_st8(col + 8, elo);
+                    tmem_st8(col + 16, ohi);
+                    tmem_st8(col + 24, olo);
+                    tmem_wait_st();
                 }
-                __syncwarp();
-                if (lane == 0) mbar_arrive(&S.sempty[q]);  // slot read: the seed loader may refill it
-                const uint32_t col = tb + lane_base + A_COL0 + 32 * s;
-                tmem_st8(col + 0, ehi);
-                tmem_st8(col + 8, elo);
-                tmem_st8(col + 16, ohi);
-                tmem_st8(col + 24, olo);
-                tmem_wait_st();
                 fence_before_sync();
                 __syncwarp();
-                if (lane == 0) mbar_arrive(&S.full_a[s]);
+                if (lane == 0) mbar_arrive(&S.full_a[slot]);  // every set arrives, active or not
             }
-            gc += G;
+            gc += (uint32_t)G;
         }
         if (!ok) fail();
     } else if (warp < W_MMA) {
         // --------------------------------- drain: chunk sums -> smem -> F
-        int64_t cc = 0;  // chunk counter across units
+        uint32_t cc = 0;
         bool ok = true;
         for (int64_t u = blockIdx.x; u < a.nunits && ok; u += gridDim.x) {
             const int tile = (int)(u % a.ntiles);
             const int m = unit_m(u / a.ntiles, lmax);
             const int G = (lmax - m + GLG_GROUP) / GLG_GROUP;
-            const int nch = (G + CHUNK - 1) / CHUNK;
-            for (int c = 0; c < nch; ++c, ++cc) {
-                const int d = (int)(cc & 1);
-                if (!wait(&S.full_d[d], (uint32_t)((cc >> 1) & 1))) { ok = false; break; }
+            for (int g0 = 0; g0 < G; g0 += CH, ++cc) {
+                const uint32_t d = cc & 1u;
+                if (!wait(&S.cdone[d], (cc >> 1) & 1u)) { ok = false; break; }
                 fence_after_sync();
                 for (int c0 = 0; c0 < 2 * N; c0 += 16) {
                     uint32_t v[16];
@@ -313,59 +321,42 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
     } else if (warp == W_MMA) {
         // ---------------------------------------------------------- MMA issue
         if (lane == 0) {
-            int64_t gc = 0, cc = 0;
+            uint32_t cc = 0;
             bool ok = true, issued = false;
             for (int64_t u = blockIdx.x; u < a.nunits && ok; u += gridDim.x) {
                 const int m = unit_m(u / a.ntiles, lmax);
                 const int G = (lmax - m + GLG_GROUP) / GLG_GROUP;
-                for (int g = 0; g < G && ok; g += CHUNK, ++cc) {
-                    const int d = (int)(cc & 1);
-                    if (cc >= 2 && !wait(&S.empty_d[d], (uint32_t)(((cc >> 1) - 1) & 1))) { ok = false; break; }
-                    fence_after_sync();
-                    const uint32_t dE = tb + 2 * N * d, dO = dE + N;
-                    const int gend = g + CHUNK < G ? g + CHUNK : G;
-                    constexpr uint32_t tsz = 32 * N;  // bytes of one B tile
-                    // The accumulator rounds toward zero: add every small
-                    // cross term (A_hi B_lo, A_lo B_hi) of the chunk first,
-                    // while D is still small, then the large A_hi B_hi terms,
-                    // so each group costs one truncation of the running sum.
-                    for (int q = g; q < gend; ++q) {
-                        const int64_t gg = gc + q;
-                        const int s = (int)(gg % NST);
-                        const int sb = (int)(gg % Smem<N>::NB);
-                        if (!wait(&S.full_b[sb], (uint32_t)((gg / Smem<N>::NB) & 1)) ||
-                            !wait(&S.full_a[s], (uint32_t)((gg / NST) & 1))) {
-                            ok = false;
-                            break;
-                        }
-                        fence_after_sync();
-                        const uint32_t acol = tb + A_COL0 + 32 * s;
-                        const uint32_t bb = smem_u32(S.st[sb].b);
-                        const uint64_t bEh = sdesc_noswz(bb, 128, 256), bEl = sdesc_noswz(bb + tsz, 128, 256);
-                        const uint64_t bOh = sdesc_noswz(bb + 2 * tsz, 128, 256);
-                        const uint64_t bOl = sdesc_noswz(bb + 3 * tsz, 128, 256);
-                        const uint32_t acc = q > g ? 1u : 0u;
-                        mma_tf32_ts(dE, acol + 0, bEl, IDESC, acc);
-                        mma_tf32_ts(dE, acol + 8, bEh, IDESC, 1u);
-                        mma_tf32_ts(dO, acol + 16, bOl, IDESC, acc);
-                        mma_tf32_ts(dO, acol + 24, bOh, IDESC, 1u);
-                        issued = true;
+                for (int g0 = 0; g0 < G; g0 += CH, ++cc) {
+                    const uint32_t k = cc & 1u, bsl = cc % NBC;
+                    if (cc >= 2 && !wait(&S.empty_d[k], ((cc >> 1) - 1) & 1u)) { ok = false; break; }
+                    if (!wait(&S.full_b[bsl], (cc / NBC) & 1u) || !wait(&S.full_a[k], (cc >> 1) & 1u)) {
+                        ok = false;
+                        break;
                     }
-                    if (!ok) break;
-                    for (int q = g; q < gend; ++q) {
-                        const int64_t gg = gc + q;
-                        const int s = (int)(gg % NST);
-                        const int sb = (int)(gg % Smem<N>::NB);
-                        const uint32_t acol = tb + A_COL0 + 32 * s;
-                        const uint32_t bb = smem_u32(S.st[sb].b);
+                    fence_after_sync();
+                    const int ng = G - g0 < CH ? G - g0 : CH;
+                    const uint32_t dE = tb + 2 * N * k, dO = dE + N;
+                    const uint32_t a0 = tb + A_COL0 + k * A_SLOT;
+                    const uint32_t b0 = smem_u32(S.bs[bsl].b);
+                    constexpr uint32_t tsz = 32 * N;  // bytes of one B tile
+                    // small cross terms of every group first, E and O alternating
+                    for (int q = 0; q < ng; ++q) {
+                        const uint32_t acol = a0 + 32 * q, bb = b0 + q * BBYTES;
+                        const uint32_t acc = q > 0 ? 1u : 0u;
+                        mma_tf32_ts(dE, acol + 0, sdesc_noswz(bb + tsz, 128, 256), IDESC, acc);
+                        mma_tf32_ts(dO, acol + 16, sdesc_noswz(bb + 3 * tsz, 128, 256), IDESC, acc);
+                        mma_tf32_ts(dE, acol + 8, sdesc_noswz(bb, 128, 256), IDESC, 1u);
+                        mma_tf32_ts(dO, acol + 24, sdesc_noswz(bb + 2 * tsz, 128, 256), IDESC, 1u);
+                    }
+                    for (int q = 0; q < ng; ++q) {
+                        const uint32_t acol = a0 + 32 * q, bb = b0 + q * BBYTES;
                         mma_tf32_ts(dE, acol + 0, sdesc_noswz(bb, 128, 256), IDESC, 1u);
                         mma_tf32_ts(dO, acol + 16, sdesc_noswz(bb + 2 * tsz, 128, 256), IDESC, 1u);
-                        mma_commit(&S.empty[s]);
-                        mma_commit(&S.bempty[sb]);
                     }
-                    if (ok) mma_commit(&S.full_d[d]);
+                    issued = true;
+                    mma_commit(&S.cdone[k]);   // lambda slot free, accumulator ready
+                    mma_commit(&S.bempty[bsl]);
                 }
-                gc += G;
             }
             if (!ok) fail();
             if (issued) {  // every MMA of this CTA retired before TMEM is freed
@@ -378,40 +369,35 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
     } else if (warp == W_LOAD) {
         // ------------------------------------------------------- B streaming
         if (lane == 0) {
-            int64_t gc = 0;
+            uint32_t cc = 0;
             bool ok = true;
-            constexpr int NB = Smem<N>::NB;
-            int64_t last_use[NB];
-            for (int s = 0; s < NB; ++s) last_use[s] = -1;
+            int64_t last_use[NBC];
+            for (int k = 0; k < NBC; ++k) last_use[k] = -1;
             for (int64_t u = blockIdx.x; u < a.nunits && ok; u += gridDim.x) {
                 const int m = unit_m(u / a.ntiles, lmax);
                 const int G = (lmax - m + GLG_GROUP) / GLG_GROUP;
                 const int64_t gb = a.goff[m];
-                for (int g = 0; g < G; ++g) {
-                    const int64_t gg = gc + g;
-                    const int s = (int)(gg % NB);
-                    const int64_t use = gg / NB;
-                    if (use > 0 && !wait(&S.bempty[s], (uint32_t)((use - 1) & 1))) { ok = false; break; }
-                    mbar_arrive_expect_tx(&S.full_b[s], Smem<N>::BBYTES);
-                    bulk_g2s(S.st[s].b, a.bpack + (size_t)(gb + g) * Smem<N>::BBYTES, Smem<N>::BBYTES, &S.full_b[s]);
-                    last_use[s] = use;
+                for (int g0 = 0; g0 < G; g0 += CH, ++cc) {
+                    const uint32_t bsl = cc % NBC, use = cc / NBC;
+                    if (use > 0 && !wait(&S.bempty[bsl], (use - 1) & 1u)) { ok = false; break; }
+                    const int ng = G - g0 < CH ? G - g0 : CH;
+                    mbar_arrive_expect_tx(&S.full_b[bsl], ng * BBYTES);
+                    bulk_g2s(S.bs[bsl].b, a.bpack + (size_t)(gb + g0) * BBYTES, ng * BBYTES, &S.full_b[bsl]);
+                    last_use[bsl] = use;
                 }
-                gc += G;
             }
             if (!ok) fail();
             // outstanding copies land before the CTA exits
-            for (int s = 0; s < NB; ++s)
-                if (last_use[s] >= 0)
-                    for (uint32_t i = 0; i < WAIT_LIMIT && !mbar_try_wait(&S.full_b[s], (uint32_t)(last_use[s] & 1)); ++i) {
+            for (int k = 0; k < NBC; ++k)
+                if (last_use[k] >= 0)
+                    for (uint32_t i = 0; i < WAIT_LIMIT && !mbar_try_wait(&S.full_b[k], (uint32_t)(last_use[k] & 1)); ++i) {
                     }
         }
         __syncwarp();
     } else {
         // ----------------------------------- seed / coefficient streaming
-        // A deeper ring than the B stages, so that a producer set finds the
-        // seeds of its next group already resident when it finishes one.
         if (lane == 0) {
-            int64_t gc = 0;
+            uint32_t gc = 0;
             bool ok = true;
             int64_t last_use[NSEED];
             for (int q = 0; q < NSEED; ++q) last_use[q] = -1;
@@ -422,17 +408,17 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
                 const int64_t gb = a.goff[m];
                 const int64_t cb = a.mofs[m];
                 for (int g = 0; g < G; ++g) {
-                    const int64_t gg = gc + g;
+                    const uint32_t gg = gc + (uint32_t)g;
                     const int q = (int)(gg % NSEED);
-                    const int64_t use = gg / NSEED;
-                    if (use > 0 && !wait(&S.sempty[q], (uint32_t)((use - 1) & 1))) { ok = false; break; }
+                    const uint32_t use = gg / NSEED;
+                    if (use > 0 && !wait(&S.sempty[q], (use - 1) & 1u)) { ok = false; break; }
                     typename Smem<N>::SeedSlot &sd = S.sd[q];
                     mbar_arrive_expect_tx(&S.sfull[q], SEED_TX);
                     bulk_g2s(sd.seed, a.seeds + (gb + g) * a.seed_stride + (int64_t)tile * 128, 128 * 8, &S.sfull[q]);
                     bulk_g2s(sd.coef, a.coef32 + cb + (int64_t)g * GLG_GROUP, GLG_GROUP * 16, &S.sfull[q]);
                     last_use[q] = use;
                 }
-                gc += G;
+                gc += (uint32_t)G;
             }
             if (!ok) fail();
             for (int q = 0; q < NSEED; ++q)
