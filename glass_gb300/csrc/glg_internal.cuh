@@ -92,6 +92,7 @@ struct glg_plan {
     float2 *seeds;           // [ngroups][seed_stride] (lambda_s0, lambda_s0+1) per group
     int64_t seed_stride;     // npairs rounded up to whole 128-pair tiles
     int *lstart;             // [mmax+1][npairs] first l with |lambda| >= 2^-100
+    int *tfirst;             // [mmax+1][ntiles] first group with a lambda >= 2^-100 in the tile
 
     // FP32 ring FFTs of the fast form.  Class 0: ring lengths whose prime
     // factors are all <= 13 (mixed-radix DIF, output order from pos16).
@@ -134,7 +135,7 @@ __host__ __device__ inline int glg_zi(int e) { return e + (e >> 4); }
 // Dynamic shared memory of one ring FFT block: the padded transform buffer
 // of length n (kind 0) or M (kind 1), a second padded buffer for the south
 // ring's fold (kind 0 with n <= mmax), 2 x threads partial sums and the half
-// twiddle table.
+// twiddle table (padded like the buffers).
 size_t glg_ring32_smem(int kind, int n_or_M, int threads, bool fold);
 
 // l values per group of the fast Legendre contraction (8 even + 8 odd)

@@ -16,6 +16,10 @@
 // memory with 1-D bulk copies.  Each group issues, per parity,
 //   D += A_hi B_lo + A_lo B_hi + A_hi B_hi     (M = 128, N = 2 * maps, K = 8).
 //
+// Groups before the first one where some ring of the tile has |lambda| >=
+// 2^-100 are zero on the whole tile and are skipped (the dense algorithmic
+// count is still the one reported).
+//
 // Pipeline.  The groups of a (tile, m) unit are processed in chunks of
 // CH = 3 groups, one per producer warp set; a chunk is the unit of every
 // hand-off: its lambda goes to one of two TMEM chunk slots, its B tiles come
@@ -63,6 +67,7 @@ struct LegTcArgs {
     const float2 *seeds;
     int64_t seed_stride;
     const int *lstart;
+    const int *tfirst;  // [m][tile] first group holding a lambda >= 2^-100
     const unsigned char *bpack;
     float2 *F;  // [map][m][ring]
     int *err;
@@ -79,7 +84,7 @@ __device__ __forceinline__ uint32_t tf32_rna(float x) {
 // transformations with fma): only the FP32 state itself is rounded, which
 // keeps the 16-step runs between FP64 seeds near 1e-7.  The __f*_rn forms
 // keep the compiler from fusing the rounded products away.
-__device__ __forceinline__ float rec_step_comp(const float4 c, const float2 x, float lm1, float lm2) {
+__device__ __forceinline__ float rec_step(const float4 c, const float2 x, float lm1, float lm2) {
     const float yh = __fmul_rn(x.x, lm1);
     float ye = fmaf(x.x, lm1, -yh);
     ye = fmaf(x.y, lm1, ye);
@@ -102,7 +107,7 @@ __device__ __forceinline__ int unit_m(int64_t mi, int lmax) {
 // before the MMAs that read them.
 template <int N>
 constexpr int nbc_slots() {
-    constexpr int room = (226 * 1024 - 1024 * N - NSEED * 1280 - 1024) / (CH * 128 * N);
+    constexpr int room = (226 * 1024 - 512 * (2 * N + 4) - NSEED * 1280 - 1024) / (CH * 128 * N);
     return room > 6 ? 6 : room;
 }
 
@@ -118,7 +123,8 @@ struct Smem {
         float2 seed[128];        // seeds of the group's 128 ring pairs
         float4 coef[GLG_GROUP];  // (A_hi, A_lo, B_hi, B_lo) of l = l0 .. l0+15
     } sd[NSEED];
-    float acc[2 * N][128];     // FP32 sums of drained chunks, [column][lane]
+    static constexpr int ACC_LD = 2 * N + 4;  // floats per lane row (odd count of float4)
+    float acc[128][ACC_LD];    // FP32 sums of drained chunks, [lane][column]
     uint64_t full_a[2], cdone[2], empty_d[2];
     uint64_t full_b[NBC], bempty[NBC];
     uint64_t sfull[NSEED], sempty[NSEED];
@@ -158,7 +164,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
         S.abort = 0;
         fence_barrier_init();
     }
-    for (int i = threadIdx.x; i < 2 * N * 128; i += THREADS) (&S.acc[0][0])[i] = 0.f;
+    for (int i = threadIdx.x; i < 128 * Smem<N>::ACC_LD; i += THREADS) (&S.acc[0][0])[i] = 0.f;
     if (warp == 0) {
         tmem_alloc(&S.tmem_base, TMEM_COLS);
         tmem_relinquish();
@@ -202,13 +208,14 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
             const int pp = live ? p : a.npairs - 1;
             const float2 x = a.cth32[pp];
             const int ls = live ? a.lstart[(int64_t)m * a.npairs + pp] : lmax + 1;
-            for (int g0 = 0; g0 < G; g0 += CH, ++cc) {
+            const int gf = a.tfirst[(int64_t)m * a.ntiles + tile];
+            for (int g0 = gf; g0 < G; g0 += CH, ++cc) {
                 const uint32_t slot = cc & 1u;
                 // lambda slot free: chunk cc - 2 has retired
                 if (cc >= 2 && !wait(&S.cdone[slot], ((cc >> 1) - 1) & 1u)) { ok = false; break; }
                 const int g = g0 + set;
                 if (g < G) {
-                    const uint32_t gg = gc + (uint32_t)g;
+                    const uint32_t gg = gc + (uint32_t)(g - gf);
                     const int q = (int)(gg % NSEED);
                     if (!wait(&S.sfull[q], (gg / NSEED) & 1u)) { ok = false; break; }
                     fence_after_sync();
@@ -223,7 +230,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
                     if (regular) {
 #pragma unroll
                         for (int j = 0; j < GLG_GROUP; ++j) {
-                            const float v = j == 0 ? seed.x : j == 1 ? seed.y : rec_step_comp(sd.coef[j], x, lm1, lm2);
+                            const float v = j == 0 ? seed.x : j == 1 ? seed.y : rec_step(sd.coef[j], x, lm1, lm2);
                             lm2 = lm1;
                             lm1 = v;
                             const uint32_t hi = tf32_rna(v);
@@ -248,7 +255,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
                             } else if (l == s0 + 1) {
                                 v = seed.y;
                             } else {
-                                v = rec_step_comp(sd.coef[j], x, lm1, lm2);
+                                v = rec_step(sd.coef[j], x, lm1, lm2);
                             }
                             lm2 = lm1;
                             lm1 = v;
@@ -276,7 +283,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&S.full_a[slot]);  // every set arrives, active or not
             }
-            gc += (uint32_t)G;
+            gc += (uint32_t)(G - gf);
         }
         if (!ok) fail();
     } else if (warp < W_MMA) {
@@ -287,16 +294,27 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
             const int tile = (int)(u % a.ntiles);
             const int m = unit_m(u / a.ntiles, lmax);
             const int G = (lmax - m + GLG_GROUP) / GLG_GROUP;
-            for (int g0 = 0; g0 < G; g0 += CH, ++cc) {
+            const int gf = a.tfirst[(int64_t)m * a.ntiles + tile];
+            for (int g0 = gf; g0 < G; g0 += CH, ++cc) {
                 const uint32_t d = cc & 1u;
                 if (!wait(&S.cdone[d], (cc >> 1) & 1u)) { ok = false; break; }
                 fence_after_sync();
-                for (int c0 = 0; c0 < 2 * N; c0 += 16) {
-                    uint32_t v[16];
-                    tmem_ld16(tb + lane_base + 2 * N * d + c0, v);
+                static_assert((2 * N) % 32 == 0, "accumulator columns in pairs of 16");
+                float4 *row = reinterpret_cast<float4 *>(&S.acc[r][0]);
+                for (int c0 = 0; c0 < 2 * N; c0 += 32) {  // two loads in flight per wait
+                    uint32_t v[32];
+                    tmem_ld16(tb + lane_base + 2 * N * d + c0, *reinterpret_cast<uint32_t(*)[16]>(&v[0]));
+                    tmem_ld16(tb + lane_base + 2 * N * d + c0 + 16, *reinterpret_cast<uint32_t(*)[16]>(&v[16]));
                     tmem_wait_ld();
 #pragma unroll
-                    for (int j = 0; j < 16; ++j) S.acc[c0 + j][r] += __uint_as_float(v[j]);
+                    for (int j = 0; j < 8; ++j) {
+                        float4 t = row[c0 / 4 + j];
+                        t.x += __uint_as_float(v[4 * j]);
+                        t.y += __uint_as_float(v[4 * j + 1]);
+                        t.z += __uint_as_float(v[4 * j + 2]);
+                        t.w += __uint_as_float(v[4 * j + 3]);
+                        row[c0 / 4 + j] = t;
+                    }
                 }
                 fence_before_sync();
                 __syncwarp();
@@ -308,14 +326,15 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
             if (p < a.npairs) {
                 const int rs = a.nrings - 1 - p;
                 for (int map = 0; map < a.nmaps; ++map) {
-                    const float er = S.acc[2 * map][r], ei = S.acc[2 * map + 1][r];
-                    const float orr = S.acc[N + 2 * map][r], oi = S.acc[N + 2 * map + 1][r];
+                    const float er = S.acc[r][2 * map], ei = S.acc[r][2 * map + 1];
+                    const float orr = S.acc[r][N + 2 * map], oi = S.acc[r][N + 2 * map + 1];
                     float2 *Fm = a.F + ((int64_t)map * (lmax + 1) + m) * a.nrings;
                     Fm[p] = make_float2(er + orr, ei + oi);
                     if (rs != p) Fm[rs] = make_float2(er - orr, ei - oi);
                 }
             }
-            for (int c0 = 0; c0 < 2 * N; ++c0) S.acc[c0][r] = 0.f;
+            for (int c0 = 0; c0 < 2 * N; c0 += 4)
+                *reinterpret_cast<float4 *>(&S.acc[r][c0]) = make_float4(0.f, 0.f, 0.f, 0.f);
         }
         if (!ok) fail();
     } else if (warp == W_MMA) {
@@ -324,9 +343,11 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
             uint32_t cc = 0;
             bool ok = true, issued = false;
             for (int64_t u = blockIdx.x; u < a.nunits && ok; u += gridDim.x) {
+                const int tile = (int)(u % a.ntiles);
                 const int m = unit_m(u / a.ntiles, lmax);
                 const int G = (lmax - m + GLG_GROUP) / GLG_GROUP;
-                for (int g0 = 0; g0 < G; g0 += CH, ++cc) {
+                const int gf = a.tfirst[(int64_t)m * a.ntiles + tile];
+                for (int g0 = gf; g0 < G; g0 += CH, ++cc) {
                     const uint32_t k = cc & 1u, bsl = cc % NBC;
                     if (cc >= 2 && !wait(&S.empty_d[k], ((cc >> 1) - 1) & 1u)) { ok = false; break; }
                     if (!wait(&S.full_b[bsl], (cc / NBC) & 1u) || !wait(&S.full_a[k], (cc >> 1) & 1u)) {
@@ -337,21 +358,28 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
                     const int ng = G - g0 < CH ? G - g0 : CH;
                     const uint32_t dE = tb + 2 * N * k, dO = dE + N;
                     const uint32_t a0 = tb + A_COL0 + k * A_SLOT;
-                    const uint32_t b0 = smem_u32(S.bs[bsl].b);
-                    constexpr uint32_t tsz = 32 * N;  // bytes of one B tile
-                    // small cross terms of every group first, E and O alternating
-                    for (int q = 0; q < ng; ++q) {
-                        const uint32_t acol = a0 + 32 * q, bb = b0 + q * BBYTES;
-                        const uint32_t acc = q > 0 ? 1u : 0u;
-                        mma_tf32_ts(dE, acol + 0, sdesc_noswz(bb + tsz, 128, 256), IDESC, acc);
-                        mma_tf32_ts(dO, acol + 16, sdesc_noswz(bb + 3 * tsz, 128, 256), IDESC, acc);
-                        mma_tf32_ts(dE, acol + 8, sdesc_noswz(bb, 128, 256), IDESC, 1u);
-                        mma_tf32_ts(dO, acol + 24, sdesc_noswz(bb + 2 * tsz, 128, 256), IDESC, 1u);
+                    // descriptor of the slot's first tile; the 14-bit start
+                    // address field (bytes / 16) takes the tile offsets
+                    const uint64_t d0 = sdesc_noswz(smem_u32(S.bs[bsl].b), 128, 256);
+                    constexpr uint64_t TT = (32 * N) >> 4, GT = BBYTES >> 4;  // tile, group strides
+                    // small cross terms of every group first, E and O
+                    // alternating; fully unrolled so that nothing but the
+                    // MMAs themselves sits between consecutive issues
+#pragma unroll
+                    for (int q = 0; q < CH; ++q) {
+                        if (q < ng) {
+                            mma_tf32_ts(dE, a0 + 32 * q + 0, d0 + q * GT + TT, IDESC, q > 0 ? 1u : 0u);
+                            mma_tf32_ts(dO, a0 + 32 * q + 16, d0 + q * GT + 3 * TT, IDESC, q > 0 ? 1u : 0u);
+                            mma_tf32_ts(dE, a0 + 32 * q + 8, d0 + q * GT, IDESC, 1u);
+                            mma_tf32_ts(dO, a0 + 32 * q + 24, d0 + q * GT + 2 * TT, IDESC, 1u);
+                        }
                     }
-                    for (int q = 0; q < ng; ++q) {
-                        const uint32_t acol = a0 + 32 * q, bb = b0 + q * BBYTES;
-                        mma_tf32_ts(dE, acol + 0, sdesc_noswz(bb, 128, 256), IDESC, 1u);
-                        mma_tf32_ts(dO, acol + 16, sdesc_noswz(bb + 2 * tsz, 128, 256), IDESC, 1u);
+#pragma unroll
+                    for (int q = 0; q < CH; ++q) {
+                        if (q < ng) {
+                            mma_tf32_ts(dE, a0 + 32 * q + 0, d0 + q * GT, IDESC, 1u);
+                            mma_tf32_ts(dO, a0 + 32 * q + 16, d0 + q * GT + 2 * TT, IDESC, 1u);
+                        }
                     }
                     issued = true;
                     mma_commit(&S.cdone[k]);   // lambda slot free, accumulator ready
@@ -374,10 +402,12 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
             int64_t last_use[NBC];
             for (int k = 0; k < NBC; ++k) last_use[k] = -1;
             for (int64_t u = blockIdx.x; u < a.nunits && ok; u += gridDim.x) {
+                const int tile = (int)(u % a.ntiles);
                 const int m = unit_m(u / a.ntiles, lmax);
                 const int G = (lmax - m + GLG_GROUP) / GLG_GROUP;
+                const int gf = a.tfirst[(int64_t)m * a.ntiles + tile];
                 const int64_t gb = a.goff[m];
-                for (int g0 = 0; g0 < G; g0 += CH, ++cc) {
+                for (int g0 = gf; g0 < G; g0 += CH, ++cc) {
                     const uint32_t bsl = cc % NBC, use = cc / NBC;
                     if (use > 0 && !wait(&S.bempty[bsl], (use - 1) & 1u)) { ok = false; break; }
                     const int ng = G - g0 < CH ? G - g0 : CH;
@@ -407,8 +437,9 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
                 const int G = (lmax - m + GLG_GROUP) / GLG_GROUP;
                 const int64_t gb = a.goff[m];
                 const int64_t cb = a.mofs[m];
-                for (int g = 0; g < G; ++g) {
-                    const uint32_t gg = gc + (uint32_t)g;
+                const int gf = a.tfirst[(int64_t)m * a.ntiles + tile];
+                for (int g = gf; g < G; ++g) {
+                    const uint32_t gg = gc + (uint32_t)(g - gf);
                     const int q = (int)(gg % NSEED);
                     const uint32_t use = gg / NSEED;
                     if (use > 0 && !wait(&S.sempty[q], (use - 1) & 1u)) { ok = false; break; }
@@ -418,7 +449,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
                     bulk_g2s(sd.coef, a.coef32 + cb + (int64_t)g * GLG_GROUP, GLG_GROUP * 16, &S.sfull[q]);
                     last_use[q] = use;
                 }
-                gc += (uint32_t)G;
+                gc += (uint32_t)(G - gf);
             }
             if (!ok) fail();
             for (int q = 0; q < NSEED; ++q)
@@ -493,6 +524,7 @@ int launch_tc(const glg_plan *P, const float2 *alm, int nmaps, float *bpack, flo
     a.seeds = P->seeds;
     a.seed_stride = P->seed_stride;
     a.lstart = P->lstart;
+    a.tfirst = P->tfirst;
     a.bpack = reinterpret_cast<const unsigned char *>(bpack);
     a.F = F;
     a.err = err;

@@ -203,7 +203,7 @@ extern "C" void glg_plan_destroy(glg_plan *P) {
     void *ptrs[] = {P->cth,   P->sth,       P->nph,     P->half,   P->startN, P->startS,
                     P->mofs,  P->coef,      P->lmm,     P->lmm_scale, P->fft_radix,
                     P->fft_nst, P->tw_ofs,  P->tw,      P->cth32,  P->tw32,   P->coef32,
-                    P->goff,  P->seeds,     P->lstart,  P->bucket_pairs, P->chirp_ofs,
+                    P->goff,  P->seeds,     P->lstart,  P->tfirst, P->bucket_pairs, P->chirp_ofs,
                     P->chirp, P->pos_ofs, P->pos16,   P->blu_ofs, P->blu_M,  P->blu_H,  P->twM};
     for (void *q : ptrs)
         if (q) cudaFree(q);
@@ -325,13 +325,33 @@ static void fft_pow2_host(std::vector<std::complex<double>> &x) {
     }
 }
 
+// First 16-l group of every (m, ring tile) that holds a lambda above
+// 2^-100 on some ring of the tile: tfirst = (min_p lstart[m][p] - m) / 16
+// (G when no ring of the tile reaches it).  Every group before it is zero
+// on the whole tile, so the contraction skips it.
+__global__ void k_plan_tfirst(int lmax, int npairs, int ntiles, const int *__restrict__ lstart,
+                              int *__restrict__ tfirst) {
+    const int m = blockIdx.y, tile = blockIdx.x;
+    const int p = tile * 128 + threadIdx.x;
+    int ls = p < npairs ? lstart[(int64_t)m * npairs + p] : lmax + 1;
+    for (int o = 16; o > 0; o >>= 1) ls = min(ls, __shfl_xor_sync(0xffffffffu, ls, o));
+    __shared__ int wmin[4];
+    if ((threadIdx.x & 31) == 0) wmin[threadIdx.x >> 5] = ls;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int v = min(min(wmin[0], wmin[1]), min(wmin[2], wmin[3]));
+        const int G = (lmax - m + GLG_GROUP) / GLG_GROUP;
+        tfirst[(int64_t)m * ntiles + tile] = v > lmax ? G : (v - m) / GLG_GROUP;
+    }
+}
+
 // Host-built tables of the FP32 ring FFTs: launch buckets, DIF output
 // orders, the Bluestein chirps c_k = e^{i pi k^2 / n} and chirp spectra
 // H = DFT_M(h), h_t = e^{-i pi t^2 / n} for |t| < n (indices mod M), stored
 // in the DIF output order of M.
 size_t glg_ring32_smem(int kind, int n_or_M, int threads, bool fold) {
     const size_t zs = (size_t)n_or_M + n_or_M / 16 + 1;
-    size_t slots = zs + 2 * (size_t)threads + n_or_M / 2 + 1;
+    size_t slots = zs + 2 * (size_t)threads + glg_zi(n_or_M / 2) + 1;
     if (kind == 0 && fold) slots += zs;
     return slots * sizeof(float2);
 }
@@ -464,7 +484,8 @@ int glg_plan_prepare_fast(glg_plan *P, cudaStream_t st) {
     if ((rc = dalloc(P, &P->cth32, np)) || (rc = dalloc(P, &P->tw32, ntw)) ||
         (rc = dalloc(P, &P->coef32, P->nalm + GLG_GROUP)) || (rc = dalloc(P, &P->goff, lmax + 2)) ||
         (rc = dalloc(P, &P->seeds, (size_t)P->ngroups * P->seed_stride)) ||
-        (rc = dalloc(P, &P->lstart, (size_t)(lmax + 1) * np)))
+        (rc = dalloc(P, &P->lstart, (size_t)(lmax + 1) * np)) ||
+        (rc = dalloc(P, &P->tfirst, (size_t)(lmax + 1) * ((np + 127) / 128))))
         return rc;
     cudaError_t e = cudaMemcpyAsync(P->goff, goff.data(), sizeof(int64_t) * goff.size(),
                                     cudaMemcpyHostToDevice, st);
@@ -478,6 +499,8 @@ int glg_plan_prepare_fast(glg_plan *P, cudaStream_t st) {
     dim3 gs((np + 127) / 128, lmax + 1);
     k_plan_seeds<<<gs, 128, 0, st>>>(lmax, np, P->cth, P->mofs, P->coef, P->lmm, P->lmm_scale,
                                      P->goff, P->seeds, P->seed_stride, P->lstart);
+    k_plan_tfirst<<<dim3((np + 127) / 128, lmax + 1), 128, 0, st>>>(lmax, np, (np + 127) / 128, P->lstart,
+                                                                   P->tfirst);
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return glg_cuda_status(e, "glg_plan_prepare_fast");

@@ -53,11 +53,12 @@ __device__ __forceinline__ c32 ldg(const float2 *p) {
 }
 __device__ __forceinline__ int zi(int e) { return glg_zi(e); }
 
-// e^{DIR 2 pi i t / n}, 0 <= t < n, from the half table wh[t] = e^{2 pi i t / n}, t <= n/2.
+// e^{DIR 2 pi i t / n}, 0 <= t < n, from the half table wh[zi(t)] = e^{2 pi i t / n},
+// t <= n/2 (padded like the data, so strided twiddle reads rarely share a bank).
 template <int DIR>
 __device__ __forceinline__ c32 tw(const c32 *wh, int n, int t) {
     const bool lo = t <= (n >> 1);
-    c32 w = wh[lo ? t : n - t];
+    c32 w = wh[zi(lo ? t : n - t)];
     if (lo != (DIR > 0)) w.y = -w.y;
     return w;
 }
@@ -177,8 +178,13 @@ __device__ __forceinline__ void dft(c32 *v, const c32 *wh, int n) {
 template <int R, int DIR, bool ADJ>
 __device__ __forceinline__ void pass(c32 *Z, const c32 *wh, int n, int L) {
     const int msub = L / R, nbf = n / R, tsc = n / L;
+    // with 32 or more sub-transforms, neighbouring threads take neighbouring
+    // sub-transforms (same twiddles: one broadcast read); otherwise
+    // neighbouring butterflies of one sub-transform
+    const bool by_blk = tsc >= 32;
     for (int bf = threadIdx.x; bf < nbf; bf += blockDim.x) {
-        const int blk = bf / msub, j1 = bf - blk * msub;
+        const int blk = by_blk ? bf % tsc : bf / msub;
+        const int j1 = by_blk ? bf / tsc : bf - blk * msub;
         const int base = blk * L + j1;
         const int ts = tsc * j1;
         c32 v[R];
@@ -378,7 +384,7 @@ __device__ void fold(const float2 *FN, const float2 *FS, bool equator, int n, in
     __syncthreads();
 }
 
-// Class 0: mixed-radix DIF.  smem: Z | SS (n <= mmax) | X[2T] | wh[n/2 + 1].
+// Class 0: mixed-radix DIF.  smem: Z | SS (n <= mmax) | X[2T] | wh[zi(n/2) + 1].
 __global__ void __launch_bounds__(TMAX) k_ring32(const RingArgs a, const Epi32 e) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int map = blockIdx.x % a.nmaps;
@@ -391,7 +397,7 @@ __global__ void __launch_bounds__(TMAX) k_ring32(const RingArgs a, const Epi32 e
     c32 *X = SS + (folds ? zs : 0);
     c32 *wh = X + 2 * T;
     const float2 *w2n = a.tw32 + a.tw_ofs[i4];  // e^{i pi t / n}, t < 2n
-    for (int t = threadIdx.x; t <= n / 2; t += T) wh[t] = ldg(w2n + 2 * t);
+    for (int t = threadIdx.x; t <= n / 2; t += T) wh[zi(t)] = ldg(w2n + 2 * t);
     const int rn = p, rs = a.nrings - 1 - p;
     const bool equator = rn == rs;
     const float2 *FN = a.Ft + ((int64_t)map * a.nrings + rn) * (a.mmax + 1);
@@ -411,7 +417,7 @@ __global__ void __launch_bounds__(TMAX) k_ring32(const RingArgs a, const Epi32 e
 }
 
 // Class 1: Bluestein.  smem: Z[M] (the south fold scratch sits at n..2n-1) |
-// X[2T] | wh[M/2 + 1].
+// X[2T] | wh[zi(M/2) + 1].
 __global__ void __launch_bounds__(TMAX) k_ring32_blu(const RingArgs a, const Epi32 e) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int map = blockIdx.x % a.nmaps;
@@ -422,7 +428,7 @@ __global__ void __launch_bounds__(TMAX) k_ring32_blu(const RingArgs a, const Epi
     c32 *X = Z + (M + M / 16 + 1);
     c32 *wh = X + 2 * T;
     const int stride = a.Mmax / M;
-    for (int t = threadIdx.x; t <= M / 2; t += T) wh[t] = ldg(a.twM + (int64_t)t * stride);
+    for (int t = threadIdx.x; t <= M / 2; t += T) wh[zi(t)] = ldg(a.twM + (int64_t)t * stride);
     const float2 *w2n = a.tw32 + a.tw_ofs[i4];
     const float2 *chirp = a.chirp + a.chirp_ofs[i4];  // e^{i pi k^2 / n}
     const int rn = p, rs = a.nrings - 1 - p;
