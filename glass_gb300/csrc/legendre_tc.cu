@@ -32,10 +32,11 @@
 // of its groups go first and the large A_hi B_hi terms last, so the
 // truncation never falls on a small term added to a large sum.
 //
-// Warp roles (608 threads): warps 0-11 produce lambda (set k = warps
+// Warp roles (640 threads): warps 0-11 produce lambda (set k = warps
 // 4k..4k+3 makes group k of every chunk), warps 12-15 drain the
-// accumulators and store F, warp 16 issues the MMAs, warp 17 streams B and
-// warp 18 streams seeds / coefficients through a ring of NSEED group slots.
+// accumulators and store F, warps 16 and 19 issue the even- and odd-parity
+// MMAs, warp 17 streams B and warp 18 streams seeds / coefficients through
+// a ring of NSEED group slots.
 // Every wait is bounded; on time-out the kernel records GLG_ERR_TIMEOUT in
 // *err, retires its outstanding MMAs and copies, frees its tensor memory and
 // returns.
@@ -51,11 +52,12 @@ namespace {
 constexpr int CH = 3;             // groups per chunk = producer warp sets
 constexpr int NSEED = 16;         // slots of the seed / coefficient ring (groups)
 constexpr int TMEM_COLS = 512;
-constexpr int THREADS = 19 * 32;
+constexpr int THREADS = 20 * 32;
 constexpr uint32_t WAIT_LIMIT = 1u << 22;
-constexpr int W_DRAIN = 12, W_MMA = 16, W_LOAD = 17, W_SEED = 18;
+constexpr int W_DRAIN = 12, W_MMA = 16, W_LOAD = 17, W_SEED = 18, W_MMA2 = 19;
 static_assert(W_DRAIN == 4 * CH, "one producer warp set per group of a chunk");
-static_assert((W_SEED + 1) * 32 == THREADS, "one warp per role after the producers and drains");
+static_assert((W_MMA2 + 1) * 32 == THREADS, "one warp per role after the producers and drains");
+static_assert(W_MMA % 4 != W_MMA2 % 4, "the two MMA-issuing warps on different SM sub-partitions");
 
 struct LegTcArgs {
     int npairs, nrings, lmax, nmaps, ntiles;
@@ -149,18 +151,18 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
     if (threadIdx.x == 0) {
         for (int k = 0; k < 2; ++k) {
             mbar_init(&S.full_a[k], 4 * CH);  // every producer warp, once per chunk
-            mbar_init(&S.cdone[k], 1);        // the chunk's commit
+            mbar_init(&S.cdone[k], 2);        // the chunk's commits (E and O warps)
             mbar_init(&S.empty_d[k], 4);      // the drain warps
         }
         for (int k = 0; k < NBC; ++k) {
             mbar_init(&S.full_b[k], 1);
-            mbar_init(&S.bempty[k], 1);
+            mbar_init(&S.bempty[k], 2);
         }
         for (int q = 0; q < NSEED; ++q) {
             mbar_init(&S.sfull[q], 1);
             mbar_init(&S.sempty[q], 4);
         }
-        mbar_init(&S.drain, 1);
+        mbar_init(&S.drain, 2);
         S.abort = 0;
         fence_barrier_init();
     }
@@ -244,19 +246,16 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
                             }
                         }
                     } else {
+                        // rings of the tile start at different l: branch-free
+                        // steps, the recurrence of zeros staying zero until the
+                        // lane's seeds at js = s0 - l0 are selected in
+                        const int js = s0 - l0, jend = lmax - l0;
 #pragma unroll
                         for (int j = 0; j < GLG_GROUP; ++j) {
-                            const int l = l0 + j;
-                            float v;
-                            if (l < s0 || l > lmax) {
-                                v = 0.f;
-                            } else if (l == s0) {
-                                v = seed.x;
-                            } else if (l == s0 + 1) {
-                                v = seed.y;
-                            } else {
-                                v = rec_step(sd.coef[j], x, lm1, lm2);
-                            }
+                            float v = rec_step(sd.coef[j], x, lm1, lm2);
+                            v = j == js ? seed.x : v;
+                            v = j == js + 1 ? seed.y : v;
+                            v = j > jend ? 0.f : v;
                             lm2 = lm1;
                             lm1 = v;
                             const uint32_t hi = tf32_rna(v);
@@ -337,8 +336,13 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
                 *reinterpret_cast<float4 *>(&S.acc[r][c0]) = make_float4(0.f, 0.f, 0.f, 0.f);
         }
         if (!ok) fail();
-    } else if (warp == W_MMA) {
+    } else if (warp == W_MMA || warp == W_MMA2) {
         // ---------------------------------------------------------- MMA issue
+        // Warp W_MMA issues the even-parity (E) accumulator's MMAs, warp
+        // W_MMA2 the odd (O) one's, from different SM sub-partitions: each
+        // competes with that sub-partition's producer and drain warps for
+        // issue slots, so two issuers halve the time spent waiting for them.
+        const uint32_t par = warp == W_MMA ? 0u : 1u;
         if (lane == 0) {
             uint32_t cc = 0;
             bool ok = true, issued = false;
@@ -356,30 +360,26 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
                     }
                     fence_after_sync();
                     const int ng = G - g0 < CH ? G - g0 : CH;
-                    const uint32_t dE = tb + 2 * N * k, dO = dE + N;
-                    const uint32_t a0 = tb + A_COL0 + k * A_SLOT;
+                    const uint32_t dD = tb + 2 * N * k + N * par;              // this parity's accumulator
+                    const uint32_t a0 = tb + A_COL0 + k * A_SLOT + 16 * par;   // its (A_hi, A_lo) columns
                     // descriptor of the slot's first tile; the 14-bit start
                     // address field (bytes / 16) takes the tile offsets
-                    const uint64_t d0 = sdesc_noswz(smem_u32(S.bs[bsl].b), 128, 256);
                     constexpr uint64_t TT = (32 * N) >> 4, GT = BBYTES >> 4;  // tile, group strides
-                    // small cross terms of every group first, E and O
-                    // alternating; fully unrolled so that nothing but the
-                    // MMAs themselves sits between consecutive issues
+                    // this parity's (B_hi, B_lo) tiles: E at tiles 0, 1; O at 2, 3
+                    const uint64_t d0 = sdesc_noswz(smem_u32(S.bs[bsl].b), 128, 256) + 2 * TT * par;
+                    // small cross terms of every group first, then the large
+                    // terms; fully unrolled so that nothing but the MMAs
+                    // themselves sits between consecutive issues
 #pragma unroll
                     for (int q = 0; q < CH; ++q) {
                         if (q < ng) {
-                            mma_tf32_ts(dE, a0 + 32 * q + 0, d0 + q * GT + TT, IDESC, q > 0 ? 1u : 0u);
-                            mma_tf32_ts(dO, a0 + 32 * q + 16, d0 + q * GT + 3 * TT, IDESC, q > 0 ? 1u : 0u);
-                            mma_tf32_ts(dE, a0 + 32 * q + 8, d0 + q * GT, IDESC, 1u);
-                            mma_tf32_ts(dO, a0 + 32 * q + 24, d0 + q * GT + 2 * TT, IDESC, 1u);
+                            mma_tf32_ts(dD, a0 + 32 * q + 0, d0 + q * GT + TT, IDESC, q > 0 ? 1u : 0u);
+                            mma_tf32_ts(dD, a0 + 32 * q + 8, d0 + q * GT, IDESC, 1u);
                         }
                     }
 #pragma unroll
                     for (int q = 0; q < CH; ++q) {
-                        if (q < ng) {
-                            mma_tf32_ts(dE, a0 + 32 * q + 0, d0 + q * GT, IDESC, 1u);
-                            mma_tf32_ts(dO, a0 + 32 * q + 16, d0 + q * GT + 2 * TT, IDESC, 1u);
-                        }
+                        if (q < ng) mma_tf32_ts(dD, a0 + 32 * q + 0, d0 + q * GT, IDESC, 1u);
                     }
                     issued = true;
                     mma_commit(&S.cdone[k]);   // lambda slot free, accumulator ready
@@ -424,7 +424,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
                     }
         }
         __syncwarp();
-    } else {
+    } else if (warp == W_SEED) {
         // ----------------------------------- seed / coefficient streaming
         if (lane == 0) {
             uint32_t gc = 0;
