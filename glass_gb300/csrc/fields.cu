@@ -201,8 +201,6 @@ __global__ void k_philox_normals(uint64_t seed, uint64_t sid, int64_t offset, in
 // form (FP32) accumulates in FP32, the plain form in FP64.
 constexpr int CT_L = 16;
 
-constexpr int CT_SB = 4;  // shells per block of the correlated sum
-
 template <typename T2, typename T>
 __global__ void k_alm_correlate(const double *__restrict__ w, const int nshell, const int lmax,
                                 const int k, const int64_t t0, const T2 *__restrict__ z,
@@ -211,8 +209,8 @@ __global__ void k_alm_correlate(const double *__restrict__ w, const int nshell, 
     extern __shared__ __align__(16) unsigned char sm_raw[];
     const int kp = k + 1;
     const int wst = kp | 1;  // odd row stride: the 16 l rows sit in distinct banks
-    T *ws = reinterpret_cast<T *>(sm_raw);  // [CT_SB][CT_L][wst]: w rows of a block of shells
-    const size_t ws_bytes = ((sizeof(T) * CT_SB * CT_L * wst) + 15) & ~(size_t)15;
+    T *ws = reinterpret_cast<T *>(sm_raw);  // [CT_L][wst]
+    const size_t ws_bytes = ((sizeof(T) * CT_L * wst) + 15) & ~(size_t)15;
     // variate window, slot-major ([slot][thread]) so a warp's accesses are contiguous
     T2 *zs = reinterpret_cast<T2 *>(sm_raw + ws_bytes) + threadIdx.x;
     const int B = blockDim.x;
@@ -234,53 +232,48 @@ __global__ void k_alm_correlate(const double *__restrict__ w, const int nshell, 
             return philox_cnormal_f32(seed, sid_base + (uint64_t)t, (uint64_t)g);
         }
     };
-    // shell t lives in slot t mod window (window >= k + CT_SB)
-    if (valid)
-        for (int64_t t = zlo; t < t0; ++t) zs[(int)(t % window) * B] = fetch(t);
-    const T *wl = ws + (l - l0) * wst;
-    for (int s0 = 0; s0 < nshell; s0 += CT_SB) {
-        const int nb = nshell - s0 < CT_SB ? nshell - s0 : CT_SB;
-        __syncthreads();
-        for (int q = threadIdx.x; q < nb * CT_L * kp; q += B) {
-            const int bq = q / (CT_L * kp), rq = q - bq * (CT_L * kp);
-            const int r = rq / kp, c = rq - r * kp;
-            const int lg = l0 + r;
-            ws[(bq * CT_L + r) * wst + c] = lg <= lmax ? (T)w[((size_t)(s0 + bq) * L + lg) * kp + c] : (T)0;
-        }
-        __syncthreads();
-        if (!valid) continue;
-        const int64_t ta = t0 + s0;  // first shell of the block
-        for (int b = 0; b < nb; ++b) zs[(int)((ta + b) % window) * B] = fetch(ta + b);
-        // alm_t = sum_{j = max(0, t-k)}^{t} w_t[k - (t - j)] z_j, oldest variate
-        // first for every shell (the order of the reference's deque sum); one
-        // read of z_j serves every shell of the block
-        T re[CT_SB], im[CT_SB];
-#pragma unroll
-        for (int b = 0; b < CT_SB; ++b) re[b] = im[b] = 0;
-        const int64_t jlo = ta - k > 0 ? ta - k : 0, jhi = ta + nb - 1;
-        int slot = (int)(jlo % window);
-        for (int64_t j = jlo; j <= jhi; ++j) {
-            const T2 zz = zs[slot * B];
+    // shell t lives in slot t mod window; head = slot of the current shell
+    int head = (int)(t0 % window);
+    if (valid) {
+        int slot = (int)(zlo % window);
+        for (int64_t t = zlo; t < t0; ++t) {
+            zs[slot * B] = fetch(t);
             if (++slot == window) slot = 0;
-#pragma unroll
-            for (int b = 0; b < CT_SB; ++b) {
-                const int64_t d = ta + b - j;  // lag of z_j for shell ta + b
-                if (b < nb && d >= 0 && d <= k) {
-                    const T c = wl[b * CT_L * wst + (k - (int)d)];
-                    re[b] += c * zz.x;
-                    im[b] += c * zz.y;
-                }
-            }
         }
-#pragma unroll
-        for (int b = 0; b < CT_SB; ++b) {
-            if (b < nb) {
-                T2 o;
-                o.x = m == 0 ? re[b] + im[b] : re[b];
-                o.y = m == 0 ? (T)0 : im[b];
-                alm[(int64_t)(s0 + b) * nalm + ix] = o;
-            }
+    }
+    for (int s = 0; s < nshell; ++s) {
+        const int64_t t = t0 + s;
+        __syncthreads();
+        for (int q = threadIdx.x; q < CT_L * kp; q += B) {
+            const int r = q / kp, c = q - r * kp;
+            const int lg = l0 + r;
+            ws[r * wst + c] = lg <= lmax ? (T)w[((size_t)s * L + lg) * kp + c] : (T)0;
         }
+        __syncthreads();
+        if (valid) {
+            zs[head * B] = fetch(t);
+            const T *wt = ws + (l - l0) * wst;
+            T re = 0, im = 0;
+            const int dmax = t < k ? (int)t : k;
+            int j = head - dmax;
+            if (j < 0) j += window;
+            for (int d = dmax; d >= 0; --d) {
+                const T2 zz = zs[j * B];
+                const T c = wt[k - d];
+                re += c * zz.x;
+                im += c * zz.y;
+                if (++j == window) j = 0;
+            }
+            if (m == 0) {
+                re = re + im;
+                im = 0;
+            }
+            T2 o;
+            o.x = re;
+            o.y = im;
+            alm[(int64_t)s * nalm + ix] = o;
+        }
+        if (++head == window) head = 0;
     }
 }
 
@@ -392,12 +385,12 @@ extern "C" int glg_alm_correlate(const double *w, int nshell, int lmax, int k, i
     GLG_REQUIRE(k <= 126, "glg_alm_correlate: k must be <= 126");
     if (z) GLG_REQUIRE(z_first == (t0 - k > 0 ? t0 - k : 0), "glg_alm_correlate: z must start at max(0, t0-k)");
     if (nshell == 0) return GLG_OK;
-    const int window = k + CT_SB;
+    const int window = k + 1;
     const size_t esz = dtype == GLG_F64 ? sizeof(double2) : sizeof(float2);
     const size_t rsz = dtype == GLG_F64 ? sizeof(double) : sizeof(float);
     int threads = 128;  // 16 l x 8 m; fewer m per tile when the variate window is long
     auto smem_for = [&](int th) {
-        return (((rsz * CT_SB * CT_L * (size_t)((k + 1) | 1)) + 15) & ~(size_t)15) + esz * (size_t)window * th;
+        return (((rsz * CT_L * (size_t)(window | 1)) + 15) & ~(size_t)15) + esz * (size_t)window * th;
     };
     while (threads > CT_L && smem_for(threads) > 200 * 1024) threads /= 2;
     const size_t smem = smem_for(threads);
