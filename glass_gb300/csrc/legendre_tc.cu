@@ -51,6 +51,8 @@ namespace {
 
 constexpr int CH = 3;             // groups per chunk = producer warp sets
 constexpr int NSEED = 16;         // slots of the seed / coefficient ring (groups)
+constexpr int NU = 8;             // slots of the unit ring
+constexpr int NCONSUMERS = 19;    // warps that read the unit ring (all but the seed streamer)
 constexpr int TMEM_COLS = 512;
 constexpr int THREADS = 20 * 32;
 constexpr uint32_t WAIT_LIMIT = 1u << 22;
@@ -73,6 +75,7 @@ struct LegTcArgs {
     const unsigned char *bpack;
     float2 *F;  // [map][m][ring]
     int *err;
+    unsigned long long *ucount;  // next unit to hand out (zeroed before the launch)
 };
 
 __device__ __forceinline__ uint32_t tf32_rna(float x) {
@@ -130,6 +133,8 @@ struct Smem {
     uint64_t full_a[2], cdone[2], empty_d[2];
     uint64_t full_b[NBC], bempty[NBC];
     uint64_t sfull[NSEED], sempty[NSEED];
+    uint64_t ufull[NU], uempty[NU];
+    int64_t unit[NU];  // units handed out to this CTA, in order
     uint64_t drain;
     uint32_t tmem_base;
     int abort;
@@ -162,6 +167,10 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
             mbar_init(&S.sfull[q], 1);
             mbar_init(&S.sempty[q], 4);
         }
+        for (int q = 0; q < NU; ++q) {
+            mbar_init(&S.ufull[q], 1);
+            mbar_init(&S.uempty[q], NCONSUMERS);
+        }
         mbar_init(&S.drain, 2);
         S.abort = 0;
         fence_barrier_init();
@@ -188,6 +197,20 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
         fail();
         return false;
     };
+    // Units are handed out dynamically from a global counter (by the seed
+    // streamer, which runs ahead), so that all CTAs work on neighbouring units
+    // at any time: the ring tiles of one m then read the same B tiles within
+    // a short window and find them in L2.  next_unit() returns the i-th unit
+    // of this CTA (>= nunits: no more) and frees its ring slot; called by all
+    // lanes of a warp (whole_warp) or by lane 0 alone.
+    auto next_unit = [&](uint32_t i, int64_t &u, bool whole_warp) -> bool {
+        const uint32_t q = i % NU;
+        if (!wait(&S.ufull[q], (i / NU) & 1u)) return false;
+        u = *reinterpret_cast<volatile int64_t *>(&S.unit[q]);
+        if (whole_warp) __syncwarp();
+        if (lane == 0) mbar_arrive(&S.uempty[q]);
+        return true;
+    };
     const int lmax = a.lmax;
     const uint32_t lane_base = (uint32_t)((warp & 3) << 5) << 16;
     const int r = ((warp & 3) << 5) + lane;  // TMEM lane = ring pair in tile
@@ -201,7 +224,10 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
         const int set = warp >> 2;
         uint32_t cc = 0, gc = 0;
         bool ok = true;
-        for (int64_t u = blockIdx.x; u < a.nunits && ok; u += gridDim.x) {
+        for (uint32_t ui = 0; ok; ++ui) {
+            int64_t u;
+            if (!next_unit(ui, u, true)) { ok = false; break; }
+            if (u >= a.nunits) break;
             const int tile = (int)(u % a.ntiles);
             const int m = unit_m(u / a.ntiles, lmax);
             const int G = (lmax - m + GLG_GROUP) / GLG_GROUP;
@@ -289,7 +315,10 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
         // --------------------------------- drain: chunk sums -> smem -> F
         uint32_t cc = 0;
         bool ok = true;
-        for (int64_t u = blockIdx.x; u < a.nunits && ok; u += gridDim.x) {
+        for (uint32_t ui = 0; ok; ++ui) {
+            int64_t u;
+            if (!next_unit(ui, u, true)) { ok = false; break; }
+            if (u >= a.nunits) break;
             const int tile = (int)(u % a.ntiles);
             const int m = unit_m(u / a.ntiles, lmax);
             const int G = (lmax - m + GLG_GROUP) / GLG_GROUP;
@@ -361,10 +390,13 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
         // competes with that sub-partition's producer and drain warps for
         // issue slots, so two issuers halve the time spent waiting for them.
         const uint32_t par = warp == W_MMA ? 0u : 1u;
-        if (lane == 0) {
-            uint32_t cc = 0;
-            bool ok = true, issued = false;
-            for (int64_t u = blockIdx.x; u < a.nunits && ok; u += gridDim.x) {
+        uint32_t cc = 0;
+        bool ok = true, issued = false;
+        for (uint32_t ui = 0; ok && lane == 0; ++ui) {
+            int64_t u;
+            if (!next_unit(ui, u, false)) { ok = false; break; }
+            if (u >= a.nunits) break;
+            {
                 const int tile = (int)(u % a.ntiles);
                 const int m = unit_m(u / a.ntiles, lmax);
                 const int G = (lmax - m + GLG_GROUP) / GLG_GROUP;
@@ -404,6 +436,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
                     mma_commit(&S.bempty[bsl]);
                 }
             }
+        }
+        if (lane == 0) {
             if (!ok) fail();
             if (issued) {  // every MMA of this CTA retired before TMEM is freed
                 mma_commit(&S.drain);
@@ -414,12 +448,15 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
         __syncwarp();
     } else if (warp == W_LOAD) {
         // ------------------------------------------------------- B streaming
-        if (lane == 0) {
-            uint32_t cc = 0;
-            bool ok = true;
-            int64_t last_use[NBC];
-            for (int k = 0; k < NBC; ++k) last_use[k] = -1;
-            for (int64_t u = blockIdx.x; u < a.nunits && ok; u += gridDim.x) {
+        uint32_t cc = 0;
+        bool ok = true;
+        int64_t last_use[NBC];
+        for (int k = 0; k < NBC; ++k) last_use[k] = -1;
+        for (uint32_t ui = 0; ok && lane == 0; ++ui) {
+            int64_t u;
+            if (!next_unit(ui, u, false)) { ok = false; break; }
+            if (u >= a.nunits) break;
+            {
                 const int tile = (int)(u % a.ntiles);
                 const int m = unit_m(u / a.ntiles, lmax);
                 const int G = (lmax - m + GLG_GROUP) / GLG_GROUP;
@@ -434,6 +471,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
                     last_use[bsl] = use;
                 }
             }
+        }
+        if (lane == 0) {
             if (!ok) fail();
             // outstanding copies land before the CTA exits
             for (int k = 0; k < NBC; ++k)
@@ -443,13 +482,19 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
         }
         __syncwarp();
     } else if (warp == W_SEED) {
-        // ----------------------------------- seed / coefficient streaming
+        // ------------------- unit hand-out, seed / coefficient streaming
         if (lane == 0) {
             uint32_t gc = 0;
             bool ok = true;
             int64_t last_use[NSEED];
             for (int q = 0; q < NSEED; ++q) last_use[q] = -1;
-            for (int64_t u = blockIdx.x; u < a.nunits && ok; u += gridDim.x) {
+            for (uint32_t ui = 0; ok; ++ui) {
+                const uint32_t uq = ui % NU;
+                if (ui >= NU && !wait(&S.uempty[uq], ((ui / NU) - 1) & 1u)) { ok = false; break; }
+                const int64_t u = (int64_t)atomicAdd(a.ucount, 1ull);
+                S.unit[uq] = u;
+                mbar_arrive(&S.ufull[uq]);  // release: the slot's unit is visible to its readers
+                if (u >= a.nunits) break;
                 const int tile = (int)(u % a.ntiles);
                 const int m = unit_m(u / a.ntiles, lmax);
                 const int G = (lmax - m + GLG_GROUP) / GLG_GROUP;
@@ -546,6 +591,7 @@ int launch_tc(const glg_plan *P, const float2 *alm, int nmaps, float *bpack, flo
     a.bpack = reinterpret_cast<const unsigned char *>(bpack);
     a.F = F;
     a.err = err;
+    a.ucount = reinterpret_cast<unsigned long long *>(reinterpret_cast<char *>(err) + 64);
     // more than half of the SM's shared memory: one CTA per SM, so no two
     // CTAs contend for the 512 tensor-memory columns
     size_t smem = sizeof(Smem<N>) + 128;
