@@ -11,7 +11,7 @@ computed by hand-written CUDA kernels for sm_103a behind the C ABI of
 
 from __future__ import annotations
 
-from . import grf, harmonics, healpix, points, rng
+from . import galaxies, grf, harmonics, healpix, points, rng
 from .fields import (
     cls2cov,
     enumerate_spectra,
@@ -24,12 +24,16 @@ from .fields import (
     spectra_indices,
 )
 from .harmonics import multalm
-from .lensing import from_convergence, shear_from_convergence
+from .galaxies import galaxy_shear
+from .lensing import MultiPlaneConvergence, from_convergence, shear_from_convergence
 
 __all__ = [
+    "MultiPlaneConvergence",
     "cls2cov",
     "enumerate_spectra",
     "from_convergence",
+    "galaxies",
+    "galaxy_shear",
     "generate",
     "generate_gaussian",
     "generate_lognormal",

@@ -26,6 +26,7 @@ from ._lib import c_p, check, get_plan, lib, ptr, stream_ptr
 
 __all__ = [
     "alm2map",
+    "ang2pix",
     "alm2map_spin",
     "almxfl",
     "get_nside",
@@ -45,6 +46,23 @@ def npix2nside(npix: int) -> int:
     if 12 * nside * nside != int(npix):
         raise ValueError(f"{npix} is not a valid number of HEALPix pixels")
     return nside
+
+
+def ang2pix(nside: int, theta, phi, *, lonlat: bool = False):
+    """RING-scheme pixel indices of positions (healpy.ang2pix, as called
+    through glass/healpix.py at glass/galaxies.py:329).  With ``lonlat``,
+    ``theta`` / ``phi`` are longitude / latitude in degrees."""
+    numpy_out = _lib.is_numpy_like(theta)
+    a = _lib.to_device(theta, torch.float64).reshape(-1)
+    b = _lib.to_device(phi, torch.float64).reshape(-1)
+    if a.numel() != b.numel():
+        raise ValueError("theta and phi must have the same size")
+    out = torch.empty(a.numel(), dtype=torch.int64, device=a.device)
+    _lib.check(_lib.lib().glg_ang2pix(int(nside), _lib.c_p(_lib.ptr(a)), _lib.c_p(_lib.ptr(b)), a.numel(),
+                                      1 if lonlat else 0, _lib.c_p(_lib.ptr(out)),
+                                      _lib.c_p(_lib.stream_ptr(a.device))), "glg_ang2pix")
+    shape = np.shape(theta) if numpy_out else tuple(theta.shape)
+    return _finish(out.reshape(shape), numpy_out)
 
 
 def get_nside(m) -> int:

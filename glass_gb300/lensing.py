@@ -1,8 +1,10 @@
-"""Weak-lensing maps from the convergence (glass/lensing.py:185-428).
+"""Weak-lensing maps from the convergence (glass/lensing.py:185-586).
 
 ``from_convergence`` follows the reference step by step: analysis of kappa
 (map2alm), multiplication by the harmonic kernels with almxfl, and spin-0,
-spin-1 and spin-2 synthesis, all on the GPU.
+spin-1 and spin-2 synthesis, all on the GPU.  ``MultiPlaneConvergence``
+keeps its convergence planes on the device and advances them with one fused
+kernel per plane.
 """
 
 from __future__ import annotations
@@ -84,3 +86,92 @@ def shear_from_convergence(kappa, lmax: int | None = None, *, discretized: bool 
     alm = hp.almxfl(alm, torch.as_tensor(fl, device=alm.device))
     q, u = hp._spin_synth(alm, None, nside, 2, lmax)
     return [q.cpu().numpy(), u.cpu().numpy()] if numpy_out else [q, u]
+
+
+class MultiPlaneConvergence:
+    """Convergence from multiple matter planes (glass/lensing.py:430-598).
+
+    Same state and recurrence as the reference: the host computes the
+    distance ratios t and the lensing weight f from ``cosmo`` exactly as the
+    reference does, and one kernel per plane applies
+    kappa3 <- kappa1 (1 - t) + t kappa2 + f delta2 to the device planes.
+    numpy planes in give numpy planes out (``kappa`` / ``delta`` copy to the
+    host on access); torch planes stay on the device.
+    """
+
+    def __init__(self, cosmo) -> None:
+        self.cosmo = cosmo
+        self.z2 = 0.0
+        self.z3 = 0.0
+        self.x3 = 0.0
+        self.w3 = 0.0
+        self.r23 = 1.0
+        self._delta3 = None
+        self._kappa2 = None
+        self._kappa3 = None
+        self._numpy = True
+
+    def add_window(self, delta, w) -> None:
+        """Add a mass plane with the weight and redshift of window ``w``."""
+        zsrc = w.zeff
+        lens_weight = float(np.trapezoid(w.wa, w.za) / np.interp(zsrc, w.za, w.wa))
+        self.add_plane(delta, zsrc, lens_weight)
+
+    def add_plane(self, delta, zsrc, wlens: float = 1.0) -> None:
+        """Add a mass plane at redshift ``zsrc`` (glass/lensing.py:512-581)."""
+        if zsrc <= self.z3:
+            raise ValueError("source redshift must be increasing")
+        self._numpy = _lib.is_numpy_like(delta)
+        d = _lib.to_device(delta, torch.float64 if np.asarray(delta).dtype != np.float32 else torch.float32) \
+            if self._numpy else delta.contiguous()
+        if d.dtype not in (torch.float32, torch.float64):
+            d = d.to(torch.float64)
+        delta2, self._delta3 = self._delta3, d
+        z1, self.z2, self.z3 = self.z2, self.z3, zsrc
+        w2, self.w3 = self.w3, wlens
+        x2, self.x3 = (self.x3,
+                       self.cosmo.transverse_comoving_distance(self.z3) / self.cosmo.hubble_distance)
+        r12 = self.r23
+        r13, self.r23 = self.cosmo.transverse_comoving_distance([z1, self.z2], self.z3) / (
+            self.cosmo.hubble_distance * self.x3)
+        t = r13 / r12
+        f = 3 * self.cosmo.Omega_m0 / 2
+        f *= x2 * self.r23
+        f *= (1 + self.z2) / self.cosmo.H_over_H0(self.z2)
+        f *= w2
+        if self._kappa2 is None:
+            self._kappa2 = torch.zeros_like(d)
+            self._kappa3 = torch.zeros_like(d)
+        self._kappa2, self._kappa3 = self._kappa3, self._kappa2
+        k3 = self._kappa3
+        if delta2 is not None and (delta2.dtype != k3.dtype or delta2.shape != k3.shape):
+            raise ValueError("mass planes must share their shape and dtype")
+        code = _lib.GLG_F64 if k3.dtype == torch.float64 else _lib.GLG_F32
+        _lib.check(_lib.lib().glg_convergence_step(
+            _lib.c_p(_lib.ptr(k3)), _lib.c_p(_lib.ptr(self._kappa2)), _lib.c_p(_lib.ptr(delta2)), code,
+            k3.numel(), float(t), float(f), _lib.c_p(_lib.stream_ptr(k3.device))), "glg_convergence_step")
+
+    def _out(self, t):
+        if t is None:
+            return None
+        return t.cpu().numpy() if self._numpy else t
+
+    @property
+    def zsrc(self):
+        """The redshift of the current convergence plane."""
+        return self.z3
+
+    @property
+    def kappa(self):
+        """The current convergence plane."""
+        return self._out(self._kappa3)
+
+    @property
+    def delta(self):
+        """The current matter plane."""
+        return self._out(self._delta3)
+
+    @property
+    def wlens(self) -> float:
+        """The weight of the current matter plane."""
+        return self.w3

@@ -126,6 +126,37 @@ int glg_almxfl(const void *alm, const double *fl, int nfl, int lmax, int nmaps, 
                void *out, void *stream);
 
 /*
+ * One step of the multi-plane convergence recurrence, replacing
+ * glass/lensing.py:577-581 (MultiPlaneConvergence.add_plane):
+ *   kappa3 <- kappa3 * (1 - t);  kappa3 += t * kappa2;  kappa3 += f * delta2
+ * in place, in that order, each step rounded to the maps' type (float64 or
+ * float32, dtype) with FP64 products.  delta2 may be NULL (a zero plane).
+ * t and f are computed on the host from the cosmology as the reference does.
+ */
+int glg_convergence_step(void *kappa3, const void *kappa2, const void *delta2, int dtype, int64_t n,
+                         double t, double f, void *stream);
+
+/*
+ * HEALPix RING-scheme pixel indices (healpy.ang2pix, used at
+ * glass/galaxies.py:329 through glass/healpix.py): lonlat != 0 takes
+ * longitude / latitude in degrees, else colatitude theta / longitude phi in
+ * radians.  Device arrays: float64 inputs [n], int64 output [n].
+ */
+int glg_ang2pix(int nside, const double *theta_or_lon, const double *phi_or_lat, int64_t n, int lonlat,
+                int64_t *ipix, void *stream);
+
+/*
+ * Lensed galaxy ellipticities, replacing glass/galaxies.py:271-347
+ * (galaxy_shear): kappa, gamma1, gamma2 gathered at the RING pixel of each
+ * (lon, lat) in degrees; reduced != 0: g = gamma / (1 - kappa), result
+ * (eps + g) / (1 + conj(g) eps); else eps + gamma.  lon, lat: float64 [n];
+ * eps, out: complex128 [n]; maps: float64 or float32 [12 nside^2] (dtype).
+ */
+int glg_galaxy_shear(const double *lon, const double *lat, const void *eps, int64_t n, const void *kappa,
+                     const void *gamma1, const void *gamma2, int dtype, int nside, int reduced,
+                     void *out, void *stream);
+
+/*
  * Per-pixel Poisson galaxy counts, replacing glass/points.py:252-348
  * (_compute_expected_count, _apply_visibility, _sample_number_galaxies):
  *   n_e = ((bias * delta_e - offset) + 1) * scale  [* vis_e],  clipped at 0,

@@ -368,3 +368,66 @@ def test_poisson_counts_bit_exact_vs_oracle(g):
                                 seed=2, stream=0)
     assert np.mean(got_m == ref_m) > 0.999  # the offset is a device mean: may differ in the last bit
     assert g.points.counts_from_delta(ngal, np.zeros(0)).size == 0
+
+
+# ------------------------------------------------- map-level lensing (8f)
+
+
+@pytest.fixture(scope="module")
+def lensing_golden():
+    from tests.conftest import ROOT
+
+    return np.load(ROOT / "tests" / "golden" / "glass_lensing.npz")
+
+
+def _cosmo():
+    import sys
+
+    from tests.conftest import ROOT
+
+    sys.path.insert(0, str(ROOT / "tests" / "golden"))
+    from cosmo_stub import FlatLCDM
+
+    return FlatLCDM()
+
+
+@pytest.mark.parametrize("tag", ["f64", "f32"])
+def test_multiplane_convergence_vs_reference(g, lensing_golden, tag):
+    """Device convergence planes equal the reference's, bit for bit."""
+    import torch
+
+    gd = lensing_golden
+    mpc = g.MultiPlaneConvergence(_cosmo())
+    mpc_t = g.MultiPlaneConvergence(_cosmo())
+    for z, w, d, ref in zip(gd[f"mpc_{tag}_z"], gd[f"mpc_{tag}_w"], gd[f"mpc_{tag}_delta"], gd[f"mpc_{tag}_kappa"]):
+        mpc.add_plane(d.copy(), float(z), float(w))
+        mpc_t.add_plane(torch.as_tensor(d, device="cuda"), float(z), float(w))
+        assert mpc.kappa.dtype == ref.dtype
+        np.testing.assert_array_equal(mpc.kappa, ref)
+        assert isinstance(mpc_t.kappa, torch.Tensor) and mpc_t.kappa.is_cuda
+        np.testing.assert_array_equal(mpc_t.kappa.cpu().numpy(), ref)
+    with pytest.raises(ValueError, match="source redshift must be increasing"):
+        mpc.add_plane(gd[f"mpc_{tag}_delta"][0], 0.1)
+
+
+def test_ang2pix_vs_oracle(g):
+    import oracle.lensing as olens
+
+    rng = np.random.default_rng(5)
+    for nside in (1, 16, 256, 2048):
+        lon = rng.uniform(-400, 400, 200_000)
+        lat = np.degrees(np.arcsin(rng.uniform(-1, 1, lon.size)))
+        lat[:4] = [90.0, -90.0, 0.0, 41.8103148958]  # poles, equator, z = 2/3
+        np.testing.assert_array_equal(g.healpix.ang2pix(nside, lon, lat, lonlat=True),
+                                      olens.ang2pix_lonlat(nside, lon, lat))
+        theta, phi = olens.lonlat_to_thetaphi(lon, lat)
+        np.testing.assert_array_equal(g.healpix.ang2pix(nside, theta, phi), olens.ang2pix_ring(nside, theta, phi))
+
+
+@pytest.mark.parametrize("reduced", [True, False])
+def test_galaxy_shear_vs_reference(g, lensing_golden, reduced):
+    gd = lensing_golden
+    got = g.galaxy_shear(gd["shear_lon"], gd["shear_lat"], gd["shear_eps"], gd["shear_kappa"], gd["shear_g1"],
+                         gd["shear_g2"], reduced_shear=reduced)
+    assert got.dtype == np.complex128
+    np.testing.assert_allclose(got, gd[f"shear_{int(reduced)}"], rtol=1e-15, atol=0)

@@ -174,3 +174,64 @@ def test_poisson_counts_statistics_and_streams():
     a = orng.poisson_counts(d[:1000], bias=1.5, offset=0.1, scale=2.0, vis=vis, seed=9)
     b = orng.poisson_counts(((1.5 * d[:1000] - 0.1) + 1.0) * 2.0 * vis, scale=1.0, bias=1.0, offset=1.0, seed=9)
     assert np.mean(a == b) > 0.99  # same uniforms, expected counts equal up to rounding
+
+
+# ------------------------------------------------- map-level lensing (8f)
+
+
+@pytest.fixture(scope="module")
+def lensing_golden():
+    from tests.conftest import ROOT
+
+    return np.load(ROOT / "tests" / "golden" / "glass_lensing.npz")
+
+
+def _cosmo():
+    import sys
+
+    from tests.conftest import ROOT
+
+    sys.path.insert(0, str(ROOT / "tests" / "golden"))
+    from cosmo_stub import FlatLCDM
+
+    return FlatLCDM()
+
+
+@pytest.mark.parametrize("tag", ["f64", "f32"])
+def test_multiplane_convergence_matches_reference(lensing_golden, tag):
+    import oracle.lensing as olens
+
+    g = lensing_golden
+    mpc = olens.MultiPlaneConvergence(_cosmo())
+    for z, w, d, ref in zip(g[f"mpc_{tag}_z"], g[f"mpc_{tag}_w"], g[f"mpc_{tag}_delta"], g[f"mpc_{tag}_kappa"]):
+        mpc.add_plane(d.copy(), float(z), float(w))
+        assert mpc.kappa.dtype == ref.dtype
+        np.testing.assert_array_equal(mpc.kappa, ref)
+
+
+def test_ang2pix_ring_pixel_centres_and_offsets():
+    import oracle.lensing as olens
+
+    for nside in (1, 2, 4, 16, 64):
+        z, _, nph, phi0, start = osht.ring_info(nside)
+        theta = np.repeat(np.arccos(z), nph)
+        j = np.concatenate([np.arange(n) for n in nph])
+        phi = np.repeat(phi0, nph) + 2 * np.pi * j / np.repeat(nph, nph)
+        ref = np.repeat(start, nph) + j
+        np.testing.assert_array_equal(olens.ang2pix_ring(nside, theta, phi), ref)
+        # small offsets inside the pixel keep it; longitudes wrap
+        rng = np.random.default_rng(nside)
+        d = 0.05 * np.pi / (4 * nside)
+        np.testing.assert_array_equal(
+            olens.ang2pix_ring(nside, theta + rng.uniform(-d, d, theta.size) * 0.2,
+                               phi + 2 * np.pi * rng.integers(-2, 3, phi.size)), ref)
+
+
+def test_galaxy_shear_matches_reference(lensing_golden):
+    import oracle.lensing as olens
+
+    g = lensing_golden
+    for red in (True, False):
+        got = olens.galaxy_shear(g["shear_lon"], g["shear_lat"], g["shear_eps"], g["shear_kappa"],
+                                 g["shear_g1"], g["shear_g2"], reduced_shear=red)
+        np.testing.assert_array_equal(got, g[f"shear_{int(red)}"])
