@@ -11,7 +11,7 @@ computed by hand-written CUDA kernels for sm_103a behind the C ABI of
 
 from __future__ import annotations
 
-from . import galaxies, grf, harmonics, healpix, points, rng
+from . import galaxies, grf, harmonics, healpix, points, rng, user
 from .fields import (
     cls2cov,
     enumerate_spectra,
@@ -25,6 +25,7 @@ from .fields import (
 )
 from .harmonics import multalm
 from .galaxies import galaxy_shear
+from .user import load_cls, save_cls
 from .lensing import MultiPlaneConvergence, from_convergence, shear_from_convergence
 
 __all__ = [
@@ -43,9 +44,11 @@ __all__ = [
     "healpix",
     "points",
     "iternorm",
+    "load_cls",
     "multalm",
     "nfields_from_nspectra",
     "rng",
+    "save_cls",
     "shear_from_convergence",
     "spectra_indices",
 ]

@@ -50,6 +50,13 @@ class Request:
     finished: float | None = None
     reserved: int = 0
 
+    @classmethod
+    def from_cls_file(cls, filename, nside: int, shifts, seed: int = 42, **kw) -> "Request":
+        """A request whose spectra come from a GLASS ``.npz`` spectra file."""
+        from .user import load_cls
+
+        return cls(gls=load_cls(filename), nside=nside, shifts=[float(x) for x in shifts], seed=seed, **kw)
+
     @property
     def nshell(self) -> int:
         return len(self.shifts)
