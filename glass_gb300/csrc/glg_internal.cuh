@@ -52,6 +52,7 @@ struct glg_launch_scope {
 #define GLG_MAX_RING_BUCKETS 24
 struct glg_ring_bucket {
     int kind, count, threads;
+    int size, fold;  // transform length bucket (n rounded up, or M) and fold scratch
     int64_t first;
     size_t smem;
 };
@@ -168,6 +169,10 @@ int glg_launch_leg_ana(const glg_plan *P, const double2 *G, int nmaps, double2 *
                        cudaStream_t st);
 int glg_launch_ring_syn_f32(const glg_plan *P, const float2 *F, float2 *Ft, int nmaps, float *maps,
                             const glg_epilogue *epi, cudaStream_t st);
+// One size bucket of the FP32 ring FFTs from transposed sums Ft, with
+// `threads` per block (0: the bucket's own), no epilogue (autotuning).
+int glg_launch_ring_bucket_f32(const glg_plan *P, int bucket, int threads, const float2 *Ft, int nmaps,
+                               float *maps, cudaStream_t st);
 size_t glg_leg_tc_pack_bytes(const glg_plan *P, int nmaps);
 int glg_launch_leg_tc(const glg_plan *P, const float2 *alm, int nmaps, float *bpack, float2 *F,
                       int *err, cudaStream_t st);

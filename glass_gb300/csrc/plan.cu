@@ -435,7 +435,9 @@ static int build_fft32_tables(glg_plan *P, cudaStream_t st) {
     for (auto &kv : groups) {
         glg_ring_bucket &b = P->buckets[P->nbuckets++];
         b.kind = kv.first.kind;
-        b.threads = kv.first.size >= 4096 ? 512 : 256;
+        b.size = kv.first.size;
+        b.fold = kv.first.fold;
+        b.threads = kv.first.size >= 4096 ? 512 : 256;  // until glg_autotune_fast picks
         b.smem = glg_ring32_smem(b.kind, kv.first.size, b.threads, kv.first.fold != 0);
         b.count = (int)kv.second.size();
         b.first = (int64_t)bpairs.size();

@@ -475,26 +475,8 @@ __global__ void k_transpose32(const float2 *__restrict__ F, float2 *__restrict__
 
 }  // namespace
 
-int glg_launch_ring_syn_f32(const glg_plan *P, const float2 *F, float2 *Ft, int nmaps, float *maps,
-                            const glg_epilogue *epi_in, cudaStream_t st) {
-    if (nmaps > EPI_MAX) {
-        glg_set_error("fast ring FFT: at most 40 maps per call");
-        return GLG_ERR_UNSUPPORTED;
-    }
-    const int nm = P->mmax + 1, nr = P->nrings;
-    for (int b = 0; b < P->nbuckets; ++b)
-        if (P->buckets[b].smem > 227 * 1024) {
-            glg_set_error("fast ring FFT: ring length too large for shared memory (nside <= 2048)");
-            return GLG_ERR_UNSUPPORTED;
-        }
-    {
-        dim3 grid((nr + 31) / 32, (nm + 31) / 32, nmaps);
-        GLG_LAUNCH_SCOPE("k_transpose32", st);
-        k_transpose32<<<grid, dim3(32, 8), 0, st>>>(F, Ft, nm, nr);
-        GLG_CHECK_LAUNCH("k_transpose32");
-    }
-    RingArgs a;
-    a.nrings = nr;
+static void ring_args(const glg_plan *P, const float2 *Ft, int nmaps, float *maps, RingArgs &a) {
+    a.nrings = P->nrings;
     a.mmax = P->mmax;
     a.nmaps = nmaps;
     a.nph = P->nph;
@@ -515,6 +497,47 @@ int glg_launch_ring_syn_f32(const glg_plan *P, const float2 *F, float2 *Ft, int 
     a.Ft = Ft;
     a.maps = maps;
     a.npix = P->npix;
+}
+
+static int launch_bucket(const glg_plan *P, const glg_ring_bucket &B, int threads, RingArgs a, const Epi32 &e,
+                         cudaStream_t st) {
+    a.pairs = P->bucket_pairs + B.first;
+    const size_t smem = glg_ring32_smem(B.kind, B.size, threads, B.fold != 0);
+    const unsigned grid = (unsigned)B.count * (unsigned)a.nmaps;
+    if (B.kind == 1) {
+        cudaFuncSetAttribute(k_ring32_blu, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        GLG_LAUNCH_SCOPE("k_ring32_blu", st);
+        k_ring32_blu<<<grid, threads, smem, st>>>(a, e);
+        GLG_CHECK_LAUNCH("k_ring32_blu");
+    } else {
+        cudaFuncSetAttribute(k_ring32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        GLG_LAUNCH_SCOPE("k_ring32", st);
+        k_ring32<<<grid, threads, smem, st>>>(a, e);
+        GLG_CHECK_LAUNCH("k_ring32");
+    }
+    return GLG_OK;
+}
+
+int glg_launch_ring_syn_f32(const glg_plan *P, const float2 *F, float2 *Ft, int nmaps, float *maps,
+                            const glg_epilogue *epi_in, cudaStream_t st) {
+    if (nmaps > EPI_MAX) {
+        glg_set_error("fast ring FFT: at most 40 maps per call");
+        return GLG_ERR_UNSUPPORTED;
+    }
+    const int nm = P->mmax + 1, nr = P->nrings;
+    for (int b = 0; b < P->nbuckets; ++b)
+        if (P->buckets[b].smem > 227 * 1024) {
+            glg_set_error("fast ring FFT: ring length too large for shared memory (nside <= 2048)");
+            return GLG_ERR_UNSUPPORTED;
+        }
+    {
+        dim3 grid((nr + 31) / 32, (nm + 31) / 32, nmaps);
+        GLG_LAUNCH_SCOPE("k_transpose32", st);
+        k_transpose32<<<grid, dim3(32, 8), 0, st>>>(F, Ft, nm, nr);
+        GLG_CHECK_LAUNCH("k_transpose32");
+    }
+    RingArgs a;
+    ring_args(P, Ft, nmaps, maps, a);
     Epi32 e;
     for (int k = 0; k < EPI_MAX; ++k) {
         const bool on = epi_in && k < nmaps;
@@ -523,20 +546,26 @@ int glg_launch_ring_syn_f32(const glg_plan *P, const float2 *F, float2 *Ft, int 
         e.lam[k] = (on && epi_in->lamda) ? (float)epi_in->lamda[k] : 1.f;
     }
     for (int b = 0; b < P->nbuckets; ++b) {
-        const glg_ring_bucket &B = P->buckets[b];
-        a.pairs = P->bucket_pairs + B.first;
-        const unsigned grid = (unsigned)B.count * (unsigned)nmaps;
-        if (B.kind == 1) {
-            cudaFuncSetAttribute(k_ring32_blu, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)B.smem);
-            GLG_LAUNCH_SCOPE("k_ring32_blu", st);
-            k_ring32_blu<<<grid, B.threads, B.smem, st>>>(a, e);
-            GLG_CHECK_LAUNCH("k_ring32_blu");
-        } else {
-            cudaFuncSetAttribute(k_ring32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)B.smem);
-            GLG_LAUNCH_SCOPE("k_ring32", st);
-            k_ring32<<<grid, B.threads, B.smem, st>>>(a, e);
-            GLG_CHECK_LAUNCH("k_ring32");
-        }
+        const int rc = launch_bucket(P, P->buckets[b], P->buckets[b].threads, a, e, st);
+        if (rc) return rc;
     }
     return GLG_OK;
+}
+
+int glg_launch_ring_bucket_f32(const glg_plan *P, int bucket, int threads, const float2 *Ft, int nmaps,
+                               float *maps, cudaStream_t st) {
+    const glg_ring_bucket &B = P->buckets[bucket];
+    if (glg_ring32_smem(B.kind, B.size, threads, B.fold != 0) > 227 * 1024) {
+        glg_set_error("fast ring FFT: block size does not fit shared memory");
+        return GLG_ERR_UNSUPPORTED;
+    }
+    RingArgs a;
+    ring_args(P, Ft, nmaps, maps, a);
+    Epi32 e;
+    for (int k = 0; k < EPI_MAX; ++k) {
+        e.kind[k] = GLG_EPI_NONE;
+        e.hvar[k] = 0.f;
+        e.lam[k] = 1.f;
+    }
+    return launch_bucket(P, B, threads, a, e, st);
 }

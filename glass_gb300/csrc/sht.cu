@@ -131,3 +131,65 @@ extern "C" int glg_map2alm(const glg_plan *P, const void *maps, int nmaps, int n
     }
     return GLG_OK;
 }
+
+// Autotuner of the fast form's ring FFTs: each size bucket is timed at
+// 128, 256 and 512 threads per block (where its shared memory fits) on the
+// caller's workspace and output, and the fastest is kept in the plan.
+extern "C" int glg_autotune_fast(glg_plan *P, int nmaps, void *maps, void *ws, size_t ws_bytes, void *stream) {
+    GLG_REQUIRE(P != nullptr, "glg_autotune_fast: null plan");
+    GLG_REQUIRE(nmaps >= 1 && nmaps <= 40, "glg_autotune_fast: nmaps must be in [1, 40]");
+    GLG_REQUIRE(maps && ws && ws_bytes >= glg_alm2map_workspace(P, nmaps, GLG_FORM_FAST),
+                "glg_autotune_fast: workspace too small");
+    cudaStream_t st = (cudaStream_t)stream;
+    int rc = glg_plan_prepare_fast(P, st);
+    if (rc) return rc;
+    const size_t fbytes = sizeof(float2) * (size_t)nmaps * P->nrings * (P->mmax + 1);
+    float2 *Ft = (float2 *)((char *)ws + GLG_WS_STATUS_BYTES + fast_pack_bytes(P, nmaps) + fbytes);
+    cudaError_t e = cudaMemsetAsync(Ft, 0, fbytes, st);
+    if (e != cudaSuccess) return glg_cuda_status(e, "glg_autotune_fast");
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    for (int k = 0; k < P->nbuckets; ++k) {
+        int best = P->buckets[k].threads;
+        float best_ms = 1e30f;
+        for (int threads : {128, 256, 512}) {
+            if (glg_ring32_smem(P->buckets[k].kind, P->buckets[k].size, threads, P->buckets[k].fold != 0) >
+                227 * 1024)
+                continue;
+            if ((rc = glg_launch_ring_bucket_f32(P, k, threads, Ft, nmaps, (float *)maps, st))) break;
+            cudaEventRecord(a, st);
+            for (int r = 0; r < 2 && !rc; ++r) rc = glg_launch_ring_bucket_f32(P, k, threads, Ft, nmaps, (float *)maps, st);
+            cudaEventRecord(b, st);
+            if (rc) break;
+            e = cudaEventSynchronize(b);
+            if (e != cudaSuccess) break;
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, a, b);
+            if (ms < best_ms) {
+                best_ms = ms;
+                best = threads;
+            }
+        }
+        if (rc || e != cudaSuccess) break;
+        P->buckets[k].threads = best;
+        P->buckets[k].smem = glg_ring32_smem(P->buckets[k].kind, P->buckets[k].size, best, P->buckets[k].fold != 0);
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (rc) return rc;
+    if (e != cudaSuccess) return glg_cuda_status(e, "glg_autotune_fast");
+    return GLG_OK;
+}
+
+extern "C" int glg_plan_buckets(const glg_plan *P, int *out, int max_buckets) {
+    GLG_REQUIRE(P != nullptr && out != nullptr, "glg_plan_buckets: null pointer");
+    int n = 0;
+    for (; n < P->nbuckets && n < max_buckets; ++n) {
+        out[4 * n + 0] = P->buckets[n].kind;
+        out[4 * n + 1] = P->buckets[n].size;
+        out[4 * n + 2] = P->buckets[n].count;
+        out[4 * n + 3] = P->buckets[n].threads;
+    }
+    return n;
+}

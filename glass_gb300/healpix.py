@@ -15,6 +15,7 @@ from __future__ import annotations
 
 import ctypes
 import math
+import os
 import warnings
 from collections.abc import Sequence
 
@@ -122,6 +123,28 @@ def synth(alm: torch.Tensor, nside: int, lmax: int, *, epilogue=None, form: str 
     return maps
 
 
+def autotune(plan, nmaps: int, maps: torch.Tensor, ws: torch.Tensor) -> None:
+    """Pick the ring-FFT block sizes of ``plan`` by timing (glg_autotune_fast).
+
+    Runs once per plan (on its first fast transform) unless the environment
+    sets ``GLASS_GB300_AUTOTUNE=0``; ``buckets`` reports the choice."""
+    if getattr(plan, "tuned", False) or os.environ.get("GLASS_GB300_AUTOTUNE", "1") == "0":
+        return
+    check(lib().glg_autotune_fast(plan.handle, nmaps, c_p(ptr(maps)), c_p(ptr(ws)), ws.numel(),
+                                  c_p(stream_ptr(maps.device))), "glg_autotune_fast")
+    plan.tuned = True
+
+
+def buckets(nside: int, lmax: int) -> list[dict]:
+    """The fast-form ring-FFT launch buckets of a plan: kind (0 mixed radix,
+    1 Bluestein), transform size, ring pairs and threads per block."""
+    plan = get_plan(nside, lmax)
+    out = (ctypes.c_int * (4 * 64))()
+    n = lib().glg_plan_buckets(plan.handle, out, 64)
+    return [dict(kind=out[4 * i], size=out[4 * i + 1], pairs=out[4 * i + 2], threads=out[4 * i + 3])
+            for i in range(n)]
+
+
 def _synth_fast(alm: torch.Tensor, nside: int, lmax: int, epilogue) -> torch.Tensor:
     plan = get_plan(nside, lmax, alm.device)
     alm = alm.to(torch.complex64).contiguous()
@@ -131,6 +154,7 @@ def _synth_fast(alm: torch.Tensor, nside: int, lmax: int, epilogue) -> torch.Ten
     ws_bytes = int(lib().glg_alm2map_workspace(plan.handle, step, _lib.FORM_FAST))
     ws = torch.empty(ws_bytes, dtype=torch.uint8, device=alm.device)
     stream = c_p(stream_ptr(alm.device))
+    autotune(plan, step, maps[:step], ws)
     for m0 in range(0, nmaps, step):
         cnt = min(step, nmaps - m0)
         epi = None

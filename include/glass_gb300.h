@@ -126,6 +126,20 @@ int glg_almxfl(const void *alm, const double *fl, int nfl, int lmax, int nmaps, 
                void *out, void *stream);
 
 /*
+ * Autotuner of the fast form (no counterpart in the reference, whose
+ * transforms are healpy's): times every ring-FFT size bucket of the plan at
+ * 128, 256 and 512 threads per block on the given workspace (sized by
+ * glg_alm2map_workspace for nmaps, GLG_FORM_FAST) and float32 output maps
+ * [nmaps][npix] (overwritten), and keeps the fastest in the plan.  Builds the
+ * fast-form tables on first use; synchronises the stream.
+ */
+int glg_autotune_fast(glg_plan *plan, int nmaps, void *maps, void *ws, size_t ws_bytes, void *stream);
+
+/* Ring-FFT launch buckets of a plan: (kind, size, ring pairs, threads) per
+ * bucket into out[4 * max_buckets]; returns the number written. */
+int glg_plan_buckets(const glg_plan *plan, int *out, int max_buckets);
+
+/*
  * One step of the multi-plane convergence recurrence, replacing
  * glass/lensing.py:577-581 (MultiPlaneConvergence.add_plane):
  *   kappa3 <- kappa3 * (1 - t);  kappa3 += t * kappa2;  kappa3 += f * delta2
