@@ -129,9 +129,14 @@ __host__ __device__ inline int glg_fft32_radices(int n, int *r) {
     return n == 1 ? k : -1;
 }
 
-// Shared-memory index of complex element e of a ring FFT buffer: one spare
-// slot per 16 values keeps every power-of-two stride free of bank conflicts.
-__host__ __device__ inline int glg_zi(int e) { return e + (e >> 4); }
+// Shared-memory index of complex element e of a ring FFT buffer: a spare
+// slot per 16, per 256 and per 4096 values makes the strides 1, 16, 256 and
+// 4096 of the radix-16 passes and of the digit-reversed output gather odd in
+// slots, so none of them repeats a bank within a warp.
+__host__ __device__ inline int glg_zi(int e) { return e + (e >> 4) + (e >> 8) + (e >> 12); }
+
+// Slots of a padded buffer of `cnt` complex values.
+__host__ __device__ inline int glg_zsize(int cnt) { return glg_zi(cnt - 1) + 1; }
 
 // Dynamic shared memory of one ring FFT block: the padded transform buffer
 // of length n (kind 0) or M (kind 1), a second padded buffer for the south

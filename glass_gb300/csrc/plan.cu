@@ -350,7 +350,7 @@ __global__ void k_plan_tfirst(int lmax, int npairs, int ntiles, const int *__res
 // H = DFT_M(h), h_t = e^{-i pi t^2 / n} for |t| < n (indices mod M), stored
 // in the DIF output order of M.
 size_t glg_ring32_smem(int kind, int n_or_M, int threads, bool fold) {
-    const size_t zs = (size_t)n_or_M + n_or_M / 16 + 1;
+    const size_t zs = (size_t)glg_zsize(n_or_M);
     size_t slots = zs + 2 * (size_t)threads + glg_zi(n_or_M / 2) + 1;
     if (kind == 0 && fold) slots += zs;
     return slots * sizeof(float2);

@@ -24,8 +24,9 @@
 // power-of-two length M >= 2n - 1 with the chirp h_t = e^{-i pi t^2 / n},
 // computed as a forward DIF FFT, a product with the chirp spectrum (stored in
 // DIF output order) and the adjoint of the DIF FFT, so no permutation pass is
-// needed.  Shared-memory buffers are padded one slot per 16 values
-// (glg_zi) so that every power-of-two stride is free of bank conflicts.
+// needed.  Shared-memory buffers are padded (glg_zi) so that the strides of
+// the passes and of the digit-reversed output gather are free of bank
+// conflicts.
 //
 // Rings are launched in size buckets built with the plan (one launch per
 // bucket, all maps of the call in one grid with the map index fastest, so the
@@ -391,7 +392,7 @@ __global__ void __launch_bounds__(TMAX) k_ring32(const RingArgs a, const Epi32 e
     const int p = a.pairs[blockIdx.x / a.nmaps];
     const int n = a.nph[p], i4 = n / 4, T = blockDim.x;
     const bool folds = n <= a.mmax;
-    const int zs = n + n / 16 + 1;
+    const int zs = glg_zsize(n);
     c32 *Z = reinterpret_cast<c32 *>(smem_raw);
     c32 *SS = Z + zs;
     c32 *X = SS + (folds ? zs : 0);
@@ -425,7 +426,7 @@ __global__ void __launch_bounds__(TMAX) k_ring32_blu(const RingArgs a, const Epi
     const int n = a.nph[p], i4 = n / 4, T = blockDim.x;
     const int M = a.blu_M[i4];
     c32 *Z = reinterpret_cast<c32 *>(smem_raw);
-    c32 *X = Z + (M + M / 16 + 1);
+    c32 *X = Z + glg_zsize(M);
     c32 *wh = X + 2 * T;
     const int stride = a.Mmax / M;
     for (int t = threadIdx.x; t <= M / 2; t += T) wh[zi(t)] = ldg(a.twM + (int64_t)t * stride);

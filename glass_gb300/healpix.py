@@ -26,6 +26,7 @@ from . import _lib
 from ._lib import c_p, check, get_plan, lib, ptr, stream_ptr
 
 __all__ = [
+    "SynthGraph",
     "alm2map",
     "ang2pix",
     "alm2map_spin",
@@ -167,6 +168,58 @@ def _synth_fast(alm: torch.Tensor, nside: int, lmax: int, epilogue) -> torch.Ten
                                 c_p(ptr(ws)), ws_bytes, stream), "glg_alm2map (fast)")
     check(lib().glg_workspace_status(c_p(ptr(ws)), stream), "glg_alm2map (fast)")
     return maps
+
+
+class SynthGraph:
+    """A fast-form synthesis captured once into a CUDA graph and replayed.
+
+    Static buffers: ``alm`` (complex64 [nmaps, nalm], HEALPix order) and
+    ``maps`` (float32 [nmaps, npix]); the epilogue (kinds, variances, shifts)
+    is fixed at capture.  ``__call__(alm)`` copies its argument into the
+    static input (or pass ``None`` after writing ``self.alm`` in place),
+    replays the ~25 launches of the transform (B packing, tensor-core
+    contraction, transpose, one launch per ring-FFT size bucket) as one graph
+    launch and returns ``self.maps`` (overwritten by the next replay).
+    """
+
+    def __init__(self, nside: int, lmax: int, nmaps: int, *, epilogue=None,
+                 device: torch.device | None = None):
+        if not 1 <= nmaps <= FAST_MAX_MAPS:
+            raise ValueError(f"nmaps must be in [1, {FAST_MAX_MAPS}]")
+        device = torch.device("cuda", torch.cuda.current_device()) if device is None else device
+        self.plan = get_plan(nside, lmax, device)
+        self.nside, self.lmax, self.nmaps = nside, lmax, nmaps
+        self.alm = torch.zeros((nmaps, self.plan.nalm), dtype=torch.complex64, device=device)
+        self.maps = torch.empty((nmaps, self.plan.npix), dtype=torch.float32, device=device)
+        ws_bytes = int(lib().glg_alm2map_workspace(self.plan.handle, nmaps, _lib.FORM_FAST))
+        self.ws = torch.empty(ws_bytes, dtype=torch.uint8, device=device)
+        self._epi = _make_epilogue(epilogue, nmaps) if epilogue is not None else None
+        side = torch.cuda.Stream(device)
+        side.wait_stream(torch.cuda.current_stream(device))
+        with torch.cuda.stream(side):
+            autotune(self.plan, nmaps, self.maps, self.ws)
+            self._launch()  # builds the fast tables outside the capture
+            torch.cuda.current_stream(device).synchronize()
+            self.graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(self.graph, stream=side):
+                self._launch()
+        torch.cuda.current_stream(device).wait_stream(side)
+
+    def _launch(self) -> None:
+        epi = ctypes.byref(self._epi) if self._epi is not None else None
+        check(lib().glg_alm2map(self.plan.handle, c_p(ptr(self.alm)), self.nmaps, _lib.FORM_FAST,
+                                c_p(ptr(self.maps)), epi, c_p(ptr(self.ws)), self.ws.numel(),
+                                c_p(stream_ptr(self.alm.device))), "glg_alm2map (graph)")
+
+    def __call__(self, alm=None) -> torch.Tensor:
+        if alm is not None:
+            self.alm.copy_(torch.as_tensor(alm).reshape(self.alm.shape))
+        self.graph.replay()
+        return self.maps
+
+    def status(self) -> None:
+        """Raise if a bounded device wait of the last replay timed out."""
+        check(lib().glg_workspace_status(c_p(ptr(self.ws)), c_p(stream_ptr(self.alm.device))), "SynthGraph")
 
 
 def _make_epilogue(epilogue, nmaps):

@@ -431,3 +431,38 @@ def test_galaxy_shear_vs_reference(g, lensing_golden, reduced):
                          gd["shear_g2"], reduced_shear=reduced)
     assert got.dtype == np.complex128
     np.testing.assert_allclose(got, gd[f"shear_{int(reduced)}"], rtol=1e-15, atol=0)
+
+
+def test_autotuner_picks_block_sizes(g):
+    """The first fast transform of a plan times every ring-FFT bucket and
+    keeps a block size per bucket; results stay within the fast tolerance."""
+    import torch
+
+    from glass_gb300 import healpix as hp
+
+    nside, lmax = 64, 150
+    ell = np.concatenate([np.arange(m, lmax + 1) for m in range(lmax + 1)])
+    alm = random_alm(lmax, seed=3, nmaps=5) * (ell + 1.0) ** -0.65
+    got = hp.synth(torch.as_tensor(alm, device="cuda").to(torch.complex64), nside, lmax, form="fast")
+    b = hp.buckets(nside, lmax)
+    assert b and all(x["threads"] in (128, 256, 512) for x in b)
+    assert sum(x["pairs"] for x in b) == 2 * nside
+    assert rel_rms(got.cpu().numpy(), osht.alm2map(alm, nside, lmax)) < FAST_RMS
+
+
+def test_synth_graph_replays_equal_direct_calls(g):
+    """A captured fast synthesis replays to the same maps as direct calls,
+    for new inputs written into its static buffer, with a fused epilogue."""
+    import torch
+
+    from glass_gb300 import healpix as hp
+
+    nside, lmax, nm = 32, 64, 3
+    epi = ([g._lib.EPI_LOGNORMAL, g._lib.EPI_NONE, g._lib.EPI_LOGNORMAL], [0.2, 0.0, 0.5], [1.0, 1.0, 2.0])
+    graph = hp.SynthGraph(nside, lmax, nm, epilogue=epi)
+    for seed in (1, 2):
+        alm = torch.as_tensor(random_alm(lmax, seed=seed, nmaps=nm) * 0.1, device="cuda").to(torch.complex64)
+        got = graph(alm).clone()
+        graph.status()
+        ref = hp.synth(alm, nside, lmax, epilogue=epi, form="fast")
+        torch.testing.assert_close(got, ref, rtol=0, atol=0)
