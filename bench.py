@@ -210,11 +210,60 @@ def measured_peaks() -> dict:
 
 
 def tf32_peak_tflops(peaks: dict) -> tuple[float, str]:
-    """Dense TF32 tensor peak: half the measured dense bf16 rate (same tensor
-    pipe, tf32 issues at half the bf16 rate on this generation)."""
+    """Dense TF32 tensor peak: the tcgen05 kind::tf32 rate measured by
+    ``bench.py --peaks`` (kept in peaks_tf32_fp64.json), else half the
+    measured dense bf16 rate (same tensor pipe, tf32 at half the bf16 rate)."""
+    p = ROOT / "peaks_tf32_fp64.json"
+    if p.exists():
+        return float(json.loads(p.read_text())["tf32_tflops"]), "tf32 tcgen05 loop (of measured)"
     bf = peaks.get("bf16_tflops", 1900.0)
     tag = "of measured" if "fallback" not in peaks else "of fallback"
     return bf / 2.0, f"tf32 = bf16_tflops/2 ({tag})"
+
+
+def measure_compute_peaks() -> dict:
+    """TF32 tensor, FP32 and FP64 FMA rates of this GPU (the denominators the
+    copy and bf16 GEMM figures do not give), with CUDA events, best of 5."""
+    import ctypes
+
+    import torch
+
+    from glass_gb300 import _lib
+
+    lib = _lib.lib()
+    st = torch.cuda.current_stream()
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+
+    def best(launch, reps=5):
+        launch()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            launch()
+            e1.record(st)
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1) * 1e-3)
+        return min(ts)
+
+    sp = ctypes.c_void_p(st.cuda_stream)
+    iters = 40_000
+    t = best(lambda: _lib.check(lib.glg_peak_tf32(sms, iters, ctypes.c_void_p(err.data_ptr()), sp), "glg_peak_tf32"))
+    if int(err.item()) != 0:
+        raise RuntimeError("glg_peak_tf32: a completion wait ran out")
+    tf32 = sms * iters * 2.0 * 128 * 256 * 8 / t / 1e12
+    out = {"tf32_tflops": round(tf32, 1), "tf32_how": f"{sms} CTAs x {iters} tcgen05.mma kind::tf32 M128 N256 K8"}
+    for name, dt, dtype, it in (("fp32", torch.float32, _lib.GLG_F32, 16384), ("fp64", torch.float64, _lib.GLG_F64, 2048)):
+        blocks = sms * 8
+        sink = torch.zeros(blocks, dtype=dt, device="cuda")
+        t = best(lambda: _lib.check(lib.glg_peak_fma(dtype, blocks, it, ctypes.c_void_p(sink.data_ptr()), sp),
+                                    "glg_peak_fma"))
+        out[f"{name}_tflops"] = round(blocks * 256 * it * 16.0 / t / 1e12, 2)
+    out["fma_how"] = f"{sms * 8} blocks x 256 threads x 8 chains of FMA (2 flop each)"
+    out["gpu_name"] = torch.cuda.get_device_name(0)
+    return out
 
 
 # ------------------------------------------------------------------- ours
@@ -390,14 +439,26 @@ def run_reference(args, rank: int, world: int) -> dict | None:
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
-def ncu_case() -> None:
-    """Small profiling case (no JSON): two fast `generate` calls of 8
+def ncu_case(which: str) -> None:
+    """Small profiling cases (no JSON).  "sht": two fast `generate` calls of 8
     lognormal shells of the serving spectra at nside 1024, lmax 2048 (the
-    Legendre sums, 0.54 GB, exceed L2); profilers capture the first call."""
+    Legendre sums, 0.54 GB, exceed L2); profilers capture the first call.
+    "alm": the correlated alm of the benchmark's 40 shells at lmax 4096 in the
+    fast form (2.7 GB written, no transform), twice."""
     import torch
 
     import glass_gb300 as g
 
+    if which == "alm":
+        from glass_gb300 import fields
+
+        gls = [torch.as_tensor(c, device="cuda") for c in spectra_cfg3(40, 4096)[0]]
+        b = fields._FieldBatcher(gls, 2048, None, g.rng.Generator(42), "fast")
+        for _ in range(2):
+            alm = b.alm(0, 40)
+            torch.cuda.synchronize()
+        print("ncu case done", float(alm.abs().max()))
+        return
     gls, lam = spectra_cfg2(8, 2048, seed=1)
     gls = [torch.as_tensor(c, device="cuda") for c in gls]
     fields = [g.grf.Lognormal(float(x)) for x in lam]
@@ -423,10 +484,15 @@ def main() -> None:
     ap.add_argument("--serving-plain", type=int, default=60,
                     help="requests of the FP64 unbatched serving comparison (0: off)")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
-    ap.add_argument("--ncu-case", action="store_true", help="run the small profiling case and exit")
+    ap.add_argument("--ncu-case", nargs="?", const="sht", choices=["sht", "alm"],
+                    help="run a small profiling case and exit")
+    ap.add_argument("--peaks", action="store_true", help="measure the TF32 / FP32 / FP64 peak rates and exit")
     args = ap.parse_args()
     if args.ncu_case:
-        ncu_case()
+        ncu_case(args.ncu_case)
+        return
+    if args.peaks:
+        print(json.dumps(measure_compute_peaks()))
         return
 
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -66,12 +66,15 @@ _SIGNATURES = {
     "glg_convergence_step": ([c_p, c_p, c_p, c_i, c_i64, ctypes.c_double, ctypes.c_double, c_p], c_i),
     "glg_ang2pix": ([c_i, c_p, c_p, c_i64, c_i, c_p, c_p], c_i),
     "glg_galaxy_shear": ([c_p, c_p, c_p, c_i64, c_p, c_p, c_p, c_i, c_i, c_i, c_p, c_p], c_i),
+    "glg_positions": ([c_i, c_p, c_i64, c_i64, c_u64, c_u64, c_p, c_p, c_p, c_p], c_i),
     "glg_poisson_counts": ([c_p, c_i, c_i64, ctypes.c_double, ctypes.c_double, ctypes.c_double, c_p,
                             c_u64, c_u64, c_p, c_p], c_i),
     "glg_alm2map_workspace": ([c_p, c_i, c_i], c_sz),
     "glg_alm2map": ([c_p, c_p, c_i, c_i, c_p, ctypes.POINTER(Epilogue), c_p, c_sz, c_p], c_i),
     "glg_workspace_status": ([c_p, c_p], c_i),
     "glg_alm2map_noalloc": ([c_i, c_i, c_p, c_i, c_p, c_p], c_i),
+    "glg_peak_tf32": ([c_i, c_i, c_p, c_p], c_i),
+    "glg_peak_fma": ([c_i, c_i, c_i, c_p, c_p], c_i),
     "glg_alm2map_spin_workspace": ([c_p], c_sz),
     "glg_alm2map_spin": ([c_p, c_p, c_p, c_i, c_p, c_p, c_p, c_sz, c_p], c_i),
     "glg_map2alm_workspace": ([c_p, c_i], c_sz),

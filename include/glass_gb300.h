@@ -171,6 +171,20 @@ int glg_galaxy_shear(const double *lon, const double *lat, const void *eps, int6
                      void *out, void *stream);
 
 /*
+ * Positions of counted galaxies inside their pixels, replacing the
+ * healpy.randang sampling of glass/points.py:351-440 (positions_from_delta):
+ * galaxy g (first <= g < first + n) belongs to the RING pixel p with
+ * offsets[p] <= g < offsets[p+1] (offsets: int64 exclusive prefix sums of
+ * the counts, [12 nside^2]); its position is uniform on the pixel's area,
+ * from the Philox stream (key seed, stream sid < 2^32, counter g).  lon in
+ * [0, 360) and lat in degrees, float64 [n].  misses: one uint64 of device
+ * memory counting galaxies whose 64 draws all fell outside the pixel (left
+ * at the pixel centre; none expected).
+ */
+int glg_positions(int nside, const int64_t *offsets, int64_t first, int64_t n, uint64_t seed, uint64_t sid,
+                  double *lon, double *lat, unsigned long long *misses, void *stream);
+
+/*
  * Per-pixel Poisson galaxy counts, replacing glass/points.py:252-348
  * (_compute_expected_count, _apply_visibility, _sample_number_galaxies):
  *   n_e = ((bias * delta_e - offset) + 1) * scale  [* vis_e],  clipped at 0,
@@ -265,6 +279,19 @@ int glg_timing_enable(int on);
 int glg_timing_reset(void);
 int64_t glg_launch_count(void);
 int glg_timing_query(const char *kernel, double *total_ms, int64_t *launches);
+
+/*
+ * Peak-rate kernels (measurement utilities, no counterpart in the
+ * reference): glg_peak_tf32 runs `ctas` CTAs (one per SM), each issuing
+ * `iters` tcgen05.mma kind::tf32 of M = 128, N = 256, K = 8 (2 * 128 * 256 * 8
+ * flop each) and sets *err to 1 if a completion wait ran out; glg_peak_fma
+ * runs `blocks` x 256 threads of 8 independent FMA chains of `iters` steps
+ * (16 * iters flop per thread) in FP64 (dtype GLG_F64) or FP32 (GLG_F32),
+ * `sink` a device buffer of `blocks` elements of that type.  Time them with
+ * CUDA events on `stream`.
+ */
+int glg_peak_tf32(int ctas, int iters, unsigned int *err, void *stream);
+int glg_peak_fma(int dtype, int blocks, int iters, void *sink, void *stream);
 
 #ifdef __cplusplus
 }

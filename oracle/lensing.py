@@ -8,7 +8,10 @@ numpy restatements, in the reference's own operation order, of
   healpy.ang2pix is what glass/healpix.py calls; healpy itself is not
   installed here, so the pixelisation is pinned by its published formulas,
   pix2ang round trips and known pixels),
-* ``galaxy_shear`` (glass/galaxies.py:271-347) on top of it.
+* ``galaxy_shear`` (glass/galaxies.py:271-347) on top of it,
+* the pixel geometry behind sampling positions inside pixels (the
+  healpy.randang step of glass/points.py:426-430): ring, position in the
+  ring and the (z, phi) box that holds each RING pixel.
 """
 
 from __future__ import annotations
@@ -120,3 +123,69 @@ class MultiPlaneConvergence:
     @property
     def kappa(self):
         return self.kappa3
+
+
+def ring_z(nside: int, r):
+    """z = cos(theta) of the centres of ring r (1 .. 4 nside - 1)."""
+    r = np.asarray(r, dtype=np.int64)
+    ns = float(nside)
+    q = 4 * nside - r
+    return np.where(r < nside, 1.0 - (r * r) / (3.0 * ns * ns),
+                    np.where(r <= 3 * nside, 4.0 / 3.0 - 2.0 * r / (3.0 * ns), (q * q) / (3.0 * ns * ns) - 1.0))
+
+
+def pix_ring(nside: int, p):
+    """(ring r, position j in the ring, ring length) of RING pixels p."""
+    p = np.asarray(p, dtype=np.int64)
+    ncap = 2 * nside * (nside - 1)
+    npix = 12 * nside * nside
+    r = np.empty_like(p)
+    j = np.empty_like(p)
+    nph = np.empty_like(p)
+    a = p < ncap
+    r[a] = (1 + np.floor(np.sqrt(1.0 + 2.0 * p[a])).astype(np.int64)) // 2
+    j[a] = p[a] - 2 * r[a] * (r[a] - 1)
+    nph[a] = 4 * r[a]
+    b = (p >= ncap) & (p < npix - ncap)
+    q = p[b] - ncap
+    r[b] = q // (4 * nside) + nside
+    j[b] = q % (4 * nside)
+    nph[b] = 4 * nside
+    c = p >= npix - ncap
+    q = npix - 1 - p[c]
+    rs = (1 + np.floor(np.sqrt(1.0 + 2.0 * q)).astype(np.int64)) // 2
+    r[c] = 4 * nside - rs
+    nph[c] = 4 * rs
+    j[c] = nph[c] - 1 - (q - 2 * rs * (rs - 1))
+    return r, j, nph
+
+
+def pixel_box(nside: int, p):
+    """(zlo, zhi, phi centre, phi width) of the box that holds RING pixel p.
+
+    A pixel of ring r lies between the centres of rings r+1 and r-1 in z and
+    within half a pixel width of its centre in phi; it fills half the box.
+    """
+    r, j, nph = pix_ring(nside, p)
+    zhi = np.where(r == 1, 1.0, ring_z(nside, np.maximum(r - 1, 1)))
+    zlo = np.where(r == 4 * nside - 1, -1.0, ring_z(nside, np.minimum(r + 1, 4 * nside - 1)))
+    shifted = (r < nside) | (r > 3 * nside) | (((r - nside) & 1) == 0)
+    dphi = 2 * np.pi / nph
+    return zlo, zhi, (j + np.where(shifted, 0.5, 0.0)) * dphi, dphi
+
+
+def randang_lonlat(nside: int, ipix, rng) -> tuple[np.ndarray, np.ndarray]:
+    """Uniform positions inside RING pixels ipix by rejection from pixel_box."""
+    ipix = np.asarray(ipix, dtype=np.int64)
+    zlo, zhi, phic, dphi = pixel_box(nside, ipix)
+    z = np.empty(ipix.shape)
+    phi = np.empty(ipix.shape)
+    todo = np.arange(ipix.size)
+    while todo.size:
+        zz = zlo[todo] + rng.random(todo.size) * (zhi[todo] - zlo[todo])
+        pp = phic[todo] + (rng.random(todo.size) - 0.5) * dphi[todo]
+        ok = ang2pix_ring(nside, np.arccos(zz), pp) == ipix[todo]
+        z[todo[ok]] = zz[ok]
+        phi[todo[ok]] = pp[ok]
+        todo = todo[~ok]
+    return np.degrees(np.mod(phi, 2 * np.pi)), np.degrees(np.arcsin(z))

@@ -433,6 +433,103 @@ def test_galaxy_shear_vs_reference(g, lensing_golden, reduced):
     np.testing.assert_allclose(got, gd[f"shear_{int(reduced)}"], rtol=1e-15, atol=0)
 
 
+def test_positions_in_their_pixels_vs_oracle(g):
+    """positions_from_delta (glass/points.py:443-540): every position lies in
+    its pixel (pixels in order, as many as the Poisson count), batches end at
+    pixel boundaries, positions do not depend on the batch size, and inside
+    the pixels they follow the oracle's uniform sampler (two-sample KS)."""
+    import torch
+    from scipy import stats
+
+    import oracle.lensing as olens
+
+    nside = 64
+    npix = 12 * nside * nside
+    rng = np.random.default_rng(4)
+    delta = np.exp(rng.normal(0.0, 0.8, npix) - 0.32) - 1.0
+    delta[:100] = -1.0  # empty pixels
+    ngal = 20.0 * npix / g.points.ARCMIN2_SPHERE
+    out = list(g.points.positions_from_delta(ngal, torch.as_tensor(delta, device="cuda"), 1.1, batch=100_000,
+                                             rng=g.rng.Generator(9)))
+    counts = g.points.counts_from_delta(ngal, delta, 1.1, rng=g.points._Keyed(9, 0))
+    lon = torch.cat([b[0] for b in out]).cpu().numpy()
+    lat = torch.cat([b[1] for b in out]).cpu().numpy()
+    sizes = np.array([b[2] for b in out])
+    assert sizes.sum() == counts.sum() == lon.size and np.all(sizes <= 100_000)
+    assert np.all(np.isin(np.cumsum(sizes), np.cumsum(counts)))  # batches end at pixel boundaries
+    ipix = np.repeat(np.arange(npix), counts)
+    np.testing.assert_array_equal(olens.ang2pix_lonlat(nside, lon, lat), ipix)
+    assert lon.min() >= 0 and lon.max() < 360 and lat.min() >= -90 and lat.max() <= 90
+    # the galaxy's counter, not its batch, keys its draws
+    again = list(g.points.positions_from_delta(ngal, delta, 1.1, batch=7_777, rng=g.rng.Generator(9)))
+    np.testing.assert_array_equal(np.concatenate([b[0] for b in again]), lon)
+    np.testing.assert_array_equal(np.concatenate([b[1] for b in again]), lat)
+    # distribution within the pixels: position in the pixel's box vs the oracle sampler
+    lon_o, lat_o = olens.randang_lonlat(nside, ipix, np.random.default_rng(1))
+    zlo, zhi, phic, dphi = olens.pixel_box(nside, ipix)
+
+    def box_coords(lo, la):
+        z = np.sin(np.radians(la))
+        dp = np.mod(np.radians(lo) - phic + np.pi, 2 * np.pi) - np.pi
+        return (z - zlo) / (zhi - zlo), dp / dphi
+
+    u, v = box_coords(lon, lat)
+    uo, vo = box_coords(lon_o, lat_o)
+    assert np.all((u >= 0) & (u <= 1) & (np.abs(v) <= 0.5))
+    assert stats.ks_2samp(u, uo).pvalue > 1e-4
+    assert stats.ks_2samp(v, vo).pvalue > 1e-4
+
+
+def test_positions_from_delta_reference_cases(g):
+    """The cases of the reference's test_positions_from_delta: scalar and
+    broadcast populations, count shapes, negative delta, no vis, the
+    TypeError, and numpy in / numpy out."""
+    import torch
+
+    import oracle.lensing as olens
+
+    def cat(gen):
+        lon, lat, cnt = [], [], 0
+        for a, b, c in gen:
+            lon.append(np.asarray(a.cpu() if isinstance(a, torch.Tensor) else a))
+            lat.append(np.asarray(b.cpu() if isinstance(b, torch.Tensor) else b))
+            cnt = cnt + c
+        return (np.concatenate(lon) if lon else np.zeros(0)), (np.concatenate(lat) if lat else np.zeros(0)), cnt
+
+    pts = g.points
+    nside = 128
+    npix = 12 * nside * nside
+    for kw in ({"bias": 0.8, "vis": np.ones(npix)}, {"bias": None, "vis": np.ones(npix), "bias_model": lambda x: x},
+               {"bias": 0.8, "vis": None}, {"bias": 0.8, "vis": np.ones(npix), "remove_monopole": True}):
+        kw = dict(kw)
+        lon, lat, count = cat(pts.positions_from_delta(1e-3, np.zeros(npix), kw.pop("bias"), kw.pop("vis"), **kw))
+        assert int(count) == count and lon.shape == lat.shape == (count,)
+        assert abs(count - 1e-3 * pts.ARCMIN2_SPHERE) < 6 * np.sqrt(1e-3 * pts.ARCMIN2_SPHERE)
+    lon, lat, count = cat(pts.positions_from_delta(1e-3, np.full(npix, -1.0), None, np.ones(npix)))
+    assert count == 0 and lon.size == 0 and lat.size == 0
+    lon, lat, count = cat(pts.positions_from_delta(1e-3, np.random.default_rng(0).normal(100, 1, npix), 0.8,
+                                                   np.ones(npix)))
+    assert lon.shape == lat.shape == (count,)
+    lon, lat, count = cat(pts.positions_from_delta(np.array([1e-3, 2e-3]), np.zeros(12), 0.8, np.ones(12)))
+    assert count.shape == (2,) and lon.shape == lat.shape == (count.sum(),)
+    assert count[1] > 1.8 * count[0]
+    lon, lat, count = cat(pts.positions_from_delta(1e-3, np.zeros((3, 2, 12)), 0.8, np.ones(12)))
+    assert count.shape == (3, 2) and lon.shape == (count.sum(),)
+    vis = np.ones(12)
+    lon, lat, count = cat(pts.positions_from_delta(np.array([1e-3, 2e-3]), np.zeros((3, 1, 12)), 0.8, vis))
+    assert count.shape == (3, 2) and lon.shape == (count.sum(),)
+    vis[:6] = 0.0  # only the southern hemisphere is visible
+    lon, lat, count = cat(pts.positions_from_delta(np.array([1e-3, 2e-3]), np.zeros((3, 1, 12)), 0.8, vis))
+    assert count.shape == (3, 2) and lon.shape == (count.sum(),)
+    assert olens.ang2pix_lonlat(1, lon, lat).min() >= 6
+    with pytest.raises(TypeError, match="bias_model must be callable"):
+        next(pts.positions_from_delta(1e-3, np.zeros(12), 0.8, vis, bias_model=0))
+    one = next(pts.positions_from_delta(1e-3, np.zeros(12)))
+    assert isinstance(one[0], np.ndarray) and one[0].dtype == np.float64
+    one = next(pts.positions_from_delta(1e-3, torch.zeros(12, device="cuda", dtype=torch.float64)))
+    assert isinstance(one[0], torch.Tensor) and one[0].is_cuda
+
+
 def test_autotuner_picks_block_sizes(g):
     """The first fast transform of a plan times every ring-FFT bucket and
     keeps a block size per bucket; results stay within the fast tolerance."""

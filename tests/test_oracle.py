@@ -227,6 +227,43 @@ def test_ang2pix_ring_pixel_centres_and_offsets():
                                phi + 2 * np.pi * rng.integers(-2, 3, phi.size)), ref)
 
 
+def test_pixel_box_holds_each_pixel():
+    """Ring geometry of RING pixels agrees with the SHT ring table, and the
+    (z, phi) box of a pixel holds every point that ang2pix puts in it; the
+    pixel fills half the box (the acceptance rate of the position sampler)."""
+    import oracle.lensing as olens
+
+    rng = np.random.default_rng(3)
+    for nside in (1, 2, 4, 16, 64):
+        z, _, nph, phi0, start = osht.ring_info(nside)
+        p = np.arange(12 * nside * nside)
+        r, j, n = olens.pix_ring(nside, p)
+        np.testing.assert_array_equal(start[r - 1] + j, p)
+        np.testing.assert_array_equal(nph[r - 1], n)
+        np.testing.assert_allclose(olens.ring_z(nside, r), z[r - 1], rtol=0, atol=1e-15)
+        zlo, zhi, phic, dphi = olens.pixel_box(nside, p)
+        np.testing.assert_allclose(phic, phi0[r - 1] + 2 * np.pi * j / n, rtol=1e-15, atol=1e-15)
+        zz = rng.uniform(-1, 1, 400_000)
+        pp = rng.uniform(0, 2 * np.pi, zz.size)
+        q = olens.ang2pix_ring(nside, np.arccos(zz), pp)
+        zlo, zhi, phic, dphi = olens.pixel_box(nside, q)
+        assert np.all((zz >= zlo) & (zz <= zhi))
+        assert np.all(np.abs(np.mod(pp - phic + np.pi, 2 * np.pi) - np.pi) <= 0.5 * dphi)
+        # a pixel (area 4 pi / npix) fills at least half of its box, and draws
+        # in the box land in the pixel at that rate
+        zlo, zhi, phic, dphi = olens.pixel_box(nside, p)
+        fill = 4 * np.pi / p.size / ((zhi - zlo) * dphi)
+        assert fill.min() > 0.5 - 1e-12 and fill.max() <= 1.0
+        for pix in (0, 6 * nside * nside):
+            zlo, zhi, phic, dphi = olens.pixel_box(nside, np.full(200_000, pix))
+            hit = olens.ang2pix_ring(nside, np.arccos(zlo + rng.random(zlo.size) * (zhi - zlo)),
+                                     phic + (rng.random(zlo.size) - 0.5) * dphi) == pix
+            assert abs(hit.mean() - fill[pix]) < 0.01
+    lon, lat = olens.randang_lonlat(4, np.repeat(np.arange(192), 50), rng)
+    np.testing.assert_array_equal(olens.ang2pix_lonlat(4, lon, lat), np.repeat(np.arange(192), 50))
+    assert lon.min() >= 0 and lon.max() < 360 and lat.min() >= -90 and lat.max() <= 90
+
+
 def test_galaxy_shear_matches_reference(lensing_golden):
     import oracle.lensing as olens
 
