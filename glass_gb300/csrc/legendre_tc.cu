@@ -535,42 +535,61 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
 // Bpack[goff[m] + g] = 4 tiles (E_hi, E_lo, O_hi, O_lo) of N x 8 tf32 values,
 // element (n, k) of a tile at float index (n/8)*64 + (k/4)*32 + (n%8)*4 + k%4,
 // holding the re (n even) or im (n odd) part of a_lm of map n/2 at
-// l = m + 16 g + 2 k + parity.
+// l = m + 16 g + 2 k + parity.  One thread per (group, parity, map, k/4): it
+// loads the 4 alm of its k quad and writes re and im of the hi and lo tiles
+// as 16-byte stores; consecutive threads take consecutive maps and quads, so
+// a warp writes 1 KB of a tile contiguously.
 template <int N>
-__global__ void k_pack_b(int lmax, int nmaps, int64_t nalm, const int64_t *__restrict__ mofs,
-                         const int64_t *__restrict__ goff, const float2 *__restrict__ alm,
-                         float *__restrict__ bpack) {
-    const int m = blockIdx.y;
-    const int G = (lmax - m + GLG_GROUP) / GLG_GROUP;
-    const int64_t mb = mofs[m];
-    for (int g = blockIdx.x; g < G; g += gridDim.x) {
-        float *dst = bpack + (goff[m] + g) * (int64_t)(32 * N);
-        for (int o = threadIdx.x; o < 32 * N; o += blockDim.x) {
-            const int t = o / (8 * N), q = o % (8 * N);
-            const int par = t >> 1, hl = t & 1;
-            const int ng = q / 64, r1 = q % 64, kc = r1 / 32, r2 = r1 % 32;
-            const int n = ng * 8 + r2 / 4, k = kc * 4 + (r2 & 3);
-            const int l = m + g * GLG_GROUP + 2 * k + par;
-            const int map = n >> 1;
-            float v = 0.f;
-            if (l <= lmax && map < nmaps) {
-                const float2 z = alm[(int64_t)map * nalm + mb + (l - m)];
-                v = (n & 1) ? z.y : z.x;
-                if (m == 0 && (n & 1)) v = 0.f;  // imaginary part of a_l0 is ignored
-            }
-            const uint32_t hi = tf32_rna(v);
-            dst[o] = hl ? __uint_as_float(tf32_rna(v - __uint_as_float(hi))) : __uint_as_float(hi);
-        }
+__global__ void __launch_bounds__(256) k_pack_b(int mmax, int lmax, int nmaps, int64_t nalm, int64_t ngroups,
+                                                const int64_t *__restrict__ mofs,
+                                                const int64_t *__restrict__ goff, const float2 *__restrict__ alm,
+                                                float *__restrict__ bpack) {
+    const int64_t idx = blockIdx.x * 256LL + threadIdx.x;
+    if (idx >= ngroups * 2 * N) return;
+    const int64_t gg = idx / (2 * N);
+    const int item = (int)(idx - gg * 2 * N);
+    int lo = 0, hi = mmax + 1;  // m = the last m with goff[m] <= gg
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (goff[mid] <= gg) lo = mid;
+        else hi = mid;
     }
+    const int m = lo;
+    const int g = (int)(gg - goff[m]);
+    const int mi = item & 3, j = (item >> 2) & 1, rest = item >> 3;
+    const int ng = rest % (N / 8), par = rest / (N / 8);
+    const int map = ng * 4 + mi;
+    float4 rh, rl, ih, il;
+    float *r4 = &rh.x, *i4 = &ih.x, *rl4 = &rl.x, *il4 = &il.x;
+    const int64_t base = (int64_t)map * nalm + mofs[m];
+#pragma unroll
+    for (int kk = 0; kk < 4; ++kk) {
+        const int l = m + g * GLG_GROUP + par + 8 * j + 2 * kk;
+        float2 z = make_float2(0.f, 0.f);
+        if (l <= lmax && map < nmaps) z = alm[base + (l - m)];
+        if (m == 0) z.y = 0.f;  // imaginary part of a_l0 is ignored
+        const uint32_t zr = tf32_rna(z.x), zi = tf32_rna(z.y);
+        r4[kk] = __uint_as_float(zr);
+        i4[kk] = __uint_as_float(zi);
+        rl4[kk] = __uint_as_float(tf32_rna(z.x - __uint_as_float(zr)));
+        il4[kk] = __uint_as_float(tf32_rna(z.y - __uint_as_float(zi)));
+    }
+    float *dst = bpack + gg * (int64_t)(32 * N) + ng * 64 + j * 32 + mi * 8;
+    float *th = dst + (2 * par) * (8 * N), *tl = dst + (2 * par + 1) * (8 * N);
+    reinterpret_cast<float4 *>(th)[0] = rh;
+    reinterpret_cast<float4 *>(th)[1] = ih;
+    reinterpret_cast<float4 *>(tl)[0] = rl;
+    reinterpret_cast<float4 *>(tl)[1] = il;
 }
 
 template <int N>
 int launch_tc(const glg_plan *P, const float2 *alm, int nmaps, float *bpack, float2 *F, int *err,
               cudaStream_t st) {
     {
-        dim3 grid(64, P->mmax + 1);
+        const int64_t items = P->ngroups * 2 * N;
         GLG_LAUNCH_SCOPE("k_pack_b", st);
-        k_pack_b<N><<<grid, 256, 0, st>>>(P->lmax, nmaps, P->nalm, P->mofs, P->goff, alm, bpack);
+        k_pack_b<N><<<(unsigned)((items + 255) / 256), 256, 0, st>>>(P->mmax, P->lmax, nmaps, P->nalm, P->ngroups,
+                                                                     P->mofs, P->goff, alm, bpack);
         GLG_CHECK_LAUNCH("k_pack_b");
     }
     LegTcArgs a;
