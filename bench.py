@@ -360,6 +360,32 @@ def run_ours(args, rank: int, world: int) -> dict | None:
                  "speedup": (nshell / plain_s) and value / (nshell / plain_s)}
         del pm, fm
 
+    # galaxy counts and positions on the benchmark's fast maps (n = 5 per
+    # pixel on average): Poisson counts of 4 shells, positions of one
+    points = {}
+    if args.points:
+        maps = step_device()
+        ngal = 5.0 * npix / g.points.ARCMIN2_SPHERE
+        gen = g.rng.Generator(7)
+        g.points.counts_from_delta(ngal, maps[0], rng=gen)  # warm-up
+        torch.cuda.synchronize()
+        _lib.timing_enable(True)
+        _lib.timing_reset()
+        for t in range(4):
+            g.points.counts_from_delta(ngal, maps[t], rng=gen)
+        torch.cuda.synchronize()
+        c_ms, _ = _lib.kernel_time("k_poisson_counts")
+        a = time.perf_counter()
+        ngal_out = sum(int(c) for _, _, c in g.points.positions_from_delta(ngal, maps[1], batch=100_000_000, rng=gen))
+        torch.cuda.synchronize()
+        p_wall = time.perf_counter() - a
+        p_ms, _ = _lib.kernel_time("k_positions")
+        _lib.timing_enable(False)
+        points = {"mean_per_pixel": 5.0, "counts_pixels_per_s": 4 * npix / (c_ms / 1e3),
+                  "positions_galaxies": ngal_out, "positions_kernel_galaxies_per_s": ngal_out / (p_ms / 1e3),
+                  "positions_from_delta_galaxies_per_s": ngal_out / p_wall}
+        del maps
+
     # end to end: numpy spectra in, numpy maps out, through the public API
     e2e = {}
     if args.e2e_steps > 0:
@@ -388,7 +414,7 @@ def run_ours(args, rank: int, world: int) -> dict | None:
         "data": "synthetic spectra (seeded), Philox variates",
         "config": dict(WORKLOAD, form="fast", l2="inputs/outputs larger than L2 (maps 8 GB/step)",
                        parallelism="replicas" if world > 1 else "1 gpu"),
-        "pixels_per_sec": value * npix, "e2e": e2e, "plain_fp64": plain, "roofline": roofline,
+        "pixels_per_sec": value * npix, "e2e": e2e, "plain_fp64": plain, "roofline": roofline, "points": points,
         "kernel_ms_per_step": {k: v[0] for k, v in kt.items()},
         "kernel_launches_per_step": {k: v[1] for k, v in kt.items()}, "gpu_launches": launches,
         "clocks": clk.summary(), "cpu_baseline": cpu, "serving": serving,
@@ -484,6 +510,8 @@ def main() -> None:
     ap.add_argument("--serving-plain", type=int, default=60,
                     help="requests of the FP64 unbatched serving comparison (0: off)")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--no-points", dest="points", action="store_false",
+                    help="skip the galaxy counts / positions aside")
     ap.add_argument("--ncu-case", nargs="?", const="sht", choices=["sht", "alm"],
                     help="run a small profiling case and exit")
     ap.add_argument("--peaks", action="store_true", help="measure the TF32 / FP32 / FP64 peak rates and exit")

@@ -74,6 +74,7 @@ _SIGNATURES = {
     "glg_workspace_status": ([c_p, c_p], c_i),
     "glg_alm2map_noalloc": ([c_i, c_i, c_p, c_i, c_p, c_p], c_i),
     "glg_peak_tf32": ([c_i, c_i, c_p, c_p], c_i),
+    "glg_host_device_pointer": ([c_p, ctypes.POINTER(c_p)], c_i),
     "glg_peak_fma": ([c_i, c_i, c_i, c_p, c_p], c_i),
     "glg_alm2map_spin_workspace": ([c_p], c_sz),
     "glg_alm2map_spin": ([c_p, c_p, c_p, c_i, c_p, c_p, c_p, c_sz, c_p], c_i),
@@ -157,6 +158,15 @@ def timing_reset() -> None:
 
 def launch_count() -> int:
     return int(lib().glg_launch_count())
+
+
+def host_device_pointer(t: torch.Tensor) -> int:
+    """Device address of a page-locked (pinned) CPU tensor's memory, for
+    kernels that write straight into host buffers; raises ValueError when the
+    memory is not pinned and mapped into the device."""
+    dev = c_p()
+    check(lib().glg_host_device_pointer(c_p(t.data_ptr()), ctypes.byref(dev)), "glg_host_device_pointer")
+    return int(dev.value)
 
 
 def kernel_time(name: str) -> tuple[float, int]:

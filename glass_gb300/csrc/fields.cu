@@ -18,7 +18,9 @@ namespace {
 // One warp per angular mode l (glass/fields.py:101-188).  The matrix m
 // (k x k, double buffered), a and atm live in shared memory.  Every sum
 // runs in the same fixed order, with explicit fma, as orc_iternorm in the
-// CPU oracle, so both give identical bits.
+// CPU oracle, so both give identical bits.  After row i only the trailing
+// z = min(i, k) rows and columns of m (and entries of a) can be non-zero, so
+// the sums start at index k - z: the terms skipped are exact zeros.
 __global__ void __launch_bounds__(32)
 k_iternorm(const double *__restrict__ cov, const int64_t nrows, const int64_t nl, const int k,
            double *__restrict__ w, int64_t *__restrict__ bad) {
@@ -37,10 +39,13 @@ k_iternorm(const double *__restrict__ cov, const int64_t nrows, const int64_t nl
     __syncwarp();
     for (int64_t i = 0; i < nrows; ++i) {
         const double *row = cov + ((size_t)i * nl + l) * kp;
+        const int z = i < k ? (int)i : k, zp = i - 1 < k ? (int)(i - 1) : k;
+        const int lo = k - z, lop = k - (zp > 0 ? zp : 0);
         if (i > 0 && k > 0) {
             for (int j = lane; j < k; j += 32) {
                 double acc = 0.0;
-                for (int q = 0; q < k; ++q) acc = fma(a[q], m[q * k + j], acc);
+                if (j >= lop)
+                    for (int q = lop; q < k; ++q) acc = fma(a[q], m[q * k + j], acc);
                 atm[j] = acc;
             }
             __syncwarp();
@@ -62,14 +67,15 @@ k_iternorm(const double *__restrict__ cov, const int64_t nrows, const int64_t nl
         }
         for (int r = lane; r < k; r += 32) {
             double acc = 0.0;
-            for (int cc = 0; cc < k; ++cc) acc = fma(m[r * k + cc], row[k - cc], acc);
+            if (r >= lo)
+                for (int cc = lo; cc < k; ++cc) acc = fma(m[r * k + cc], row[k - cc], acc);
             a[r] = acc;
         }
         __syncwarp();
         double sv = 0.0;
         if (lane == 0) {
             double aa = 0.0;
-            for (int r = 0; r < k; ++r) aa = fma(a[r], a[r], aa);
+            for (int r = lo; r < k; ++r) aa = fma(a[r], a[r], aa);
             sv = row[0] - aa;
             if (sv < 0) {
                 atomicMin((unsigned long long *)bad, (unsigned long long)i);
@@ -202,7 +208,7 @@ __global__ void k_philox_normals(uint64_t seed, uint64_t sid, int64_t offset, in
 constexpr int CT_L = 16;
 
 template <typename T2, typename T>
-__global__ void k_alm_correlate(const double *__restrict__ w, const int nshell, const int lmax,
+__global__ void k_alm_correlate(const T *__restrict__ w, const int nshell, const int lmax,
                                 const int k, const int64_t t0, const T2 *__restrict__ z,
                                 const int64_t z_first, const uint64_t seed, const uint64_t sid_base,
                                 T2 *__restrict__ alm, const int window) {
@@ -247,22 +253,35 @@ __global__ void k_alm_correlate(const double *__restrict__ w, const int nshell, 
         for (int q = threadIdx.x; q < CT_L * kp; q += B) {
             const int r = q / kp, c = q - r * kp;
             const int lg = l0 + r;
-            ws[r * wst + c] = lg <= lmax ? (T)w[((size_t)s * L + lg) * kp + c] : (T)0;
+            ws[r * wst + c] = lg <= lmax ? w[((size_t)s * L + lg) * kp + c] : (T)0;
         }
         __syncthreads();
         if (valid) {
             zs[head * B] = fetch(t);
-            const T *wt = ws + (l - l0) * wst;
             T re = 0, im = 0;
             const int dmax = t < k ? (int)t : k;
-            int j = head - dmax;
-            if (j < 0) j += window;
-            for (int d = dmax; d >= 0; --d) {
-                const T2 zz = zs[j * B];
-                const T c = wt[k - d];
+            // the window z_{t-dmax} .. z_t, oldest first, in at most two
+            // contiguous runs of slots (j0 .. window-1, then 0 .. head);
+            // coefficient of slot j: w_t[k - dmax + (j - j0) mod window]
+            int j0 = head - dmax;
+            if (j0 < 0) j0 += window;
+            const int run1 = j0 + dmax + 1 <= window ? dmax + 1 : window - j0;
+            const T *wc = ws + (l - l0) * wst + (k - dmax) - j0;
+            const T2 *zp = zs;
+#pragma unroll 4
+            for (int j = j0; j < j0 + run1; ++j) {
+                const T2 zz = zp[j * B];
+                const T c = wc[j];
                 re += c * zz.x;
                 im += c * zz.y;
-                if (++j == window) j = 0;
+            }
+            wc += window;
+#pragma unroll 4
+            for (int j = 0; j < dmax + 1 - run1; ++j) {
+                const T2 zz = zp[j * B];
+                const T c = wc[j];
+                re += c * zz.x;
+                im += c * zz.y;
             }
             if (m == 0) {
                 re = re + im;
@@ -376,7 +395,7 @@ extern "C" int glg_philox_normals(uint64_t seed, uint64_t sid, int64_t offset, i
     return GLG_OK;
 }
 
-extern "C" int glg_alm_correlate(const double *w, int nshell, int lmax, int k, int64_t t0,
+extern "C" int glg_alm_correlate(const void *w, int nshell, int lmax, int k, int64_t t0,
                                  const void *z, int64_t z_first, uint64_t seed, uint64_t sid_base,
                                  int dtype, void *alm, void *stream) {
     GLG_REQUIRE(w && alm, "glg_alm_correlate: null pointer");
@@ -402,13 +421,13 @@ extern "C" int glg_alm_correlate(const double *w, int nshell, int lmax, int k, i
             cudaFuncSetAttribute(k_alm_correlate<double2, double>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k_alm_correlate<double2, double><<<grid, threads, smem, st>>>(
-            w, nshell, lmax, k, t0, (const double2 *)z, z_first, seed, sid_base, (double2 *)alm, window);
+            (const double *)w, nshell, lmax, k, t0, (const double2 *)z, z_first, seed, sid_base, (double2 *)alm, window);
     } else {
         if (smem > 48 * 1024)
             cudaFuncSetAttribute(k_alm_correlate<float2, float>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k_alm_correlate<float2, float><<<grid, threads, smem, st>>>(
-            w, nshell, lmax, k, t0, (const float2 *)z, z_first, seed, sid_base, (float2 *)alm, window);
+            (const float *)w, nshell, lmax, k, t0, (const float2 *)z, z_first, seed, sid_base, (float2 *)alm, window);
     }
     GLG_CHECK_LAUNCH("k_alm_correlate");
     return GLG_OK;

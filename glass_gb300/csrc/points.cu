@@ -8,7 +8,9 @@
 // than a math library.  A Poisson(lam) variate is the sum of Poisson pieces
 // of mean <= 256 (Poisson additivity), each drawn by sequential inversion
 // from one 53-bit uniform: k = min{k : u <= F(k)}, F accumulated from
-// p_0 = e^{-lam}, p_k = p_{k-1} lam / k.  Piece c of pixel e uses words
+// p_0 = e^{-lam}, p_k = (p_{k-1} lam) (1/k), 1/k the correctly rounded
+// reciprocal (a per-block table in shared memory: FP64 division is a long
+// instruction sequence on this GPU, a table load is one).  Piece c of pixel e uses words
 // (2 (c & 1), 2 (c & 1) + 1) of the Philox block with counter
 // (e, sid, c >> 1) and key = seed.
 #include <cuda_runtime.h>
@@ -43,12 +45,15 @@ __device__ __forceinline__ double exp_neg(double x) {
     return ldexp(p, -(int)kd);
 }
 
-__device__ __forceinline__ int64_t poisson_piece(double lam, double u) {
+constexpr int NINV = 512;  // reciprocals 1/k, k < NINV, in shared memory
+
+__device__ __forceinline__ int64_t poisson_piece(double lam, double u, const double *__restrict__ inv) {
     double p = exp_neg(lam), F = p;
     int64_t k = 0;
     while (u > F && p > 0.0 && k < KMAX) {
         k += 1;
-        p = __ddiv_rn(__dmul_rn(p, lam), (double)k);
+        const double rk = k < NINV ? inv[k] : __drcp_rn((double)k);
+        p = __dmul_rn(__dmul_rn(p, lam), rk);
         F = __dadd_rn(F, p);
     }
     return k;
@@ -58,6 +63,9 @@ template <typename T>
 __global__ void k_poisson_counts(const T *__restrict__ delta, int64_t npix, double bias, double offset,
                                  double scale, const double *__restrict__ vis, uint64_t seed, uint32_t sid,
                                  int64_t *__restrict__ counts) {
+    __shared__ double inv[NINV];
+    for (int k = threadIdx.x; k < NINV; k += blockDim.x) inv[k] = k > 0 ? __drcp_rn((double)k) : 0.0;
+    __syncthreads();
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < npix;
          e += (int64_t)gridDim.x * blockDim.x) {
         const double d = (double)delta[e];
@@ -74,7 +82,7 @@ __global__ void k_poisson_counts(const T *__restrict__ delta, int64_t npix, doub
                 x = glg_rng::philox4x32_10((uint32_t)e, (uint32_t)(e >> 32), sid, c >> 1, (uint32_t)seed,
                                            (uint32_t)(seed >> 32));
             const double u = (c & 1u) ? glg_rng::u53(x.z, x.w) : glg_rng::u53(x.x, x.y);
-            total += poisson_piece(lam, u);
+            total += poisson_piece(lam, u, inv);
         }
         counts[e] = total;
     }

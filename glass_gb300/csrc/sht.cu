@@ -65,6 +65,20 @@ extern "C" int glg_alm2map(const glg_plan *P, const void *alm, int nmaps, int fo
     return glg_launch_ring_syn(P, F, nmaps, (double *)maps, epi, st);
 }
 
+extern "C" int glg_host_device_pointer(const void *host, void **dev) {
+    GLG_REQUIRE(host && dev, "glg_host_device_pointer: null pointer");
+    *dev = nullptr;
+    cudaPointerAttributes attr;
+    cudaError_t e = cudaPointerGetAttributes(&attr, host);
+    if (e != cudaSuccess || attr.type != cudaMemoryTypeHost || attr.devicePointer == nullptr) {
+        cudaGetLastError();
+        glg_set_error("glg_host_device_pointer: not page-locked host memory mapped into the device");
+        return GLG_ERR_INVALID;
+    }
+    *dev = attr.devicePointer;
+    return GLG_OK;
+}
+
 extern "C" int glg_workspace_status(const void *ws, void *stream) {
     GLG_REQUIRE(ws != nullptr, "glg_workspace_status: null workspace");
     int st_host = 0;

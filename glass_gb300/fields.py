@@ -294,7 +294,7 @@ class _FieldBatcher:
     def alm(self, t0: int, nshell: int) -> torch.Tensor:
         """Correlated alm of shells t0..t0+nshell-1 (HEALPix order) [nshell][nalm]."""
         alm = torch.empty((nshell, self.z_size), dtype=self.cdtype, device=self.device)
-        w = self.w[t0:t0 + nshell].contiguous()
+        w = self.w[t0:t0 + nshell].to(torch.float64 if self.form == "plain" else torch.float32).contiguous()
         zlo = max(0, t0 - self.k)
         if self.np_rng is not None:
             for t in range(t0, t0 + nshell):
@@ -313,9 +313,9 @@ class _FieldBatcher:
                   "glg_alm_correlate")
         return alm
 
-    def maps(self, t0: int, nshell: int, epi=None) -> torch.Tensor:
+    def maps(self, t0: int, nshell: int, epi=None, out=None) -> torch.Tensor:
         alm = self.alm(t0, nshell)
-        return hp.synth(alm, self.nside, self.lmax, epilogue=epi, form=self.form)
+        return hp.synth(alm, self.nside, self.lmax, epilogue=epi, form=self.form, out=out)
 
 
 def _group_size(ngrf: int, nside: int, lmax: int, form: str, host_rng: bool = False) -> int:
@@ -347,6 +347,24 @@ def _generate_grf(gls, nside: int, *, ncorr=None, rng=None, form: str | None = N
             yield maps[s]
         if b.bad >= 0 and b.bad < t0 + g:
             raise ValueError(b.bad_msg)
+
+
+_HOST_MAPPED: list[bool] = []  # whether pinned host memory is device-addressable here
+
+
+def _pinned_maps(nmaps: int, npix: int) -> torch.Tensor | None:
+    """Pinned float32 [nmaps, npix] host buffer that kernels can write into
+    directly, or None where pinned memory is not mapped into the device."""
+    if _HOST_MAPPED == [False]:
+        return None
+    out = torch.empty((nmaps, npix), dtype=torch.float32, pin_memory=True)
+    try:
+        _lib.host_device_pointer(out)
+    except ValueError:
+        _HOST_MAPPED[:] = [False]
+        return None
+    _HOST_MAPPED[:] = [True]
+    return out
 
 
 def _to_host(maps: torch.Tensor) -> list[np.ndarray]:
@@ -396,9 +414,17 @@ def _generate(fields, gls, nside, ncorr, rng, form):
             epi_kind = [_lib.EPI_LOGNORMAL if f else _lib.EPI_NONE for f in fused]
             epi = (epi_kind, [variances[t] for t in range(t0, t0 + cnt)],
                    [kinds[t][1] if fused[s] else 1.0 for s, t in enumerate(range(t0, t0 + cnt))])
-            maps = b.maps(t0, cnt, epi=epi)
-            if b.numpy_out:
-                maps = _to_host(maps)
+            host = _pinned_maps(cnt, 12 * b.nside * b.nside) if b.numpy_out and form == "fast" else None
+            if host is not None:
+                # the ring FFTs store the float32 maps straight into pinned
+                # host memory while they run: no device-to-host copy after
+                b.maps(t0, cnt, epi=epi, out=host)
+                torch.cuda.current_stream(b.device).synchronize()
+                maps = [h.numpy() for h in host]
+            else:
+                maps = b.maps(t0, cnt, epi=epi)
+                if b.numpy_out:
+                    maps = _to_host(maps)
         for s in range(cnt):
             t = t0 + s
             x = maps[s]

@@ -104,14 +104,19 @@ def _resize_alm(alm: torch.Tensor, lmax_in: int, lmax_out: int) -> torch.Tensor:
 FAST_MAX_MAPS = 40  # maps per fast-form launch (N = 80 tensor-core columns)
 
 
-def synth(alm: torch.Tensor, nside: int, lmax: int, *, epilogue=None, form: str = "plain") -> torch.Tensor:
+def synth(alm: torch.Tensor, nside: int, lmax: int, *, epilogue=None, form: str = "plain",
+          out: torch.Tensor | None = None) -> torch.Tensor:
     """Spin-0 synthesis of alm [nmaps, nalm] -> maps [nmaps, npix].
 
     ``form="plain"``: complex128 alm, float64 maps (FP64 throughout).
-    ``form="fast"``: complex64 alm, float32 maps (tensor-core Legendre sums).
+    ``form="fast"``: complex64 alm, float32 maps (tensor-core Legendre sums);
+    ``out`` may be a float32 [nmaps, npix] device tensor or pinned host
+    tensor to write the maps into.
     """
     if form == "fast":
-        return _synth_fast(alm, nside, lmax, epilogue)
+        return _synth_fast(alm, nside, lmax, epilogue, out)
+    if out is not None:
+        raise ValueError("out is supported by the fast form only")
     plan = get_plan(nside, lmax, alm.device)
     nmaps = alm.shape[0]
     maps = torch.empty((nmaps, plan.npix), dtype=torch.float64, device=alm.device)
@@ -146,16 +151,27 @@ def buckets(nside: int, lmax: int) -> list[dict]:
             for i in range(n)]
 
 
-def _synth_fast(alm: torch.Tensor, nside: int, lmax: int, epilogue) -> torch.Tensor:
+def _synth_fast(alm: torch.Tensor, nside: int, lmax: int, epilogue, out: torch.Tensor | None = None) -> torch.Tensor:
+    """Fast-form synthesis into new device maps, or into ``out``: float32
+    [nmaps, npix] on the device or in pinned host memory, which the ring FFTs
+    then write across the CPU-GPU link while they run (no separate copy)."""
     plan = get_plan(nside, lmax, alm.device)
     alm = alm.to(torch.complex64).contiguous()
     nmaps = alm.shape[0]
-    maps = torch.empty((nmaps, plan.npix), dtype=torch.float32, device=alm.device)
+    if out is None:
+        maps = torch.empty((nmaps, plan.npix), dtype=torch.float32, device=alm.device)
+    else:
+        if out.dtype != torch.float32 or tuple(out.shape) != (nmaps, plan.npix) or not out.is_contiguous():
+            raise ValueError("out must be a contiguous float32 [nmaps, npix] tensor")
+        maps = out
+    base = ptr(maps) if maps.is_cuda else _lib.host_device_pointer(maps)
     step = min(nmaps, FAST_MAX_MAPS)
     ws_bytes = int(lib().glg_alm2map_workspace(plan.handle, step, _lib.FORM_FAST))
     ws = torch.empty(ws_bytes, dtype=torch.uint8, device=alm.device)
     stream = c_p(stream_ptr(alm.device))
-    autotune(plan, step, maps[:step], ws)
+    if not getattr(plan, "tuned", False):  # time the FFT buckets on device maps
+        autotune(plan, step, maps[:step] if maps.is_cuda else
+                 torch.empty((step, plan.npix), dtype=torch.float32, device=alm.device), ws)
     for m0 in range(0, nmaps, step):
         cnt = min(step, nmaps - m0)
         epi = None
@@ -164,7 +180,7 @@ def _synth_fast(alm: torch.Tensor, nside: int, lmax: int, epilogue) -> torch.Ten
             kinds = list(kind) if isinstance(kind, (list, tuple)) else [int(kind)] * nmaps
             epi = _make_epilogue((kinds[m0:m0 + cnt], var[m0:m0 + cnt], lam[m0:m0 + cnt]), cnt)
         check(lib().glg_alm2map(plan.handle, c_p(ptr(alm[m0:m0 + cnt])), cnt, _lib.FORM_FAST,
-                                c_p(ptr(maps[m0:m0 + cnt])), ctypes.byref(epi) if epi is not None else None,
+                                c_p(base + 4 * m0 * plan.npix), ctypes.byref(epi) if epi is not None else None,
                                 c_p(ptr(ws)), ws_bytes, stream), "glg_alm2map (fast)")
     check(lib().glg_workspace_status(c_p(ptr(ws)), stream), "glg_alm2map (fast)")
     return maps

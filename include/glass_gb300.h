@@ -107,14 +107,15 @@ int glg_philox_normals(uint64_t seed, uint64_t sid, int64_t offset, int64_t n, i
  *   alm_t = sum_{d=0..min(t,k)} multalm(z_{t-d}, w_t[:, k-d])
  * (glass/harmonics.py:17-47), reordered from GLASS to HEALPix order
  * (glass/fields.py:943-962) with the m = 0 realification of
- * glass/fields.py:425.  w: float64 [nshell][L][k+1] (iternorm output of
- * those shells, L = lmax+1).  z: complex [nz][nalm] in GLASS order holding
+ * glass/fields.py:425.  w: [nshell][L][k+1] (iternorm output of those
+ * shells, L = lmax+1).  z: complex [nz][nalm] in GLASS order holding
  * shells z_first..t0+nshell-1 (z_first = max(0, t0-k)), or NULL to draw them
  * from the Philox stream (key seed, stream sid_base + shell index, element =
  * GLASS index).  alm: complex [nshell][nalm], HEALPix order.  dtype applies
- * to z and alm.
+ * to w (float64 or float32, the iternorm rows rounded to float32 by the
+ * caller), z and alm.
  */
-int glg_alm_correlate(const double *w, int nshell, int lmax, int k, int64_t t0, const void *z,
+int glg_alm_correlate(const void *w, int nshell, int lmax, int k, int64_t t0, const void *z,
                       int64_t z_first, uint64_t seed, uint64_t sid_base, int dtype, void *alm,
                       void *stream);
 
@@ -225,6 +226,12 @@ typedef struct glg_epilogue {
 size_t glg_alm2map_workspace(const glg_plan *plan, int nmaps, int form);
 int glg_alm2map(const glg_plan *plan, const void *alm, int nmaps, int form, void *maps,
                 const glg_epilogue *epi, void *workspace, size_t workspace_bytes, void *stream);
+
+/* Device address of page-locked host memory (allocated by cudaHostAlloc or
+ * registered with cudaHostRegister, mapped into the device), so that maps
+ * can be written straight into host buffers across the CPU-GPU link:
+ * GLG_ERR_INVALID for any other pointer.  No counterpart in the reference. */
+int glg_host_device_pointer(const void *host, void **dev);
 
 /* Status word of a fast-form workspace (synchronises `stream`): GLG_OK or
  * GLG_ERR_TIMEOUT.  No counterpart in the reference (no device waits there). */

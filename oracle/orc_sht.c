@@ -395,6 +395,10 @@ void orc_alm2ring_spin(const double *elm, const double *blm, int spin, int lmax,
  */
 long orc_iternorm(const double *cov, long nrows, long nl, int k, double *w)
 {
+    /* After the update of row i only the trailing z = min(i, k) rows and
+     * columns of m (and entries of a) can be non-zero; every sum starts at
+     * the first index of that block.  The terms skipped are exact zeros, so
+     * the result is the same as summing over all k indices. */
     long bad = -1;
     const int kp = k + 1;
     for (long l = 0; l < nl; ++l) {
@@ -405,11 +409,14 @@ long orc_iternorm(const double *cov, long nrows, long nl, int k, double *w)
         double s = 1.0;
         for (long i = 0; i < nrows; ++i) {
             const double *row = cov + ((size_t)i * nl + l) * kp;
+            const int z = i < k ? (int)i : k, zp = i - 1 < k ? (int)(i - 1) : k;
+            const int lo = k - z, lop = k - (zp > 0 ? zp : 0);
             if (i > 0 && k > 0) {
                 /* atm_j = sum_p a_p m[p][j] (p ascending) */
                 for (int j = 0; j < k; ++j) {
                     double acc = 0.0;
-                    for (int p = 0; p < k; ++p) acc = fma(a[p], m[p * k + j], acc);
+                    if (j >= lop)
+                        for (int p = lop; p < k; ++p) acc = fma(a[p], m[p * k + j], acc);
                     atm[j] = acc;
                 }
                 double u = s > 0 ? 1.0 : 0.0;
@@ -429,10 +436,11 @@ long orc_iternorm(const double *cov, long nrows, long nl, int k, double *w)
             double aa = 0.0;
             for (int r = 0; r < k; ++r) {
                 double acc = 0.0;
-                for (int c = 0; c < k; ++c) acc = fma(m[r * k + c], row[k - c], acc);
+                if (r >= lo)
+                    for (int c = lo; c < k; ++c) acc = fma(m[r * k + c], row[k - c], acc);
                 a[r] = acc;
             }
-            for (int r = 0; r < k; ++r) aa = fma(a[r], a[r], aa);
+            for (int r = lo; r < k; ++r) aa = fma(a[r], a[r], aa);
             double sv = row[0] - aa;
             if (sv < 0) {
                 if (bad < 0 || i < bad) bad = i;
@@ -513,7 +521,8 @@ void orc_philox_normals(uint64_t seed, uint64_t sid, int64_t offset, int64_t n,
  * Taylor polynomial (no libm), every step a single rounded FP64 operation
  * (this file is built with -ffp-contract=off).  Poisson(n) is a sum of
  * pieces of mean <= 256 (Poisson additivity), each drawn by sequential
- * inversion from one 53-bit uniform; piece c of pixel e uses words
+ * inversion from one 53-bit uniform (p_k = (p_{k-1} lam) (1/k), 1/k the
+ * correctly rounded reciprocal); piece c of pixel e uses words
  * 2(c&1), 2(c&1)+1 of the Philox block with counter (e_lo, e_hi, sid, c>>1).
  */
 double orc_exp_neg(double x)
@@ -539,7 +548,7 @@ static int64_t orc_poisson_piece(double lam, double u)
     int64_t k = 0;
     while (u > F && p > 0.0 && k < (1 << 20)) {
         k += 1;
-        p = (p * lam) / (double)k;
+        p = (p * lam) * (1.0 / (double)k);
         F = F + p;
     }
     return k;

@@ -547,6 +547,38 @@ def test_autotuner_picks_block_sizes(g):
     assert rel_rms(got.cpu().numpy(), osht.alm2map(alm, nside, lmax)) < FAST_RMS
 
 
+def test_fast_maps_written_to_pinned_host_memory(g):
+    """Fast synthesis into a pinned host buffer (the ring FFTs store across
+    the CPU-GPU link) gives the same bits as into device memory; generate
+    with numpy spectra (which takes that route) equals it with torch spectra."""
+    import torch
+
+    from glass_gb300 import healpix as hp
+
+    nside, lmax, nm = 64, 128, 3
+    alm = torch.as_tensor(random_alm(lmax, seed=8, nmaps=nm) * 0.1, device="cuda").to(torch.complex64)
+    ref = hp.synth(alm, nside, lmax, form="fast")
+    host = torch.empty((nm, 12 * nside * nside), dtype=torch.float32, pin_memory=True)
+    try:
+        g._lib.host_device_pointer(host)
+    except ValueError:
+        pytest.skip("pinned host memory is not mapped into the device here")
+    got = hp.synth(alm, nside, lmax, form="fast", out=host)
+    torch.cuda.synchronize()
+    assert got is host
+    torch.testing.assert_close(host, ref.cpu(), rtol=0, atol=0)
+    with pytest.raises(ValueError):
+        g._lib.host_device_pointer(torch.empty(4))  # pageable memory is refused
+    gls, lam = spectra_cfg2(4, 2 * nside)
+    fields = [g.grf.Lognormal(float(x)) for x in lam]
+    a = list(g.generate(fields, gls, nside, rng=g.rng.Generator(3), form="fast"))
+    b = list(g.generate(fields, [torch.as_tensor(c, device="cuda") for c in gls], nside, rng=g.rng.Generator(3),
+                        form="fast"))
+    assert all(isinstance(x, np.ndarray) and x.dtype == np.float32 for x in a)
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x, y.cpu().numpy())
+
+
 def test_synth_graph_replays_equal_direct_calls(g):
     """A captured fast synthesis replays to the same maps as direct calls,
     for new inputs written into its static buffer, with a fused epilogue."""
