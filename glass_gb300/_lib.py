@@ -63,6 +63,7 @@ _SIGNATURES = {
     "glg_almxfl": ([c_p, c_p, c_i, c_i, c_i, c_i, c_p, c_p], c_i),
     "glg_autotune_fast": ([c_p, c_i, c_p, c_p, c_sz, c_p], c_i),
     "glg_plan_buckets": ([c_p, c_p, c_i], c_i),
+    "glg_plan_bucket_times": ([c_p, c_p, c_i], c_i),
     "glg_convergence_step": ([c_p, c_p, c_p, c_i, c_i64, ctypes.c_double, ctypes.c_double, c_p], c_i),
     "glg_ang2pix": ([c_i, c_p, c_p, c_i64, c_i, c_p, c_p], c_i),
     "glg_galaxy_shear": ([c_p, c_p, c_p, c_i64, c_p, c_p, c_p, c_i, c_i, c_i, c_p, c_p], c_i),

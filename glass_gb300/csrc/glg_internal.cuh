@@ -49,12 +49,13 @@ struct glg_launch_scope {
 
 // One launch of the FP32 ring FFTs: `count` ring pairs of one kind
 // (0: mixed radix, 1: Bluestein) starting at bucket_pairs[first].
-#define GLG_MAX_RING_BUCKETS 24
+#define GLG_MAX_RING_BUCKETS 40
 struct glg_ring_bucket {
     int kind, count, threads;
     int size, fold;  // transform length bucket (n rounded up, or M) and fold scratch
     int64_t first;
     size_t smem;
+    float ms;  // autotuner's time of one launch at `threads` (0 before tuning)
 };
 
 struct glg_plan {

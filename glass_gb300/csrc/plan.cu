@@ -352,7 +352,7 @@ __global__ void k_plan_tfirst(int lmax, int npairs, int ntiles, const int *__res
 size_t glg_ring32_smem(int kind, int n_or_M, int threads, bool fold) {
     const size_t zs = (size_t)glg_zsize(n_or_M);
     size_t slots = zs + 2 * (size_t)threads + glg_zi(n_or_M / 2) + 1;
-    if (kind == 0 && fold) slots += zs;
+    if (kind != 1 && fold) slots += zs;
     return slots * sizeof(float2);
 }
 
@@ -408,7 +408,8 @@ static int build_fft32_tables(glg_plan *P, cudaStream_t st) {
         twM[t] = make_float2((float)cos(2.0 * M_PI * t / Mmax), (float)sin(2.0 * M_PI * t / Mmax));
 
     // buckets: Bluestein rings by M, mixed-radix rings by (next power of two
-    // of n, whether m folds onto the ring); largest work first
+    // of n, power-of-two n or not, whether m folds onto the ring); largest
+    // work first
     struct Key {
         int kind, size, fold;
         bool operator<(const Key &o) const {
@@ -426,7 +427,9 @@ static int build_fft32_tables(glg_plan *P, cudaStream_t st) {
         } else {
             int nb = 1;
             while (nb < n) nb <<= 1;
-            groups[{0, nb, n <= mmax ? 1 : 0}].push_back(p);
+            // power-of-two rings get their own launches (kind 2): a kernel
+            // built for radices 16/8/4/2 only needs half the registers
+            groups[{nb == n ? 2 : 0, nb, n <= mmax ? 1 : 0}].push_back(p);
         }
     }
     GLG_REQUIRE((int)groups.size() <= GLG_MAX_RING_BUCKETS, "fast ring FFT: too many ring buckets");
@@ -439,6 +442,7 @@ static int build_fft32_tables(glg_plan *P, cudaStream_t st) {
         b.fold = kv.first.fold;
         b.threads = kv.first.size >= 4096 ? 512 : 256;  // until glg_autotune_fast picks
         b.smem = glg_ring32_smem(b.kind, kv.first.size, b.threads, kv.first.fold != 0);
+        b.ms = 0.f;
         b.count = (int)kv.second.size();
         b.first = (int64_t)bpairs.size();
         bpairs.insert(bpairs.end(), kv.second.begin(), kv.second.end());

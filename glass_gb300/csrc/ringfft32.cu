@@ -385,7 +385,9 @@ __device__ void fold(const float2 *FN, const float2 *FS, bool equator, int n, in
     __syncthreads();
 }
 
-// Class 0: mixed-radix DIF.  smem: Z | SS (n <= mmax) | X[2T] | wh[zi(n/2) + 1].
+// Class 0 (any n) and class 2 (power-of-two n, POW2: radices 16/8/4/2 only):
+// mixed-radix DIF.  smem: Z | SS (n <= mmax) | X[2T] | wh[zi(n/2) + 1].
+template <bool POW2>
 __global__ void __launch_bounds__(TMAX) k_ring32(const RingArgs a, const Epi32 e) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int map = blockIdx.x % a.nmaps;
@@ -404,7 +406,7 @@ __global__ void __launch_bounds__(TMAX) k_ring32(const RingArgs a, const Epi32 e
     const float2 *FN = a.Ft + ((int64_t)map * a.nrings + rn) * (a.mmax + 1);
     const float2 *FS = a.Ft + ((int64_t)map * a.nrings + rs) * (a.mmax + 1);
     fold(FN, FS, equator, n, a.mmax, a.half[p], w2n, nullptr, Z, SS, 0, X);
-    fft_dif<1, false>(Z, wh, n);
+    fft_dif<1, POW2>(Z, wh, n);
     const uint16_t *pos = a.pos16 + a.pos_ofs[i4];
     float *mp = a.maps + (int64_t)map * a.npix;
     const int64_t sN = a.startN[p], sS = a.startS[p];
@@ -510,10 +512,15 @@ static int launch_bucket(const glg_plan *P, const glg_ring_bucket &B, int thread
         GLG_LAUNCH_SCOPE("k_ring32_blu", st);
         k_ring32_blu<<<grid, threads, smem, st>>>(a, e);
         GLG_CHECK_LAUNCH("k_ring32_blu");
-    } else {
-        cudaFuncSetAttribute(k_ring32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    } else if (B.kind == 2) {
+        cudaFuncSetAttribute(k_ring32<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         GLG_LAUNCH_SCOPE("k_ring32", st);
-        k_ring32<<<grid, threads, smem, st>>>(a, e);
+        k_ring32<true><<<grid, threads, smem, st>>>(a, e);
+        GLG_CHECK_LAUNCH("k_ring32");
+    } else {
+        cudaFuncSetAttribute(k_ring32<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        GLG_LAUNCH_SCOPE("k_ring32", st);
+        k_ring32<false><<<grid, threads, smem, st>>>(a, e);
         GLG_CHECK_LAUNCH("k_ring32");
     }
     return GLG_OK;

@@ -187,6 +187,7 @@ extern "C" int glg_autotune_fast(glg_plan *P, int nmaps, void *maps, void *ws, s
         }
         if (rc || e != cudaSuccess) break;
         P->buckets[k].threads = best;
+        P->buckets[k].ms = best_ms / 2.0f;
         P->buckets[k].smem = glg_ring32_smem(P->buckets[k].kind, P->buckets[k].size, best, P->buckets[k].fold != 0);
     }
     cudaEventDestroy(a);
@@ -194,6 +195,13 @@ extern "C" int glg_autotune_fast(glg_plan *P, int nmaps, void *maps, void *ws, s
     if (rc) return rc;
     if (e != cudaSuccess) return glg_cuda_status(e, "glg_autotune_fast");
     return GLG_OK;
+}
+
+extern "C" int glg_plan_bucket_times(const glg_plan *P, float *ms, int max_buckets) {
+    GLG_REQUIRE(P != nullptr && ms != nullptr, "glg_plan_bucket_times: null pointer");
+    int n = 0;
+    for (; n < P->nbuckets && n < max_buckets; ++n) ms[n] = P->buckets[n].ms;
+    return n;
 }
 
 extern "C" int glg_plan_buckets(const glg_plan *P, int *out, int max_buckets) {

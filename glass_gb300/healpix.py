@@ -143,12 +143,15 @@ def autotune(plan, nmaps: int, maps: torch.Tensor, ws: torch.Tensor) -> None:
 
 def buckets(nside: int, lmax: int) -> list[dict]:
     """The fast-form ring-FFT launch buckets of a plan: kind (0 mixed radix,
-    1 Bluestein), transform size, ring pairs and threads per block."""
+    1 Bluestein, 2 power-of-two length), transform size, ring pairs, threads per block and the
+    autotuner's time of one launch (ms, for the map count it was tuned on)."""
     plan = get_plan(nside, lmax)
     out = (ctypes.c_int * (4 * 64))()
     n = lib().glg_plan_buckets(plan.handle, out, 64)
-    return [dict(kind=out[4 * i], size=out[4 * i + 1], pairs=out[4 * i + 2], threads=out[4 * i + 3])
-            for i in range(n)]
+    ms = (ctypes.c_float * 64)()
+    lib().glg_plan_bucket_times(plan.handle, ms, 64)
+    return [dict(kind=out[4 * i], size=out[4 * i + 1], pairs=out[4 * i + 2], threads=out[4 * i + 3],
+                 ms=float(ms[i])) for i in range(n)]
 
 
 def _synth_fast(alm: torch.Tensor, nside: int, lmax: int, epilogue, out: torch.Tensor | None = None) -> torch.Tensor:

@@ -137,8 +137,12 @@ int glg_almxfl(const void *alm, const double *fl, int nfl, int lmax, int nmaps, 
 int glg_autotune_fast(glg_plan *plan, int nmaps, void *maps, void *ws, size_t ws_bytes, void *stream);
 
 /* Ring-FFT launch buckets of a plan: (kind, size, ring pairs, threads) per
- * bucket into out[4 * max_buckets]; returns the number written. */
+ * bucket into out[4 * max_buckets], kind 0 mixed radix, 1 Bluestein, 2
+ * power-of-two length; returns the number written. */
 int glg_plan_buckets(const glg_plan *plan, int *out, int max_buckets);
+/* The autotuner's time (ms) of one launch of each bucket at its chosen block
+ * size (0 before glg_autotune_fast ran); returns the number written. */
+int glg_plan_bucket_times(const glg_plan *plan, float *ms, int max_buckets);
 
 /*
  * One step of the multi-plane convergence recurrence, replacing
