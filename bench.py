@@ -269,6 +269,23 @@ def measure_compute_peaks() -> dict:
 # ------------------------------------------------------------------- ours
 
 
+def max_over_ranks(ms: float, world: int, device) -> float:
+    """The slowest rank's time (all ranks receive it); `ms` itself at N = 1."""
+    if world <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(world: int, nshell: int, ms_step: float) -> float:
+    """Whole-job throughput: every rank runs the full workload (replicas)."""
+    return world * nshell / (ms_step / 1e3)
+
+
 def run_ours(args, rank: int, world: int) -> dict | None:
     import torch
 
@@ -305,14 +322,12 @@ def run_ours(args, rank: int, world: int) -> dict | None:
             step_device()
         t1.record(stream)
         torch.cuda.synchronize()
-    ms = t0.elapsed_time(t1)
-    launches = _lib.launch_count() - launches0
     if world > 1:
-        tt = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        ms = float(tt.item())
+        torch.distributed.barrier()
+    ms = max_over_ranks(t0.elapsed_time(t1), world, dev)
+    launches = _lib.launch_count() - launches0
     ms_step = ms / args.steps
-    value = world * nshell / (ms_step / 1e3)
+    value = job_value(world, nshell, ms_step)
 
     # per-kernel timing of the dominant kernel (one extra step, events per launch)
     _lib.timing_enable(True)
