@@ -427,9 +427,10 @@ static int build_fft32_tables(glg_plan *P, cudaStream_t st) {
         } else {
             int nb = 1;
             while (nb < n) nb <<= 1;
-            // power-of-two rings get their own launches (kind 2): a kernel
-            // built for radices 16/8/4/2 only needs half the registers
-            groups[{nb == n ? 2 : 0, nb, n <= mmax ? 1 : 0}].push_back(p);
+            // power-of-two equatorial rings get their own launch (kind 2): a
+            // kernel built for radices 16/8/4/2 only needs half the registers
+            // (a lone polar ring of that length stays with its size class)
+            groups[{nb == n && i == nside ? 2 : 0, nb, n <= mmax ? 1 : 0}].push_back(p);
         }
     }
     GLG_REQUIRE((int)groups.size() <= GLG_MAX_RING_BUCKETS, "fast ring FFT: too many ring buckets");

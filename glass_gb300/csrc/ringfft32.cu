@@ -37,7 +37,8 @@
 
 namespace {
 
-constexpr int TMAX = 512;
+constexpr int TMAX = 512;        // block size limit of the kernel with odd radices (125 registers)
+constexpr int TMAX_POW2 = 1024;  // power-of-two transforms (64 registers): up to 1024 threads
 constexpr int EPI_MAX = 40;
 
 struct c32 {
@@ -385,10 +386,11 @@ __device__ void fold(const float2 *FN, const float2 *FS, bool equator, int n, in
     __syncthreads();
 }
 
-// Class 0 (any n) and class 2 (power-of-two n, POW2: radices 16/8/4/2 only):
+// Class 0 (any n) and class 2 (power-of-two equatorial n, POW2: radices
+// 16/8/4/2 only):
 // mixed-radix DIF.  smem: Z | SS (n <= mmax) | X[2T] | wh[zi(n/2) + 1].
 template <bool POW2>
-__global__ void __launch_bounds__(TMAX) k_ring32(const RingArgs a, const Epi32 e) {
+__global__ void __launch_bounds__(POW2 ? TMAX_POW2 : TMAX) k_ring32(const RingArgs a, const Epi32 e) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int map = blockIdx.x % a.nmaps;
     const int p = a.pairs[blockIdx.x / a.nmaps];
@@ -421,7 +423,7 @@ __global__ void __launch_bounds__(TMAX) k_ring32(const RingArgs a, const Epi32 e
 
 // Class 1: Bluestein.  smem: Z[M] (the south fold scratch sits at n..2n-1) |
 // X[2T] | wh[zi(M/2) + 1].
-__global__ void __launch_bounds__(TMAX) k_ring32_blu(const RingArgs a, const Epi32 e) {
+__global__ void __launch_bounds__(TMAX_POW2) k_ring32_blu(const RingArgs a, const Epi32 e) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int map = blockIdx.x % a.nmaps;
     const int p = a.pairs[blockIdx.x / a.nmaps];
@@ -465,10 +467,14 @@ __global__ void k_transpose32(const float2 *__restrict__ F, float2 *__restrict__
     const int r0 = blockIdx.x * 32, m0 = blockIdx.y * 32;
     const float2 *src = F + (int64_t)map * nm * nr;
     float2 *dst = Ft + (int64_t)map * nm * nr;
-    for (int y = threadIdx.y; y < 32; y += blockDim.y) {
-        const int m = m0 + y, r = r0 + threadIdx.x;
-        if (m < nm && r < nr) tile[y][threadIdx.x] = src[(int64_t)m * nr + r];
+    float2 v[4];  // blockDim.y == 8: four loads in flight per thread
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int y = threadIdx.y + 8 * i, m = m0 + y, r = r0 + threadIdx.x;
+        v[i] = (m < nm && r < nr) ? src[(int64_t)m * nr + r] : make_float2(0.f, 0.f);
     }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) tile[threadIdx.y + 8 * i][threadIdx.x] = v[i];
     __syncthreads();
     for (int y = threadIdx.y; y < 32; y += blockDim.y) {
         const int r = r0 + y, m = m0 + threadIdx.x;

@@ -167,7 +167,9 @@ extern "C" int glg_autotune_fast(glg_plan *P, int nmaps, void *maps, void *ws, s
     for (int k = 0; k < P->nbuckets; ++k) {
         int best = P->buckets[k].threads;
         float best_ms = 1e30f;
-        for (int threads : {128, 256, 512}) {
+        for (int threads : {128, 256, 512, 1024}) {
+            // 1024 threads only for the power-of-two kernels (kinds 1, 2)
+            if (threads > 512 && P->buckets[k].kind == 0) continue;
             if (glg_ring32_smem(P->buckets[k].kind, P->buckets[k].size, threads, P->buckets[k].fold != 0) >
                 227 * 1024)
                 continue;

@@ -143,8 +143,9 @@ def autotune(plan, nmaps: int, maps: torch.Tensor, ws: torch.Tensor) -> None:
 
 def buckets(nside: int, lmax: int) -> list[dict]:
     """The fast-form ring-FFT launch buckets of a plan: kind (0 mixed radix,
-    1 Bluestein, 2 power-of-two length), transform size, ring pairs, threads per block and the
-    autotuner's time of one launch (ms, for the map count it was tuned on)."""
+    1 Bluestein, 2 power-of-two equatorial length), transform size, ring
+    pairs, threads per block and the autotuner's time of one launch (ms, for
+    the map count it was tuned on)."""
     plan = get_plan(nside, lmax)
     out = (ctypes.c_int * (4 * 64))()
     n = lib().glg_plan_buckets(plan.handle, out, 64)

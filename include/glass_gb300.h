@@ -129,7 +129,8 @@ int glg_almxfl(const void *alm, const double *fl, int nfl, int lmax, int nmaps, 
 /*
  * Autotuner of the fast form (no counterpart in the reference, whose
  * transforms are healpy's): times every ring-FFT size bucket of the plan at
- * 128, 256 and 512 threads per block on the given workspace (sized by
+ * 128, 256, 512 and (power-of-two transforms) 1024 threads per block on the
+ * given workspace (sized by
  * glg_alm2map_workspace for nmaps, GLG_FORM_FAST) and float32 output maps
  * [nmaps][npix] (overwritten), and keeps the fastest in the plan.  Builds the
  * fast-form tables on first use; synchronises the stream.
@@ -138,7 +139,7 @@ int glg_autotune_fast(glg_plan *plan, int nmaps, void *maps, void *ws, size_t ws
 
 /* Ring-FFT launch buckets of a plan: (kind, size, ring pairs, threads) per
  * bucket into out[4 * max_buckets], kind 0 mixed radix, 1 Bluestein, 2
- * power-of-two length; returns the number written. */
+ * power-of-two equatorial length; returns the number written. */
 int glg_plan_buckets(const glg_plan *plan, int *out, int max_buckets);
 /* The autotuner's time (ms) of one launch of each bucket at its chosen block
  * size (0 before glg_autotune_fast ran); returns the number written. */
