@@ -88,7 +88,7 @@ struct glg_plan {
     bool fast_ready;
     float2 *cth32;           // [npairs] cos theta as FP32 (hi, lo)
     float2 *tw32;            // FP32 copy of tw
-    float4 *coef32;          // [nalm] (A_hi, A_lo, B_hi, B_lo) in FP32
+    float4 *coef32;          // [nalm] (alpha_hi, alpha_lo, d, 0) of the scaled FP32 recurrence
     int64_t *goff;           // [mmax+2] first 16-l group of m: sum_{m'<m} ceil((lmax-m'+1)/16)
     int64_t ngroups;         // total groups
     float2 *seeds;           // [ngroups][seed_stride] (lambda_s0, lambda_s0+1) per group

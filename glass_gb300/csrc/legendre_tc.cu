@@ -11,7 +11,11 @@
 // lambda is generated on the fly in FP32 by producer warps, restarting every
 // 16 l (one "group") from seeds computed once per plan by an FP64
 // recurrence, split into TF32 hi + lo parts and written straight into tensor
-// memory as the MMA's A operand.  B (the alm, split the same way), the
+// memory as the MMA's A operand.  Within a group the producers carry the
+// scaled mu_l = lambda_l / d_l, d = 1 at the group's first two l and
+// d_l = B_l d_{l-2} after, whose recurrence mu_l = alpha_l x mu_{l-1} -
+// mu_{l-2} (alpha_l = A_l d_{l-1} / d_l) has no second product; the alm
+// carry d_l instead (B[l][n] = a_lm d_l), so the sums are unchanged.  B (the alm, split the same way), the
 // group's seeds and its recurrence coefficients are streamed into shared
 // memory with 1-D bulk copies.  Each group issues, per parity,
 //   D += A_hi B_lo + A_lo B_hi + A_hi B_hi     (M = 128, N = 2 * maps, K = 8).
@@ -84,11 +88,11 @@ __device__ __forceinline__ uint32_t tf32_rna(float x) {
     return r;
 }
 
-// One step lambda_l = A (x lambda_{l-1}) - B lambda_{l-2} in FP32 with the
-// products and the coefficients carried as (hi, lo) pairs (error-free
-// transformations with fma): only the FP32 state itself is rounded, which
-// keeps the 16-step runs between FP64 seeds near 1e-7.  The __f*_rn forms
-// keep the compiler from fusing the rounded products away.
+// One step mu_l = alpha (x mu_{l-1}) - mu_{l-2} in FP32 with the products
+// and the coefficient carried as (hi, lo) pairs (error-free transformations
+// with fma): only the FP32 state itself is rounded, which keeps the 16-step
+// runs between FP64 seeds near 1e-7.  c = (alpha_hi, alpha_lo, d, 0).  The
+// __f*_rn forms keep the compiler from fusing the rounded products away.
 __device__ __forceinline__ float rec_step(const float4 c, const float2 x, float lm1, float lm2) {
     const float yh = __fmul_rn(x.x, lm1);
     float ye = fmaf(x.x, lm1, -yh);
@@ -97,10 +101,7 @@ __device__ __forceinline__ float rec_step(const float4 c, const float2 x, float 
     float pe = fmaf(c.x, yh, -ph);
     pe = fmaf(c.x, ye, pe);
     pe = fmaf(c.y, yh, pe);
-    const float qh = __fmul_rn(c.z, lm2);
-    float qe = fmaf(c.z, lm2, -qh);
-    qe = fmaf(c.w, lm2, qe);
-    return __fadd_rn(__fsub_rn(ph, qh), __fsub_rn(pe, qe));
+    return __fadd_rn(__fsub_rn(ph, lm2), pe);
 }
 
 __device__ __forceinline__ int unit_m(int64_t mi, int lmax) {
@@ -534,16 +535,17 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
 
 // Bpack[goff[m] + g] = 4 tiles (E_hi, E_lo, O_hi, O_lo) of N x 8 tf32 values,
 // element (n, k) of a tile at float index (n/8)*64 + (k/4)*32 + (n%8)*4 + k%4,
-// holding the re (n even) or im (n odd) part of a_lm of map n/2 at
-// l = m + 16 g + 2 k + parity.  One thread per (group, parity, map, k/4): it
+// holding the re (n even) or im (n odd) part of a_lm d_l of map n/2 at
+// l = m + 16 g + 2 k + parity (d_l the group scale of the recurrence; the
+// product's rounding error is carried into the lo part).  One thread per (group, parity, map, k/4): it
 // loads the 4 alm of its k quad and writes re and im of the hi and lo tiles
 // as 16-byte stores; consecutive threads take consecutive maps and quads, so
 // a warp writes 1 KB of a tile contiguously.
 template <int N>
 __global__ void __launch_bounds__(256) k_pack_b(int mmax, int lmax, int nmaps, int64_t nalm, int64_t ngroups,
                                                 const int64_t *__restrict__ mofs,
-                                                const int64_t *__restrict__ goff, const float2 *__restrict__ alm,
-                                                float *__restrict__ bpack) {
+                                                const int64_t *__restrict__ goff, const float4 *__restrict__ coef32,
+                                                const float2 *__restrict__ alm, float *__restrict__ bpack) {
     const int64_t idx = blockIdx.x * 256LL + threadIdx.x;
     if (idx >= ngroups * 2 * N) return;
     const int64_t gg = idx / (2 * N);
@@ -566,13 +568,19 @@ __global__ void __launch_bounds__(256) k_pack_b(int mmax, int lmax, int nmaps, i
     for (int kk = 0; kk < 4; ++kk) {
         const int l = m + g * GLG_GROUP + par + 8 * j + 2 * kk;
         float2 z = make_float2(0.f, 0.f);
-        if (l <= lmax && map < nmaps) z = alm[base + (l - m)];
+        float d = 0.f;
+        if (l <= lmax && map < nmaps) {
+            z = alm[base + (l - m)];
+            d = coef32[mofs[m] + (l - m)].z;
+        }
         if (m == 0) z.y = 0.f;  // imaginary part of a_l0 is ignored
-        const uint32_t zr = tf32_rna(z.x), zi = tf32_rna(z.y);
+        const float pr = __fmul_rn(z.x, d), pi = __fmul_rn(z.y, d);
+        const float er = fmaf(z.x, d, -pr), ei = fmaf(z.y, d, -pi);  // exact product errors
+        const uint32_t zr = tf32_rna(pr), zi = tf32_rna(pi);
         r4[kk] = __uint_as_float(zr);
         i4[kk] = __uint_as_float(zi);
-        rl4[kk] = __uint_as_float(tf32_rna(z.x - __uint_as_float(zr)));
-        il4[kk] = __uint_as_float(tf32_rna(z.y - __uint_as_float(zi)));
+        rl4[kk] = __uint_as_float(tf32_rna(__fadd_rn(__fsub_rn(pr, __uint_as_float(zr)), er)));
+        il4[kk] = __uint_as_float(tf32_rna(__fadd_rn(__fsub_rn(pi, __uint_as_float(zi)), ei)));
     }
     float *dst = bpack + gg * (int64_t)(32 * N) + ng * 64 + j * 32 + mi * 8;
     float *th = dst + (2 * par) * (8 * N), *tl = dst + (2 * par + 1) * (8 * N);
@@ -589,7 +597,7 @@ int launch_tc(const glg_plan *P, const float2 *alm, int nmaps, float *bpack, flo
         const int64_t items = P->ngroups * 2 * N;
         GLG_LAUNCH_SCOPE("k_pack_b", st);
         k_pack_b<N><<<(unsigned)((items + 255) / 256), 256, 0, st>>>(P->mmax, P->lmax, nmaps, P->nalm, P->ngroups,
-                                                                     P->mofs, P->goff, alm, bpack);
+                                                                     P->mofs, P->goff, P->coef32, alm, bpack);
         GLG_CHECK_LAUNCH("k_pack_b");
     }
     LegTcArgs a;

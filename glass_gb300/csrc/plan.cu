@@ -213,10 +213,12 @@ extern "C" void glg_plan_destroy(glg_plan *P) {
 // ------------------------------------------------------- fast-form tables
 
 // FP64 recurrence per (m, ring pair) that records, for every group of 16 l
-// values starting at l0 = m + 16 j, the seed pair (lambda_s0, lambda_s0+1)
-// with s0 = max(l0, ls), ls the first l whose |lambda| reaches 2^-100.  The
-// FP32 recurrence of the fast contraction restarts from these seeds, so its
-// rounding error never accumulates over more than 16 steps.
+// values starting at l0 = m + 16 j, the seed pair (mu_s0, mu_s0+1) with
+// s0 = max(l0, ls), ls the first l whose |lambda| reaches 2^-100 and
+// mu_l = lambda_l / d_l the group-scaled values of the fast contraction (d = 1
+// at l0 and l0 + 1, d_l = B_l d_{l-2} after).  The FP32 recurrence of the
+// fast contraction restarts from these seeds, so its rounding error never
+// accumulates over more than 16 steps.
 __global__ void k_plan_seeds(int lmax, int npairs, const double *__restrict__ cth,
                              const int64_t *__restrict__ mofs, const double2 *__restrict__ coef,
                              const double *__restrict__ lmm, const int *__restrict__ lmm_scale,
@@ -234,7 +236,11 @@ __global__ void k_plan_seeds(int lmax, int npairs, const double *__restrict__ ct
     int64_t pend = -1;  // group whose seed still needs lambda_{s0+1}
     const int64_t base = mofs[m];
     const int64_t g0 = goff[m];
+    double d1 = 1.0, d2 = 1.0;  // d_{l-1}, d_{l-2} of the group scale
     for (int l = m; l <= lmax; ++l) {
+        const double dl = (l - m) % GLG_GROUP < 2 ? 1.0 : coef[base + l - m].y * d2;
+        d2 = d1;
+        d1 = dl;
         if (l > m) {
             double nl;
             if (l == m + 1) {
@@ -251,8 +257,9 @@ __global__ void k_plan_seeds(int lmax, int npairs, const double *__restrict__ ct
                 sc += 1;
             }
         }
-        const double tv = sc == 0 ? l1 : 0.0;
-        if (ls < 0 && fabs(tv) >= thr) ls = l;
+        const double lam = sc == 0 ? l1 : 0.0;
+        if (ls < 0 && fabs(lam) >= thr) ls = l;
+        const double tv = lam / dl;  // the seed value mu_l
         const int j = (l - m) / GLG_GROUP;
         const int lg0 = m + j * GLG_GROUP;
         if (pend >= 0) {  // l == s0 + 1 of the pending seed
@@ -286,10 +293,31 @@ __global__ void k_plan_cth32(int n, const double *__restrict__ src, float2 *__re
     if (i < n) dst[i] = split_f64(src[i]);
 }
 
-__global__ void k_plan_coef32(int64_t n, const double2 *__restrict__ src, float4 *__restrict__ dst) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const float2 a = split_f64(src[i].x), b = split_f64(src[i].y);
-        dst[i] = make_float4(a.x, a.y, b.x, b.y);
+// Coefficients of the fast contraction's scaled recurrence, per (l, m):
+// (alpha_hi, alpha_lo, d, 0), d the group scale (1 at the group's first two
+// l, d_l = B_l d_{l-2} after) and alpha_l = A_l d_{l-1} / d_l (0 at the
+// group's first two l, which are seeds).  One thread per (m, group).
+__global__ void k_plan_coef32(int lmax, const int64_t *__restrict__ mofs, const double2 *__restrict__ coef,
+                              float4 *__restrict__ dst) {
+    const int m = blockIdx.y;
+    const int G = (lmax - m + GLG_GROUP) / GLG_GROUP;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= G) return;
+    const int64_t base = mofs[m];
+    double d1 = 1.0, d2 = 1.0;  // d_{l-1}, d_{l-2}
+    for (int t = 0; t < GLG_GROUP; ++t) {
+        const int l = m + j * GLG_GROUP + t;
+        if (l > lmax) break;
+        if (t < 2) {
+            dst[base + l - m] = make_float4(0.f, 0.f, 1.f, 0.f);
+            continue;
+        }
+        const double2 ab = coef[base + l - m];
+        const double d = ab.y * d2;
+        const float2 al = split_f64(ab.x * d1 / d);
+        dst[base + l - m] = make_float4(al.x, al.y, (float)d, 0.f);
+        d2 = d1;
+        d1 = d;
     }
 }
 
@@ -502,7 +530,8 @@ int glg_plan_prepare_fast(glg_plan *P, cudaStream_t st) {
     if (e != cudaSuccess) return glg_cuda_status(e, "glg_plan_prepare_fast: upload");
     k_plan_cth32<<<(np + 255) / 256, 256, 0, st>>>(np, P->cth, P->cth32);
     k_plan_f32<<<1024, 256, 0, st>>>(ntw, P->tw, P->tw32);
-    k_plan_coef32<<<1024, 256, 0, st>>>(P->nalm, P->coef, P->coef32);
+    k_plan_coef32<<<dim3((lmax / GLG_GROUP + 128) / 128, lmax + 1), 128, 0, st>>>(lmax, P->mofs, P->coef,
+                                                                                 P->coef32);
     dim3 gs((np + 127) / 128, lmax + 1);
     k_plan_seeds<<<gs, 128, 0, st>>>(lmax, np, P->cth, P->mofs, P->coef, P->lmm, P->lmm_scale,
                                      P->goff, P->seeds, P->seed_stride, P->lstart);
