@@ -414,6 +414,7 @@ __global__ void __launch_bounds__(POW2 ? TMAX_POW2 : TMAX) k_ring32(const RingAr
     const int64_t sN = a.startN[p], sS = a.startS[p];
     const int kind = e.kind[map];
     const float hv = e.hvar[map], lam = e.lam[map];
+#pragma unroll 4
     for (int j = threadIdx.x; j < n; j += T) {
         const c32 v = Z[zi(pos[j])];
         mp[sN + j] = epi(v.x, kind, hv, lam);
@@ -445,7 +446,8 @@ __global__ void __launch_bounds__(TMAX_POW2) k_ring32_blu(const RingArgs a, cons
     __syncthreads();
     fft_dif<-1, true>(Z, wh, M);
     const float2 *H = a.blu_H + a.blu_ofs[i4];
-    for (int k = threadIdx.x; k < M; k += T) Z[zi(k)] = cmul(Z[zi(k)], ldg(H + k));
+#pragma unroll 8
+    for (int k = threadIdx.x; k < M; k += T) Z[zi(k)] = cmul(Z[zi(k)], ldg(H + k));  // 8 loads in flight
     __syncthreads();
     fft_dif_adjoint<-1, true>(Z, wh, M);
     float *mp = a.maps + (int64_t)map * a.npix;
@@ -453,6 +455,7 @@ __global__ void __launch_bounds__(TMAX_POW2) k_ring32_blu(const RingArgs a, cons
     const int kind = e.kind[map];
     const float hv = e.hvar[map], lam = e.lam[map];
     const float invM = 1.0f / (float)M;
+#pragma unroll 4
     for (int j = threadIdx.x; j < n; j += T) {
         const c32 v = cscale(cmul(Z[zi(j)], ldg(chirp + j)), invM);
         mp[sN + j] = epi(v.x, kind, hv, lam);
