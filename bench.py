@@ -14,7 +14,10 @@ Printed JSON (one line, rank 0):
             (numpy) maps, copies inside the timed region,
   plain  -- the FP64 drop-in form on the same workload, and the fast form's
             relative RMS map error against it,
-  roofline / gpu_launches / clocks / cpu_baseline as described in DESIGN.md,
+  roofline -- the Legendre contraction's algorithmic TF32 rate against the
+            measured TF32 peak, with its DRAM bytes per launch,
+  gpu_launches / clocks / cpu_baseline -- this library's launches in the
+            timed region, SM clocks sampled during it, the CPU port's rate,
   serving -- p50/p99 latency and shell-maps/s of the serving workload: a
             Poisson stream of 2000 requests (nside in {128, 256, 512, 1024},
             lmax = 2 nside, 3-20 lognormal shells each) at 70% of the
@@ -45,7 +48,7 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "shell-maps/sec and pixels/sec at nside 2048 vs plain FP64 GPU @1e-6; p50/p99 latency"
 UNIT = "shell-maps/s"
-WORKLOAD = dict(workload="40-shell lognormal field generation (configs[2])", nshell=40, nside=2048,
+WORKLOAD = dict(workload="40-shell lognormal field generation, nside 2048, lmax 4096", nshell=40, nside=2048,
                 lmax=4096)
 
 

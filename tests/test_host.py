@@ -113,35 +113,23 @@ def test_serving_memory_model():
 
 
 def test_cls_files_interchange_with_reference(tmp_path):
-    """save_cls / load_cls use the reference's .npz layout: files written by
-    either side load on the other (glass/user.py:42-86, run from the
-    reference checkout when it is present)."""
-    import importlib
-    import pathlib
-    import sys
-
+    """save_cls / load_cls use the reference's .npz layout (glass/user.py:42-86):
+    a file written by the reference's own save_cls (tests/golden/make_golden_cls.py)
+    loads here, and the file written here holds the same arrays under the same
+    keys."""
     import numpy as np
 
     import glass_gb300 as g
     from tests.conftest import ROOT
+    from tests.golden.make_golden_cls import spectra
 
-    rng = np.random.default_rng(0)
-    cls = [rng.normal(size=n) for n in (5, 7, 7, 3)]
-    g.save_cls(tmp_path / "mine.npz", cls)
-    back = g.load_cls(tmp_path / "mine.npz")
+    cls = spectra()
+    ref = ROOT / "tests" / "golden" / "glass_cls_ref.npz"
+    back = g.load_cls(ref)
     assert len(back) == 4 and all(np.array_equal(a, b) for a, b in zip(cls, back))
-    with np.load(tmp_path / "mine.npz") as npz:
-        np.testing.assert_array_equal(npz["split"], [5, 12, 19])
-    ref = pathlib.Path("/root/reference")
-    if not (ref / "glass" / "user.py").exists():
-        pytest.skip("reference checkout not present")
-    sys.path[:0] = [str(ROOT / "tests" / "golden" / "shims"), str(ref)]
-    try:
-        user = importlib.import_module("glass.user")
-        theirs = user.load_cls(tmp_path / "mine.npz")
-        assert all(np.array_equal(a, b) for a, b in zip(cls, theirs))
-        user.save_cls(tmp_path / "theirs.npz", cls)
-        mine = g.load_cls(tmp_path / "theirs.npz")
-        assert all(np.array_equal(a, b) for a, b in zip(cls, mine))
-    finally:
-        del sys.path[:2]
+    g.save_cls(tmp_path / "mine.npz", cls)
+    with np.load(tmp_path / "mine.npz") as mine, np.load(ref) as theirs:
+        assert sorted(mine.files) == sorted(theirs.files)
+        for k in theirs.files:
+            np.testing.assert_array_equal(mine[k], theirs[k])
+            assert mine[k].dtype == theirs[k].dtype
