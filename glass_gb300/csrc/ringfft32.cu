@@ -177,16 +177,25 @@ __device__ __forceinline__ void dft(c32 *v, const c32 *wh, int n) {
 // One in-place DIF pass of radix R (sub-length L) of a length-n transform,
 // or its adjoint.  DIF: y = DFT_R(v), then y_k *= w_L^(DIR j1 k).  Adjoint:
 // v_k *= w_L^(-DIR j1 k), then y = DFT_R^(-DIR)(v).
-template <int R, int DIR, bool ADJ>
+// P2: n is a power of two, so the butterfly's sub-transform and position
+// come from shifts and masks instead of integer divisions.
+template <int R, int DIR, bool ADJ, bool P2>
 __device__ __forceinline__ void pass(c32 *Z, const c32 *wh, int n, int L) {
     const int msub = L / R, nbf = n / R, tsc = n / L;
     // with 32 or more sub-transforms, neighbouring threads take neighbouring
     // sub-transforms (same twiddles: one broadcast read); otherwise
     // neighbouring butterflies of one sub-transform
     const bool by_blk = tsc >= 32;
+    const int lg_tsc = __ffs(tsc) - 1, lg_msub = __ffs(msub) - 1;
     for (int bf = threadIdx.x; bf < nbf; bf += blockDim.x) {
-        const int blk = by_blk ? bf % tsc : bf / msub;
-        const int j1 = by_blk ? bf / tsc : bf - blk * msub;
+        int blk, j1;
+        if constexpr (P2) {
+            blk = by_blk ? bf & (tsc - 1) : bf >> lg_msub;
+            j1 = by_blk ? bf >> lg_tsc : bf & (msub - 1);
+        } else {
+            blk = by_blk ? bf % tsc : bf / msub;
+            j1 = by_blk ? bf / tsc : bf - blk * msub;
+        }
         const int base = blk * L + j1;
         const int ts = tsc * j1;
         c32 v[R];
@@ -212,18 +221,18 @@ __device__ __forceinline__ void pass(c32 *Z, const c32 *wh, int n, int L) {
 template <int DIR, bool ADJ, bool POW2>
 __device__ __forceinline__ void pass_any(c32 *Z, const c32 *wh, int n, int R, int L) {
     switch (R) {
-        case 16: pass<16, DIR, ADJ>(Z, wh, n, L); break;
-        case 8: pass<8, DIR, ADJ>(Z, wh, n, L); break;
-        case 4: pass<4, DIR, ADJ>(Z, wh, n, L); break;
-        case 2: pass<2, DIR, ADJ>(Z, wh, n, L); break;
+        case 16: pass<16, DIR, ADJ, POW2>(Z, wh, n, L); break;
+        case 8: pass<8, DIR, ADJ, POW2>(Z, wh, n, L); break;
+        case 4: pass<4, DIR, ADJ, POW2>(Z, wh, n, L); break;
+        case 2: pass<2, DIR, ADJ, POW2>(Z, wh, n, L); break;
         default:
             if constexpr (!POW2) {
                 switch (R) {
-                    case 3: pass<3, DIR, ADJ>(Z, wh, n, L); break;
-                    case 5: pass<5, DIR, ADJ>(Z, wh, n, L); break;
-                    case 7: pass<7, DIR, ADJ>(Z, wh, n, L); break;
-                    case 11: pass<11, DIR, ADJ>(Z, wh, n, L); break;
-                    case 13: pass<13, DIR, ADJ>(Z, wh, n, L); break;
+                    case 3: pass<3, DIR, ADJ, POW2>(Z, wh, n, L); break;
+                    case 5: pass<5, DIR, ADJ, POW2>(Z, wh, n, L); break;
+                    case 7: pass<7, DIR, ADJ, POW2>(Z, wh, n, L); break;
+                    case 11: pass<11, DIR, ADJ, POW2>(Z, wh, n, L); break;
+                    case 13: pass<13, DIR, ADJ, POW2>(Z, wh, n, L); break;
                     default: break;
                 }
             }
