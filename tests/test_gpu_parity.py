@@ -310,7 +310,9 @@ def _fast_synth(alm, nside, lmax):
 
 
 @pytest.mark.parametrize(("nside", "lmax", "nmaps"), [(4, 11, 1), (16, 40, 3), (32, 64, 8),
-                                                      (64, 128, 40), (32, 300, 5), (128, 256, 2)])
+                                                      (64, 128, 40), (32, 300, 5), (128, 256, 2),
+                                                      (1, 2, 1), (2, 5, 2), (8, 31, 2), (16, 47, 3),
+                                                      (64, 63, 4)])
 def test_alm2map_fast_vs_oracle(g, nside, lmax, nmaps):
     ell = np.concatenate([np.arange(m, lmax + 1) for m in range(lmax + 1)])
     alm = random_alm(lmax, seed=7, nmaps=nmaps) * (ell + 1.0) ** -0.65
