@@ -83,9 +83,9 @@ struct LegTcArgs {
 };
 
 __device__ __forceinline__ uint32_t tf32_rna(float x) {
-    uint32_t r;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-    return r;
+    // round the magnitude to 10 fraction bits, ties away from zero (the
+    // rounding of cvt.rna.tf32.f32), as an integer add and mask
+    return (__float_as_uint(x) + 0x1000u) & 0xFFFFE000u;
 }
 
 // One step mu_l = alpha (x mu_{l-1}) - mu_{l-2} in FP32 with the products
