@@ -131,10 +131,10 @@ __host__ __device__ inline int glg_fft32_radices(int n, int *r) {
 }
 
 // Shared-memory index of complex element e of a ring FFT buffer: a spare
-// slot per 16, per 256 and per 4096 values makes the strides 1, 16, 256 and
-// 4096 of the radix-16 passes and of the digit-reversed output gather odd in
-// slots, so none of them repeats a bank within a warp.
-__host__ __device__ inline int glg_zi(int e) { return e + (e >> 4) + (e >> 8) + (e >> 12); }
+// slot per 16 and per 256 values makes the strides 1, 16 and 256 of the
+// radix-16 passes and of the digit-reversed output gather odd in slots, so
+// none of them repeats a bank within a warp.
+__host__ __device__ inline int glg_zi(int e) { return e + (e >> 4) + (e >> 8); }
 
 // Slots of a padded buffer of `cnt` complex values.
 __host__ __device__ inline int glg_zsize(int cnt) { return glg_zi(cnt - 1) + 1; }
