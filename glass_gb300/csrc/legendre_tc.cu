@@ -11,7 +11,9 @@
 // lambda is generated on the fly in FP32 by producer warps, restarting every
 // 16 l (one "group") from seeds computed once per plan by an FP64
 // recurrence, split into TF32 hi + lo parts and written straight into tensor
-// memory as the MMA's A operand.  Within a group the producers carry the
+// memory as the MMA's A operand (hi rounded to nearest; lo = v - hi, which
+// the tensor core truncates to TF32: |lo| <= half a TF32 ulp of v with
+// either sign, so the truncation is unbiased and below 2^-21 |v|).  Within a group the producers carry the
 // scaled mu_l = lambda_l / d_l, d = 1 at the group's first two l and
 // d_l = B_l d_{l-2} after, whose recurrence mu_l = alpha_l x mu_{l-1} -
 // mu_{l-2} (alpha_l = A_l d_{l-1} / d_l) has no second product; the alm
@@ -263,7 +265,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
                             lm2 = lm1;
                             lm1 = v;
                             const uint32_t hi = tf32_rna(v);
-                            const uint32_t lo = tf32_rna(v - __uint_as_float(hi));
+                            const uint32_t lo = __float_as_uint(v - __uint_as_float(hi));
                             if (j & 1) {
                                 ohi[j >> 1] = hi;
                                 olo[j >> 1] = lo;
@@ -286,7 +288,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
                             lm2 = lm1;
                             lm1 = v;
                             const uint32_t hi = tf32_rna(v);
-                            const uint32_t lo = tf32_rna(v - __uint_as_float(hi));
+                            const uint32_t lo = __float_as_uint(v - __uint_as_float(hi));
                             if (j & 1) {
                                 ohi[j >> 1] = hi;
                                 olo[j >> 1] = lo;
