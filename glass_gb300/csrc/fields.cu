@@ -42,35 +42,41 @@ k_iternorm(const double *__restrict__ cov, const int64_t nrows, const int64_t nl
         const int z = i < k ? (int)i : k, zp = i - 1 < k ? (int)(i - 1) : k;
         const int lo = k - z, lop = k - (zp > 0 ? zp : 0);
         if (i > 0 && k > 0) {
-            for (int j = lane; j < k; j += 32) {
+            // lanes over the non-zero columns first (one pass while z <= 32)
+            for (int j = lop + lane; j < k; j += 32) {
                 double acc = 0.0;
-                if (j >= lop)
-                    for (int q = lop; q < k; ++q) acc = fma(a[q], m[q * k + j], acc);
+                for (int q = lop; q < k; ++q) acc = fma(a[q], m[q * k + j], acc);
                 atm[j] = acc;
             }
+            for (int j = lane; j < lop; j += 32) atm[j] = 0.0;
             __syncwarp();
             const double u = s > 0 ? 1.0 : 0.0;
             const double sd = s > 0 ? s : 1.0;
-            for (int t = lane; t < kk; t += 32) {
-                const int r = t / k, cc = t - r * k;
+            // only the new non-zero block [lo, k) x [lo, k) of m is written
+            // (nothing reads outside it); its z x z entries are split into
+            // (row, column) with an FP32 reciprocal, exact for z <= 127
+            const float inv_z = 1.0f / (float)z;
+            for (int t = lane; t < z * z; t += 32) {
+                const int rr = (int)(((float)t + 0.5f) * inv_z);
+                const int r = lo + rr, cc = lo + (t - rr * z);
                 double v;
                 if (r < k - 1)
                     v = (cc + 1 < k) ? m[(r + 1) * k + (cc + 1)] : 0.0;
                 else
                     v = ((cc + 1 < k) ? -atm[cc + 1] : u) / sd;
-                mn[t] = v;
+                mn[r * k + cc] = v;
             }
             __syncwarp();
             double *tmp = m;
             m = mn;
             mn = tmp;
         }
-        for (int r = lane; r < k; r += 32) {
+        for (int r = lo + lane; r < k; r += 32) {
             double acc = 0.0;
-            if (r >= lo)
-                for (int cc = lo; cc < k; ++cc) acc = fma(m[r * k + cc], row[k - cc], acc);
+            for (int cc = lo; cc < k; ++cc) acc = fma(m[r * k + cc], row[k - cc], acc);
             a[r] = acc;
         }
+        for (int r = lane; r < lo; r += 32) a[r] = 0.0;
         __syncwarp();
         double sv = 0.0;
         if (lane == 0) {
