@@ -93,8 +93,8 @@ struct glg_plan {
     int64_t ngroups;         // total groups
     float2 *seeds;           // [ngroups][seed_stride] (lambda_s0, lambda_s0+1) per group
     int64_t seed_stride;     // npairs rounded up to whole 128-pair tiles
-    int *lstart;             // [mmax+1][npairs] first l with |lambda| >= 2^-100
-    int *tfirst;             // [mmax+1][ntiles] first group with a lambda >= 2^-100 in the tile
+    int *lstart;             // [mmax+1][npairs] first l with |lambda| >= 2^-40
+    int *tfirst;             // [mmax+1][ntiles] first group with a lambda >= 2^-40 in the tile
 
     // FP32 ring FFTs of the fast form.  Class 0: ring lengths whose prime
     // factors are all <= 13 (mixed-radix DIF, output order from pos16).

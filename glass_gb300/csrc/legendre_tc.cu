@@ -23,7 +23,7 @@
 //   D += A_hi B_lo + A_lo B_hi + A_hi B_hi     (M = 128, N = 2 * maps, K = 8).
 //
 // Groups before the first one where some ring of the tile has |lambda| >=
-// 2^-100 are zero on the whole tile and are skipped (the dense algorithmic
+// 2^-40 are zero on the whole tile and are skipped (the dense algorithmic
 // count is still the one reported).
 //
 // Pipeline.  The groups of a (tile, m) unit are processed in chunks of
@@ -77,7 +77,7 @@ struct LegTcArgs {
     const float2 *seeds;
     int64_t seed_stride;
     const int *lstart;
-    const int *tfirst;  // [m][tile] first group holding a lambda >= 2^-100
+    const int *tfirst;  // [m][tile] first group holding a lambda >= 2^-40
     const unsigned char *bpack;
     float2 *F;  // [map][m][ring]
     int *err;

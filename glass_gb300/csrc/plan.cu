@@ -214,7 +214,7 @@ extern "C" void glg_plan_destroy(glg_plan *P) {
 
 // FP64 recurrence per (m, ring pair) that records, for every group of 16 l
 // values starting at l0 = m + 16 j, the seed pair (mu_s0, mu_s0+1) with
-// s0 = max(l0, ls), ls the first l whose |lambda| reaches 2^-100 and
+// s0 = max(l0, ls), ls the first l whose |lambda| reaches 2^-40 and
 // mu_l = lambda_l / d_l the group-scaled values of the fast contraction (d = 1
 // at l0 and l0 + 1, d_l = B_l d_{l-2} after).  The FP32 recurrence of the
 // fast contraction restarts from these seeds, so its rounding error never
@@ -228,7 +228,7 @@ __global__ void k_plan_seeds(int lmax, int npairs, const double *__restrict__ ct
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= npairs) return;
     const double x = cth[p];
-    const double thr = 7.888609052210118e-31;  // 2^-100
+    const double thr = 9.094947017729282e-13;  // 2^-40, ~1e-12 of the O(1) normalised lambda
     double l0 = 0.0, l1 = lmm[(int64_t)m * npairs + p];
     int sc = lmm_scale[(int64_t)m * npairs + p];
     int ls = -1;
@@ -354,7 +354,7 @@ static void fft_pow2_host(std::vector<std::complex<double>> &x) {
 }
 
 // First 16-l group of every (m, ring tile) that holds a lambda above
-// 2^-100 on some ring of the tile: tfirst = (min_p lstart[m][p] - m) / 16
+// 2^-40 on some ring of the tile: tfirst = (min_p lstart[m][p] - m) / 16
 // (G when no ring of the tile reaches it).  Every group before it is zero
 // on the whole tile, so the contraction skips it.
 __global__ void k_plan_tfirst(int lmax, int npairs, int ntiles, const int *__restrict__ lstart,
