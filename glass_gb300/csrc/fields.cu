@@ -221,6 +221,8 @@ __global__ void k_alm_correlate(const T *__restrict__ w, const int nshell, const
     extern __shared__ __align__(16) unsigned char sm_raw[];
     const int kp = k + 1;
     const int wst = kp | 1;  // odd row stride: the 16 l rows sit in distinct banks
+    // q / kp as a multiply-high by ceil(2^32 / kp): exact for q < 17 kp, kp <= 127
+    const uint32_t kmagic = kp > 1 ? (uint32_t)((0x100000000ull + (uint64_t)kp - 1) / (uint64_t)kp) : 0u;
     T *ws = reinterpret_cast<T *>(sm_raw);  // [CT_L][wst]
     const size_t ws_bytes = ((sizeof(T) * CT_L * wst) + 15) & ~(size_t)15;
     // variate window, slot-major ([slot][thread]) so a warp's accesses are contiguous
@@ -257,7 +259,7 @@ __global__ void k_alm_correlate(const T *__restrict__ w, const int nshell, const
         const int64_t t = t0 + s;
         __syncthreads();
         for (int q = threadIdx.x; q < CT_L * kp; q += B) {
-            const int r = q / kp, c = q - r * kp;
+            const int r = kp > 1 ? (int)__umulhi((uint32_t)q, kmagic) : q, c = q - r * kp;
             const int lg = l0 + r;
             ws[r * wst + c] = lg <= lmax ? w[((size_t)s * L + lg) * kp + c] : (T)0;
         }
