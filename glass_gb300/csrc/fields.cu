@@ -169,18 +169,20 @@ __device__ __forceinline__ float2 philox_cnormal_f32(uint64_t seed, uint64_t sid
     const uint32_t a1 = x.x >> 5, b1 = x.y >> 6, a2 = x.z >> 5, b2 = x.w >> 6;
     const float h1 = (float)(a1 >> 3) * s24, t1 = ((float)((a1 & 7u) << 26 | b1) + 0.5f) * s53;
     const float h2 = (float)(a2 >> 3) * s24, t2 = ((float)((a2 & 7u) << 26 | b2) + 0.5f) * s53;
-    float lg;
-    if (h1 >= 0.5f) {
-        // log(u1) = log1p(-v), v = 1 - u1 from the complemented bits
-        const uint32_t ca = 0x7FFFFFFu - a1, cb = 0x3FFFFFFu - b1;
-        const float vh = (float)(ca >> 3) * s24, vt = ((float)((ca & 7u) << 26 | cb) + 0.5f) * s53;
-        lg = log1pf(-vh) - vt / (1.0f - vh);
-    } else if (h1 > 0.0f) {
-        const float q = t1 / h1;  // < 1; only near u1 ~ 2^-24 is it not tiny
-        lg = logf(h1) + (q < 1e-3f ? q : log1pf(q));
-    } else {
-        lg = logf(t1);
-    }
+    // log(u1), without divergence: logf(A) + log1pf(P) + C with
+    //   u1 >= 1/2: A = 1, P = -vh, C = -vt / (1 - vh)   (v = 1 - u1 = vh + vt
+    //              from the complemented bits, so log(u1) = log1p(-v));
+    //   0 < h1 < 1/2: A = h1, P = t1 / h1, C = 0       (log(h1) + log1p(t1 / h1));
+    //   h1 = 0 (u1 < 2^-24): A = t1, P = C = 0.
+    const bool up = h1 >= 0.5f;
+    const uint32_t ca = 0x7FFFFFFu - a1, cb = 0x3FFFFFFu - b1;
+    const float vh = (float)(ca >> 3) * s24, vt = ((float)((ca & 7u) << 26 | cb) + 0.5f) * s53;
+    const float num = up ? -vt : t1, den = up ? 1.0f - vh : (h1 > 0.0f ? h1 : 1.0f);
+    const float qd = num / den;
+    const float A = up ? 1.0f : (h1 > 0.0f ? h1 : t1);
+    const float P = up ? -vh : (h1 > 0.0f ? qd : 0.0f);
+    const float C = up ? qd : 0.0f;
+    const float lg = (logf(A) + log1pf(P)) + C;
     const float r = sqrtf(-2.0f * lg);
     float sn, cs;
     sincospif(2.0f * h2, &sn, &cs);
