@@ -129,7 +129,7 @@ struct Smem {
     } bs[NBC];
     struct SeedSlot {
         float2 seed[128];        // seeds of the group's 128 ring pairs
-        float4 coef[GLG_GROUP];  // (A_hi, A_lo, B_hi, B_lo) of l = l0 .. l0+15
+        float4 coef[GLG_GROUP];  // (alpha_hi, alpha_lo, d, 0) of l = l0 .. l0+15
     } sd[NSEED];
     static constexpr int ACC_LD = 2 * N + 4;  // floats per lane row (odd count of float4)
     float acc[128][ACC_LD];    // FP32 sums of drained chunks, [lane][column]
