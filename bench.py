@@ -348,10 +348,10 @@ def run_ours(args, rank: int, world: int) -> dict | None:
     peak_tf, peak_note = tf32_peak_tflops(peaks)
     achieved = flops / (leg_ms / max(leg_n, 1) / 1e3) / 1e12 if leg_ms > 0 else None
     # DRAM bytes of one full-size k_leg_tc launch (40 maps, nside 2048, lmax
-    # 4096) from ncu: dram__bytes_read.sum 18.06e9 + dram__bytes_write.sum
+    # 4096) from ncu: dram__bytes_read.sum 17.68e9 + dram__bytes_write.sum
     # 10.71e9, one-pass capture of the second launch of
     # `bench.py --steps 1 --warmup 1 --plain-steps 0 --e2e-steps 0 ...`
-    traffic = 18.056145920e9 + 10.707729920e9 if (nshell, nside, lmax) == (40, 2048, 4096) else None
+    traffic = 17.684237568e9 + 10.706691328e9 if (nshell, nside, lmax) == (40, 2048, 4096) else None
     roofline = {"bound": "tensor", "kernel": "k_leg_tc", "achieved": achieved, "peak": peak_tf,
                 "unit": "TFLOP/s", "frac": (achieved / peak_tf) if achieved else None,
                 "traffic": traffic, "traffic_unit": "bytes per launch", "peak_note": peak_note, "passes": 3,
