@@ -301,7 +301,7 @@ k_leg_ana(const int npairs, const int nrings, const int lmax, const int64_t nalm
 
 int glg_launch_leg_syn(const glg_plan *P, const double2 *alm, int nmaps, double2 *F,
                        cudaStream_t st) {
-    constexpr int NS = 4;
+    constexpr int NS = 8;  // maps per pass: the FP64 recurrence is shared by 8 maps
     dim3 grid((P->npairs + LEG_THREADS - 1) / LEG_THREADS, P->mmax + 1, (nmaps + NS - 1) / NS);
     GLG_LAUNCH_SCOPE("k_leg_syn", st);
     k_leg_syn<NS><<<grid, LEG_THREADS, 0, st>>>(P->npairs, P->nrings, P->lmax, P->nalm, P->cth,
