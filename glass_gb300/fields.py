@@ -256,7 +256,9 @@ class _FieldBatcher:
             flat_h = np.concatenate([np.asarray(g, dtype=np.float64).reshape(-1) for g in gls if g is not None])
             flat = torch.from_numpy(flat_h).to(self.device)
         else:
-            flat = torch.cat([_lib.to_device(g, torch.float64, self.device).reshape(-1)
+            dev, f64 = self.device, torch.float64
+            flat = torch.cat([g if (isinstance(g, torch.Tensor) and g.dtype == f64 and g.device == dev
+                                    and g.dim() == 1) else _lib.to_device(g, f64, dev).reshape(-1)
                               for g in gls if g is not None])
         offs_d = torch.from_numpy(offs).to(self.device)
         cov = torch.empty((self.ngrf, n, k + 1), dtype=torch.float64, device=self.device)
