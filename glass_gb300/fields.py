@@ -234,7 +234,8 @@ class _FieldBatcher:
         self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else device
         self.ngrf = nfields_from_nspectra(len(gls))
         self.ncorr = self.ngrf - 1 if ncorr is None else int(ncorr)
-        n = max((g.shape[0] for g in gls), default=0)
+        lens = [0 if g is None else int(g.shape[0]) for g in gls]
+        n = max(lens, default=0)
         if n == 0:
             raise ValueError("all gls are empty")
         self.n = n
@@ -250,7 +251,6 @@ class _FieldBatcher:
         self.k = k
         # cls2cov + variances of every field in one launch from the
         # concatenated spectra, then iternorm of every field in one launch
-        lens = [0 if g is None else int(g.shape[0]) for g in gls]
         offs = np.concatenate([[0], np.cumsum(lens)]).astype(np.int64)
         if self.numpy_out:
             flat_h = np.concatenate([np.asarray(g, dtype=np.float64).reshape(-1) for g in gls if g is not None])
