@@ -423,11 +423,20 @@ __global__ void __launch_bounds__(POW2 ? TMAX_POW2 : TMAX) k_ring32(const RingAr
     const int64_t sN = a.startN[p], sS = a.startS[p];
     const int kind = e.kind[map];
     const float hv = e.hvar[map], lam = e.lam[map];
-#pragma unroll 4
-    for (int j = threadIdx.x; j < n; j += T) {
-        const c32 v = Z[zi(pos[j])];
-        mp[sN + j] = epi(v.x, kind, hv, lam);
-        if (!equator) mp[sS + j] = epi(v.y, kind, hv, lam);
+    // four consecutive pixels per thread, stored as one 16-byte vector (ring
+    // starts and lengths are multiples of 4 pixels): fewer, larger stores,
+    // which the CPU-GPU link takes better when the maps are host memory
+#pragma unroll 2
+    for (int q = threadIdx.x; q < (n >> 2); q += T) {
+        const ushort4 ps = *reinterpret_cast<const ushort4 *>(pos + 4 * q);
+        const c32 v0 = Z[zi(ps.x)], v1 = Z[zi(ps.y)], v2 = Z[zi(ps.z)], v3 = Z[zi(ps.w)];
+        *reinterpret_cast<float4 *>(mp + sN + 4 * q) =
+            make_float4(epi(v0.x, kind, hv, lam), epi(v1.x, kind, hv, lam), epi(v2.x, kind, hv, lam),
+                        epi(v3.x, kind, hv, lam));
+        if (!equator)
+            *reinterpret_cast<float4 *>(mp + sS + 4 * q) =
+                make_float4(epi(v0.y, kind, hv, lam), epi(v1.y, kind, hv, lam), epi(v2.y, kind, hv, lam),
+                            epi(v3.y, kind, hv, lam));
     }
 }
 
@@ -464,11 +473,21 @@ __global__ void __launch_bounds__(TMAX_POW2) k_ring32_blu(const RingArgs a, cons
     const int kind = e.kind[map];
     const float hv = e.hvar[map], lam = e.lam[map];
     const float invM = 1.0f / (float)M;
-#pragma unroll 4
-    for (int j = threadIdx.x; j < n; j += T) {
-        const c32 v = cscale(cmul(Z[zi(j)], ldg(chirp + j)), invM);
-        mp[sN + j] = epi(v.x, kind, hv, lam);
-        if (!equator) mp[sS + j] = epi(v.y, kind, hv, lam);
+#pragma unroll 1
+    for (int q = threadIdx.x; q < (n >> 2); q += T) {  // four pixels per thread, 16-byte stores
+        const float4 ca = __ldg(reinterpret_cast<const float4 *>(chirp + 4 * q));
+        const float4 cb = __ldg(reinterpret_cast<const float4 *>(chirp + 4 * q) + 1);
+        const c32 v0 = cscale(cmul(Z[zi(4 * q)], c32{ca.x, ca.y}), invM);
+        const c32 v1 = cscale(cmul(Z[zi(4 * q + 1)], c32{ca.z, ca.w}), invM);
+        const c32 v2 = cscale(cmul(Z[zi(4 * q + 2)], c32{cb.x, cb.y}), invM);
+        const c32 v3 = cscale(cmul(Z[zi(4 * q + 3)], c32{cb.z, cb.w}), invM);
+        *reinterpret_cast<float4 *>(mp + sN + 4 * q) =
+            make_float4(epi(v0.x, kind, hv, lam), epi(v1.x, kind, hv, lam), epi(v2.x, kind, hv, lam),
+                        epi(v3.x, kind, hv, lam));
+        if (!equator)
+            *reinterpret_cast<float4 *>(mp + sS + 4 * q) =
+                make_float4(epi(v0.y, kind, hv, lam), epi(v1.y, kind, hv, lam), epi(v2.y, kind, hv, lam),
+                            epi(v3.y, kind, hv, lam));
     }
 }
 

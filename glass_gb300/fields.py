@@ -253,7 +253,10 @@ class _FieldBatcher:
         # concatenated spectra, then iternorm of every field in one launch
         offs = np.concatenate([[0], np.cumsum(lens)]).astype(np.int64)
         if self.numpy_out:
-            flat_h = np.concatenate([np.asarray(g, dtype=np.float64).reshape(-1) for g in gls if g is not None])
+            if all(isinstance(g, np.ndarray) and g.dtype == np.float64 and g.ndim == 1 for g in gls):
+                flat_h = np.concatenate(gls)
+            else:
+                flat_h = np.concatenate([np.asarray(g, dtype=np.float64).reshape(-1) for g in gls if g is not None])
             flat = torch.from_numpy(flat_h).to(self.device)
         else:
             dev, f64 = self.device, torch.float64
