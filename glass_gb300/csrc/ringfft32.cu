@@ -306,27 +306,37 @@ __device__ void fold(const float2 *FN, const float2 *FS, bool equator, int n, in
     const int T = blockDim.x, t = threadIdx.x;
     const c32 one = {1.f, 0.f};
     if (n > mmax) {
-        // at most one term per residue: read F directly
-#pragma unroll 4
-        for (int k = t; k < n; k += T) {
+        // at most one term per residue: read F directly; the residues k and
+        // n - k use the same two values of F, so one thread makes both
+#pragma unroll 2
+        for (int k = t; k <= (n >> 1); k += T) {
             const int k2 = k ? n - k : 0;
             const float ck = k ? 1.f : 0.5f;
-            c32 an = {0.f, 0.f}, as = an, bn = an, bs = an;
+            c32 fn = {0.f, 0.f}, fs = fn, gn = fn, gs = fn;  // F at k and at k2
             if (k <= mmax) {
-                an = cscale(ldg(FN + k), ck);
-                as = cscale(ldg(FS + k), ck);
+                fn = ldg(FN + k);
+                fs = ldg(FS + k);
             }
             if (k2 <= mmax) {
-                bn = cscale(ldg(FN + k2), ck);
-                bs = cscale(ldg(FS + k2), ck);
+                gn = ldg(FN + k2);
+                gs = ldg(FS + k2);
             }
             const c32 wk = h ? ldg(w2n + k) : one, wk2 = h ? ldg(w2n + k2) : one;
+            const c32 an = cscale(fn, ck), as = cscale(fs, ck), bn = cscale(gn, ck), bs = cscale(gs, ck);
             const c32 BN = cadd(cmul(wk, an), cconj(cmul(wk2, bn)));
             c32 BS = cadd(cmul(wk, as), cconj(cmul(wk2, bs)));
             if (equator) BS = {0.f, 0.f};
             c32 z = pack(BN, BS);
             if (chirp) z = cmul(z, ldg(chirp + k));
             Z[zi(k)] = z;
+            if (k2 != k) {  // residue n - k: the roles of the two values swap
+                const c32 BN2 = cadd(cmul(wk2, gn), cconj(cmul(wk, fn)));
+                c32 BS2 = cadd(cmul(wk2, gs), cconj(cmul(wk, fs)));
+                if (equator) BS2 = {0.f, 0.f};
+                c32 z2 = pack(BN2, BS2);
+                if (chirp) z2 = cmul(z2, ldg(chirp + k2));
+                Z[zi(k2)] = z2;
+            }
         }
         __syncthreads();
         return;
