@@ -278,7 +278,7 @@ __global__ void k_alm_correlate(const T *__restrict__ w, const int nshell, const
             const int run1 = j0 + dmax + 1 <= window ? dmax + 1 : window - j0;
             const T *wc = ws + (l - l0) * wst + (k - dmax) - j0;
             const T2 *zp = zs;
-#pragma unroll 4
+#pragma unroll 8
             for (int j = j0; j < j0 + run1; ++j) {
                 const T2 zz = zp[j * B];
                 const T c = wc[j];

@@ -179,8 +179,10 @@ __device__ __forceinline__ void dft(c32 *v, const c32 *wh, int n) {
 // v_k *= w_L^(-DIR j1 k), then y = DFT_R^(-DIR)(v).
 // P2: n is a power of two, so the butterfly's sub-transform and position
 // come from shifts and masks instead of integer divisions.
-template <int R, int DIR, bool ADJ, bool P2>
-__device__ __forceinline__ void pass(c32 *Z, const c32 *wh, int n, int L) {
+// ZV: elements at or beyond nv are zero and not read (the zero padding of a
+// Bluestein input, on its first pass).
+template <int R, int DIR, bool ADJ, bool P2, bool ZV = false>
+__device__ __forceinline__ void pass(c32 *Z, const c32 *wh, int n, int L, int nv = 0) {
     const int msub = L / R, nbf = n / R, tsc = n / L;
     // with 32 or more sub-transforms, neighbouring threads take neighbouring
     // sub-transforms (same twiddles: one broadcast read); otherwise
@@ -201,7 +203,10 @@ __device__ __forceinline__ void pass(c32 *Z, const c32 *wh, int n, int L) {
         c32 v[R];
         if constexpr (!ADJ) {
 #pragma unroll
-            for (int j = 0; j < R; ++j) v[j] = Z[zi(base + msub * j)];
+            for (int j = 0; j < R; ++j) {
+                if constexpr (ZV) v[j] = base + msub * j < nv ? Z[zi(base + msub * j)] : c32{0.f, 0.f};
+                else v[j] = Z[zi(base + msub * j)];
+            }
             dft<R, DIR>(v, wh, n);
             Z[zi(base)] = v[0];
 #pragma unroll
@@ -240,13 +245,28 @@ __device__ __forceinline__ void pass_any(c32 *Z, const c32 *wh, int n, int R, in
     }
 }
 
+// First forward pass of a power-of-two transform whose input is zero at and
+// beyond nv.
+template <int DIR>
+__device__ __forceinline__ void pass_first_zv(c32 *Z, const c32 *wh, int n, int R, int L, int nv) {
+    switch (R) {
+        case 16: pass<16, DIR, false, true, true>(Z, wh, n, L, nv); break;
+        case 8: pass<8, DIR, false, true, true>(Z, wh, n, L, nv); break;
+        case 4: pass<4, DIR, false, true, true>(Z, wh, n, L, nv); break;
+        case 2: pass<2, DIR, false, true, true>(Z, wh, n, L, nv); break;
+        default: break;
+    }
+}
+
+// nv < n: the input is zero at and beyond nv (power-of-two n only).
 template <int DIR, bool POW2>
-__device__ void fft_dif(c32 *Z, const c32 *wh, int n) {
+__device__ void fft_dif(c32 *Z, const c32 *wh, int n, int nv = -1) {
     int r[GLG_MAX_FFT_STAGES];
     const int ns = glg_fft32_radices(n, r);
     int L = n;
     for (int s = 0; s < ns; ++s) {
-        pass_any<DIR, false, POW2>(Z, wh, n, r[s], L);
+        if (POW2 && s == 0 && nv >= 0) pass_first_zv<DIR>(Z, wh, n, r[s], L, nv);
+        else pass_any<DIR, false, POW2>(Z, wh, n, r[s], L);
         L /= r[s];
     }
 }
@@ -470,9 +490,7 @@ __global__ void __launch_bounds__(TMAX_POW2) k_ring32_blu(const RingArgs a, cons
     const float2 *FN = a.Ft + ((int64_t)map * a.nrings + rn) * (a.mmax + 1);
     const float2 *FS = a.Ft + ((int64_t)map * a.nrings + rs) * (a.mmax + 1);
     fold(FN, FS, equator, n, a.mmax, a.half[p], w2n, chirp, Z, Z, n, X);
-    for (int k = n + threadIdx.x; k < M; k += T) Z[zi(k)] = {0.f, 0.f};
-    __syncthreads();
-    fft_dif<-1, true>(Z, wh, M);
+    fft_dif<-1, true>(Z, wh, M, n);  // the padding beyond n is zero: not written, not read
     const float2 *H = a.blu_H + a.blu_ofs[i4];
 #pragma unroll 8
     for (int k = threadIdx.x; k < M; k += T) Z[zi(k)] = cmul(Z[zi(k)], ldg(H + k));  // 8 loads in flight
