@@ -333,36 +333,25 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
                 static_assert((2 * N) % 32 == 0, "accumulator columns in pairs of 16");
                 float4 *row = reinterpret_cast<float4 *>(&S.acc[r][0]);
                 const uint32_t dcol = tb + lane_base + 2 * N * d;
-                int c0 = 0;
-                for (; c0 + 64 <= 2 * N; c0 += 64) {  // four loads in flight per wait
-                    uint32_t v[64];
+                // rounds of 32 columns: the running sums' shared-memory loads
+                // are issued before the tensor-memory loads, so both
+                // latencies overlap before the adds
+#pragma unroll 1
+                for (int c0 = 0; c0 < 2 * N; c0 += 32) {
+                    float4 t[8];
 #pragma unroll
-                    for (int h = 0; h < 4; ++h)
-                        tmem_ld16(dcol + c0 + 16 * h, *reinterpret_cast<uint32_t(*)[16]>(&v[16 * h]));
-                    tmem_wait_ld();
-#pragma unroll
-                    for (int j = 0; j < 16; ++j) {
-                        float4 t = row[c0 / 4 + j];
-                        t.x += __uint_as_float(v[4 * j]);
-                        t.y += __uint_as_float(v[4 * j + 1]);
-                        t.z += __uint_as_float(v[4 * j + 2]);
-                        t.w += __uint_as_float(v[4 * j + 3]);
-                        row[c0 / 4 + j] = t;
-                    }
-                }
-                if (c0 < 2 * N) {  // 32 columns left
+                    for (int j = 0; j < 8; ++j) t[j] = row[c0 / 4 + j];
                     uint32_t v[32];
                     tmem_ld16(dcol + c0, *reinterpret_cast<uint32_t(*)[16]>(&v[0]));
                     tmem_ld16(dcol + c0 + 16, *reinterpret_cast<uint32_t(*)[16]>(&v[16]));
                     tmem_wait_ld();
 #pragma unroll
                     for (int j = 0; j < 8; ++j) {
-                        float4 t = row[c0 / 4 + j];
-                        t.x += __uint_as_float(v[4 * j]);
-                        t.y += __uint_as_float(v[4 * j + 1]);
-                        t.z += __uint_as_float(v[4 * j + 2]);
-                        t.w += __uint_as_float(v[4 * j + 3]);
-                        row[c0 / 4 + j] = t;
+                        t[j].x += __uint_as_float(v[4 * j]);
+                        t[j].y += __uint_as_float(v[4 * j + 1]);
+                        t[j].z += __uint_as_float(v[4 * j + 2]);
+                        t[j].w += __uint_as_float(v[4 * j + 3]);
+                        row[c0 / 4 + j] = t[j];
                     }
                 }
                 fence_before_sync();
