@@ -259,10 +259,11 @@ __device__ __forceinline__ void pass_first_zv(c32 *Z, const c32 *wh, int n, int 
 }
 
 // nv < n: the input is zero at and beyond nv (power-of-two n only).
+// skip_last: leave out the last pass (the caller folds it into its reads).
 template <int DIR, bool POW2>
-__device__ void fft_dif(c32 *Z, const c32 *wh, int n, int nv = -1) {
+__device__ void fft_dif(c32 *Z, const c32 *wh, int n, int nv = -1, bool skip_last = false) {
     int r[GLG_MAX_FFT_STAGES];
-    const int ns = glg_fft32_radices(n, r);
+    const int ns = glg_fft32_radices(n, r) - (skip_last ? 1 : 0);
     int L = n;
     for (int s = 0; s < ns; ++s) {
         if (POW2 && s == 0 && nv >= 0) pass_first_zv<DIR>(Z, wh, n, r[s], L, nv);
@@ -447,7 +448,12 @@ __global__ void __launch_bounds__(POW2 ? TMAX_POW2 : TMAX) k_ring32(const RingAr
     const float2 *FN = a.Ft + ((int64_t)map * a.nrings + rn) * (a.mmax + 1);
     const float2 *FS = a.Ft + ((int64_t)map * a.nrings + rs) * (a.mmax + 1);
     fold(FN, FS, equator, n, a.mmax, a.half[p], w2n, nullptr, Z, SS, 0, X);
-    fft_dif<1, POW2>(Z, wh, n);
+    // a last DIF pass of radix 2 (L = 2: no twiddles) is folded into the
+    // output gather: frequency at storage slot s is Z[s & ~1] +- Z[s | 1]
+    int rr[GLG_MAX_FFT_STAGES];
+    const int nst = glg_fft32_radices(n, rr);
+    const bool last2 = POW2 && nst > 1 && rr[nst - 1] == 2;
+    fft_dif<1, POW2>(Z, wh, n, -1, last2);
     const uint16_t *pos = a.pos16 + a.pos_ofs[i4];
     float *mp = a.maps + (int64_t)map * a.npix;
     const int64_t sN = a.startN[p], sS = a.startS[p];
@@ -459,7 +465,12 @@ __global__ void __launch_bounds__(POW2 ? TMAX_POW2 : TMAX) k_ring32(const RingAr
 #pragma unroll 2
     for (int q = threadIdx.x; q < (n >> 2); q += T) {
         const ushort4 ps = *reinterpret_cast<const ushort4 *>(pos + 4 * q);
-        const c32 v0 = Z[zi(ps.x)], v1 = Z[zi(ps.y)], v2 = Z[zi(ps.z)], v3 = Z[zi(ps.w)];
+        auto at = [&](int sl) -> c32 {
+            if (!last2) return Z[zi(sl)];
+            const c32 u0 = Z[zi(sl & ~1)], u1 = Z[zi(sl | 1)];
+            return (sl & 1) ? csub(u0, u1) : cadd(u0, u1);
+        };
+        const c32 v0 = at(ps.x), v1 = at(ps.y), v2 = at(ps.z), v3 = at(ps.w);
         *reinterpret_cast<float4 *>(mp + sN + 4 * q) =
             make_float4(epi(v0.x, kind, hv, lam), epi(v1.x, kind, hv, lam), epi(v2.x, kind, hv, lam),
                         epi(v3.x, kind, hv, lam));
