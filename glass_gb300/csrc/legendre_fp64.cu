@@ -299,9 +299,8 @@ k_leg_ana(const int npairs, const int nrings, const int lmax, const int64_t nalm
 
 }  // namespace
 
-int glg_launch_leg_syn(const glg_plan *P, const double2 *alm, int nmaps, double2 *F,
-                       cudaStream_t st) {
-    constexpr int NS = 8;  // maps per pass: the FP64 recurrence is shared by 8 maps
+template <int NS>
+static int launch_leg_syn(const glg_plan *P, const double2 *alm, int nmaps, double2 *F, cudaStream_t st) {
     dim3 grid((P->npairs + LEG_THREADS - 1) / LEG_THREADS, P->mmax + 1, (nmaps + NS - 1) / NS);
     GLG_LAUNCH_SCOPE("k_leg_syn", st);
     k_leg_syn<NS><<<grid, LEG_THREADS, 0, st>>>(P->npairs, P->nrings, P->lmax, P->nalm, P->cth,
@@ -309,6 +308,28 @@ int glg_launch_leg_syn(const glg_plan *P, const double2 *alm, int nmaps, double2
                                                 nmaps, F);
     GLG_CHECK_LAUNCH("k_leg_syn");
     return GLG_OK;
+}
+
+// Maps per pass: the FP64 recurrence (~4 operations per lambda) is shared by
+// the NS maps of a pass (2 FMA per lambda and map, also for empty slots of
+// the last pass): NS in {1, 2, 4, 8} minimising passes x (2 NS + 4).
+int glg_launch_leg_syn(const glg_plan *P, const double2 *alm, int nmaps, double2 *F,
+                       cudaStream_t st) {
+    int best = 1;
+    long best_cost = -1;
+    for (int ns : {8, 4, 2, 1}) {
+        const long cost = (long)((nmaps + ns - 1) / ns) * (2 * ns + 4);
+        if (best_cost < 0 || cost < best_cost) {
+            best_cost = cost;
+            best = ns;
+        }
+    }
+    switch (best) {
+        case 8: return launch_leg_syn<8>(P, alm, nmaps, F, st);
+        case 4: return launch_leg_syn<4>(P, alm, nmaps, F, st);
+        case 2: return launch_leg_syn<2>(P, alm, nmaps, F, st);
+        default: return launch_leg_syn<1>(P, alm, nmaps, F, st);
+    }
 }
 
 int glg_launch_leg_syn_spin(const glg_plan *P, const double2 *elm, const double2 *blm, int spin,
