@@ -11,8 +11,8 @@
  *
  * Each function names the reference interface it replaces (GLASS, file:line
  * within the glass-dev/glass project).  The Python package glass_gb300 binds
- * these through ctypes; INTEGRATION.md shows the binding a GLASS maintainer
- * would add.
+ * these through ctypes (glass_gb300/_lib.py); a binding on the GLASS side
+ * would be a ctypes module of the same kind.
  */
 #ifndef GLASS_GB300_H
 #define GLASS_GB300_H
