@@ -78,6 +78,8 @@ def _declare(L: ctypes.CDLL) -> None:
     L.orc_alm2ring_spin.restype = None
     L.orc_iternorm.argtypes = [dp, ctypes.c_long, ctypes.c_long, ctypes.c_int, dp]
     L.orc_iternorm.restype = ctypes.c_long
+    L.orc_iternorm_dense.argtypes = [dp, ctypes.c_long, ctypes.c_long, ctypes.c_int, dp]
+    L.orc_iternorm_dense.restype = ctypes.c_long
     L.orc_philox4x32_10.argtypes = [u32p, u32p, u32p]
     L.orc_philox4x32_10.restype = None
     L.orc_philox_normals.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int64, ctypes.c_int64, dp, u32p]

@@ -49,13 +49,17 @@ def cls2cov(cls, nl: int, nf: int, nc: int):
         yield cov / 2
 
 
-def iternorm_stack(cov: np.ndarray) -> tuple[np.ndarray, int]:
-    """cov [nrows][nl][k+1] -> (w same shape, first bad row or -1)."""
+def iternorm_stack(cov: np.ndarray, dense: bool = False) -> tuple[np.ndarray, int]:
+    """cov [nrows][nl][k+1] -> (w same shape, first bad row or -1).
+
+    ``dense``: every sum over all k indices (orc_iternorm_dense) instead of
+    over the non-zero block only; the two agree bit for bit."""
     cov = np.ascontiguousarray(cov, dtype=np.float64)
     nrows, nl, kp = cov.shape
     w = np.empty_like(cov)
     dp = ctypes.POINTER(ctypes.c_double)
-    bad = lib().orc_iternorm(cov.ctypes.data_as(dp), nrows, nl, kp - 1, w.ctypes.data_as(dp))
+    fn = lib().orc_iternorm_dense if dense else lib().orc_iternorm
+    bad = fn(cov.ctypes.data_as(dp), nrows, nl, kp - 1, w.ctypes.data_as(dp))
     return w, int(bad)
 
 

@@ -456,6 +456,62 @@ long orc_iternorm(const double *cov, long nrows, long nl, int k, double *w)
     return bad;
 }
 
+/*
+ * The same iternorm with every sum over all k indices (no block restriction):
+ * the straightforward form, against which the block-restricted sums of
+ * orc_iternorm (and of the GPU kernel) are checked bit for bit.
+ */
+long orc_iternorm_dense(const double *cov, long nrows, long nl, int k, double *w)
+{
+    long bad = -1;
+    const int kp = k + 1;
+    for (long l = 0; l < nl; ++l) {
+        double *m = calloc((size_t)(k > 0 ? k * k : 1), sizeof(double));
+        double *mn = calloc((size_t)(k > 0 ? k * k : 1), sizeof(double));
+        double *a = calloc((size_t)(k > 0 ? k : 1), sizeof(double));
+        double *atm = calloc((size_t)(k > 0 ? k : 1), sizeof(double));
+        double s = 1.0;
+        for (long i = 0; i < nrows; ++i) {
+            const double *row = cov + ((size_t)i * nl + l) * kp;
+            if (i > 0 && k > 0) {
+                for (int j = 0; j < k; ++j) {
+                    double acc = 0.0;
+                    for (int p = 0; p < k; ++p) acc = fma(a[p], m[p * k + j], acc);
+                    atm[j] = acc;
+                }
+                double u = s > 0 ? 1.0 : 0.0;
+                double sd = s > 0 ? s : 1.0;
+                for (int r = 0; r < k - 1; ++r)
+                    for (int c = 0; c < k; ++c)
+                        mn[r * k + c] = (c + 1 < k) ? m[(r + 1) * k + (c + 1)] : 0.0;
+                for (int c = 0; c < k; ++c) {
+                    double v = (c + 1 < k) ? -atm[c + 1] : u;
+                    mn[(k - 1) * k + c] = v / sd;
+                }
+                double *t = m; m = mn; mn = t;
+            }
+            double aa = 0.0;
+            for (int r = 0; r < k; ++r) {
+                double acc = 0.0;
+                for (int c = 0; c < k; ++c) acc = fma(m[r * k + c], row[k - c], acc);
+                a[r] = acc;
+            }
+            for (int r = 0; r < k; ++r) aa = fma(a[r], a[r], aa);
+            double sv = row[0] - aa;
+            if (sv < 0) {
+                if (bad < 0 || i < bad) bad = i;
+                sv = 0.0;
+            }
+            s = sqrt(sv);
+            double *wo = w + ((size_t)i * nl + l) * kp;
+            for (int r = 0; r < k; ++r) wo[r] = a[r];
+            wo[k] = s;
+        }
+        free(m); free(mn); free(a); free(atm);
+    }
+    return bad;
+}
+
 /* ------------------------------------------------------------------ philox */
 
 static inline uint32_t mulhilo32(uint32_t a, uint32_t b, uint32_t *hi)

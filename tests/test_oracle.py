@@ -103,6 +103,25 @@ def test_iternorm_reference_test_matrices(golden, k, nd):
         np.testing.assert_allclose(w[i][:, kmax - kk:], ref, rtol=1e-13, atol=1e-16)
 
 
+def test_iternorm_block_sums_equal_dense_sums(golden):
+    """The sums over the non-zero block of m (what the GPU kernel does) give
+    the same bits as sums over all k indices: the skipped terms are exact
+    zeros.  Correlated spectra with k up to 59, perturbed into
+    non-positive-definite cases too."""
+    rng = np.random.default_rng(0)
+    for nshell, k, nl in [(1, 0, 5), (3, 2, 7), (10, 9, 33), (10, 3, 33), (40, 39, 40), (60, 59, 12)]:
+        ell = np.arange(nl)
+        amp = 10 ** rng.uniform(-3, -1, nshell)
+        auto = [a * (ell + 1.0) ** -1.3 for a in amp]
+        gls = [np.exp(-abs(i - j) / 3.0) * np.sqrt(auto[i] * auto[j]) for i in range(nshell) for j in range(i, -1, -1)]
+        cov = np.stack(list(of.cls2cov(gls, nl, nshell, k)))
+        for c in (cov, cov * rng.uniform(0.5, 1.5, cov.shape)):
+            w1, b1 = of.iternorm_stack(c)
+            w2, b2 = of.iternorm_stack(c, dense=True)
+            assert b1 == b2
+            np.testing.assert_array_equal(w1.view(np.uint64), w2.view(np.uint64))
+
+
 def test_iternorm_not_posdef():
     cov = np.array([[[1.0, 0.0]], [[0.1, 1.0]]])  # second row: var 0.1 < corr^2
     _, bad = of.iternorm_stack(cov)
