@@ -104,7 +104,8 @@ struct glg_plan {
     // map of the call in the same grid), each with its own shared memory.
     int nbuckets;
     glg_ring_bucket buckets[GLG_MAX_RING_BUCKETS];
-    int *bucket_pairs;       // ring pairs of all buckets, bucket after bucket
+    int *bucket_pairs;       // ring pairs of all buckets, bucket after bucket (ascending in each)
+    int *bucket_pairs_host;  // host copy (new[]), to launch a bucket over a ring-pair range
     int64_t *pos_ofs;        // [nside+1] offset of the output permutation of n = 4 i
     uint16_t *pos16;         // DIF output position of every frequency, per length
     int64_t *blu_ofs;        // [nside+1] offset of the chirp spectrum of n = 4 i (-1: class 0)
@@ -180,8 +181,21 @@ int glg_launch_ring_syn_f32(const glg_plan *P, const float2 *F, float2 *Ft, int 
 int glg_launch_ring_bucket_f32(const glg_plan *P, int bucket, int threads, const float2 *Ft, int nmaps,
                                float *maps, cudaStream_t st);
 size_t glg_leg_tc_pack_bytes(const glg_plan *P, int nmaps);
+// Ring tiles (128 ring pairs each) of one tensor-core contraction launch, the
+// unit counter it draws from (slot in the status block) and whether the B
+// tiles are packed first (once per call).
+struct glg_tile_run {
+    int tile0, ntiles, slot;
+    bool pack;
+};
 int glg_launch_leg_tc(const glg_plan *P, const float2 *alm, int nmaps, float *bpack, float2 *F,
-                      int *err, cudaStream_t st);
+                      int *err, const glg_tile_run &run, cudaStream_t st);
+// Ring FFTs of the ring pairs [p0, p1) only (transpose included).
+int glg_launch_ring_syn_f32_range(const glg_plan *P, const float2 *F, float2 *Ft, int nmaps, float *maps,
+                                  const glg_epilogue *epi, int p0, int p1, cudaStream_t st);
 
 // Fast-form workspace: [status ints | B pack | F (float2 [map][m][ring])]
+// The status block holds the error word and, from byte 64, the unit
+// counters of the contraction launches of one call.
 #define GLG_WS_STATUS_BYTES 256
+#define GLG_WS_UNIT_COUNTERS 24

@@ -69,7 +69,8 @@ static_assert(W_MMA % 4 != W_MMA2 % 4, "the two MMA-issuing warps on different S
 
 struct LegTcArgs {
     int npairs, nrings, lmax, nmaps, ntiles;
-    int64_t nunits;
+    int tile0, nrun;  // this launch's ring tiles: tile0 .. tile0 + nrun - 1
+    int64_t nunits;   // nrun x (lmax + 1): unit u is tile tile0 + u % nrun of m unit_m(u / nrun)
     const float2 *cth32;
     const float4 *coef32;
     const int64_t *mofs;
@@ -231,8 +232,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
             int64_t u;
             if (!next_unit(ui, u, true)) { ok = false; break; }
             if (u >= a.nunits) break;
-            const int tile = (int)(u % a.ntiles);
-            const int m = unit_m(u / a.ntiles, lmax);
+            const int tile = a.tile0 + (int)(u % a.nrun);
+            const int m = unit_m(u / a.nrun, lmax);
             const int G = (lmax - m + GLG_GROUP) / GLG_GROUP;
             const int p = tile * 128 + r;
             const bool live = p < a.npairs;
@@ -322,8 +323,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
             int64_t u;
             if (!next_unit(ui, u, true)) { ok = false; break; }
             if (u >= a.nunits) break;
-            const int tile = (int)(u % a.ntiles);
-            const int m = unit_m(u / a.ntiles, lmax);
+            const int tile = a.tile0 + (int)(u % a.nrun);
+            const int m = unit_m(u / a.nrun, lmax);
             const int G = (lmax - m + GLG_GROUP) / GLG_GROUP;
             const int gf = a.tfirst[(int64_t)m * a.ntiles + tile];
             for (int g0 = gf; g0 < G; g0 += CH, ++cc) {
@@ -389,8 +390,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
             if (!next_unit(ui, u, false)) { ok = false; break; }
             if (u >= a.nunits) break;
             {
-                const int tile = (int)(u % a.ntiles);
-                const int m = unit_m(u / a.ntiles, lmax);
+                const int tile = a.tile0 + (int)(u % a.nrun);
+                const int m = unit_m(u / a.nrun, lmax);
                 const int G = (lmax - m + GLG_GROUP) / GLG_GROUP;
                 const int gf = a.tfirst[(int64_t)m * a.ntiles + tile];
                 for (int g0 = gf; g0 < G; g0 += CH, ++cc) {
@@ -449,8 +450,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
             if (!next_unit(ui, u, false)) { ok = false; break; }
             if (u >= a.nunits) break;
             {
-                const int tile = (int)(u % a.ntiles);
-                const int m = unit_m(u / a.ntiles, lmax);
+                const int tile = a.tile0 + (int)(u % a.nrun);
+                const int m = unit_m(u / a.nrun, lmax);
                 const int G = (lmax - m + GLG_GROUP) / GLG_GROUP;
                 const int gf = a.tfirst[(int64_t)m * a.ntiles + tile];
                 const int64_t gb = a.goff[m];
@@ -487,8 +488,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
                 S.unit[uq] = u;
                 mbar_arrive(&S.ufull[uq]);  // release: the slot's unit is visible to its readers
                 if (u >= a.nunits) break;
-                const int tile = (int)(u % a.ntiles);
-                const int m = unit_m(u / a.ntiles, lmax);
+                const int tile = a.tile0 + (int)(u % a.nrun);
+                const int m = unit_m(u / a.nrun, lmax);
                 const int G = (lmax - m + GLG_GROUP) / GLG_GROUP;
                 const int64_t gb = a.goff[m];
                 const int64_t cb = a.mofs[m];
@@ -583,8 +584,8 @@ __global__ void __launch_bounds__(256) k_pack_b(int mmax, int lmax, int nmaps, i
 
 template <int N>
 int launch_tc(const glg_plan *P, const float2 *alm, int nmaps, float *bpack, float2 *F, int *err,
-              cudaStream_t st) {
-    {
+              const glg_tile_run &run, cudaStream_t st) {
+    if (run.pack) {
         const int64_t items = P->ngroups * 2 * N;
         GLG_LAUNCH_SCOPE("k_pack_b", st);
         k_pack_b<N><<<(unsigned)((items + 255) / 256), 256, 0, st>>>(P->mmax, P->lmax, nmaps, P->nalm, P->ngroups,
@@ -597,7 +598,14 @@ int launch_tc(const glg_plan *P, const float2 *alm, int nmaps, float *bpack, flo
     a.lmax = P->lmax;
     a.nmaps = nmaps;
     a.ntiles = (P->npairs + 127) / 128;
-    a.nunits = (int64_t)a.ntiles * (P->mmax + 1);
+    a.tile0 = run.tile0;
+    a.nrun = run.ntiles;
+    if (a.tile0 < 0 || a.nrun <= 0 || a.tile0 + a.nrun > a.ntiles || run.slot < 0 ||
+        run.slot >= GLG_WS_UNIT_COUNTERS) {
+        glg_set_error("fast Legendre contraction: tile range or counter slot out of range");
+        return GLG_ERR_INVALID;
+    }
+    a.nunits = (int64_t)a.nrun * (P->mmax + 1);
     a.cth32 = P->cth32;
     a.coef32 = P->coef32;
     a.mofs = P->mofs;
@@ -609,7 +617,8 @@ int launch_tc(const glg_plan *P, const float2 *alm, int nmaps, float *bpack, flo
     a.bpack = reinterpret_cast<const unsigned char *>(bpack);
     a.F = F;
     a.err = err;
-    a.ucount = reinterpret_cast<unsigned long long *>(reinterpret_cast<char *>(err) + 64);
+    // one zeroed counter per launch of a call (the status block is cleared once per call)
+    a.ucount = reinterpret_cast<unsigned long long *>(reinterpret_cast<char *>(err) + 64) + run.slot;
     // more than half of the SM's shared memory: one CTA per SM, so no two
     // CTAs contend for the 512 tensor-memory columns
     size_t smem = sizeof(Smem<N>) + 128;
@@ -633,14 +642,14 @@ size_t glg_leg_tc_pack_bytes(const glg_plan *P, int nmaps) {
 }
 
 int glg_launch_leg_tc(const glg_plan *P, const float2 *alm, int nmaps, float *bpack, float2 *F,
-                      int *err, cudaStream_t st) {
+                      int *err, const glg_tile_run &run, cudaStream_t st) {
     const int N = ((2 * nmaps + 15) / 16) * 16;
     switch (N) {
-        case 16: return launch_tc<16>(P, alm, nmaps, bpack, F, err, st);
-        case 32: return launch_tc<32>(P, alm, nmaps, bpack, F, err, st);
-        case 48: return launch_tc<48>(P, alm, nmaps, bpack, F, err, st);
-        case 64: return launch_tc<64>(P, alm, nmaps, bpack, F, err, st);
-        case 80: return launch_tc<80>(P, alm, nmaps, bpack, F, err, st);
+        case 16: return launch_tc<16>(P, alm, nmaps, bpack, F, err, run, st);
+        case 32: return launch_tc<32>(P, alm, nmaps, bpack, F, err, run, st);
+        case 48: return launch_tc<48>(P, alm, nmaps, bpack, F, err, run, st);
+        case 64: return launch_tc<64>(P, alm, nmaps, bpack, F, err, run, st);
+        case 80: return launch_tc<80>(P, alm, nmaps, bpack, F, err, run, st);
         default:
             glg_set_error("fast Legendre contraction: at most 40 maps per launch");
             return GLG_ERR_UNSUPPORTED;

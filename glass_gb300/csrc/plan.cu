@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include <algorithm>
 #include <complex>
 #include <map>
 #include <mutex>
@@ -207,6 +208,7 @@ extern "C" void glg_plan_destroy(glg_plan *P) {
                     P->chirp, P->pos_ofs, P->pos16,   P->blu_ofs, P->blu_M,  P->blu_H,  P->twM};
     for (void *q : ptrs)
         if (q) cudaFree(q);
+    delete[] P->bucket_pairs_host;
     delete P;
 }
 
@@ -489,6 +491,9 @@ static int build_fft32_tables(glg_plan *P, cudaStream_t st) {
         if (e == cudaSuccess && bytes) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st);
     };
     up(P->bucket_pairs, bpairs.data(), sizeof(int) * bpairs.size());
+    delete[] P->bucket_pairs_host;
+    P->bucket_pairs_host = new int[bpairs.size() ? bpairs.size() : 1];
+    std::copy(bpairs.begin(), bpairs.end(), P->bucket_pairs_host);
     up(P->pos_ofs, pos_ofs.data(), sizeof(int64_t) * pos_ofs.size());
     up(P->pos16, pos16.data(), sizeof(uint16_t) * pos16.size());
     up(P->blu_ofs, blu_ofs.data(), sizeof(int64_t) * blu_ofs.size());

@@ -33,6 +33,8 @@
 // blocks that share a ring's tables run together).
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "glg_internal.cuh"
 
 namespace {
@@ -530,25 +532,26 @@ __global__ void __launch_bounds__(TMAX_POW2) k_ring32_blu(const RingArgs a, cons
     }
 }
 
-// F[map][m][ring] -> Ft[map][ring][m], 32 x 32 tiles.
-__global__ void k_transpose32(const float2 *__restrict__ F, float2 *__restrict__ Ft, int nm, int nr) {
+// F[map][m][ring] -> Ft[map][ring][m] for rings rb .. re-1, 32 x 32 tiles.
+__global__ void k_transpose32(const float2 *__restrict__ F, float2 *__restrict__ Ft, int nm, int nr, int rb,
+                              int re) {
     __shared__ float2 tile[32][33];
     const int map = blockIdx.z;
-    const int r0 = blockIdx.x * 32, m0 = blockIdx.y * 32;
+    const int r0 = rb + blockIdx.x * 32, m0 = blockIdx.y * 32;
     const float2 *src = F + (int64_t)map * nm * nr;
     float2 *dst = Ft + (int64_t)map * nm * nr;
     float2 v[4];  // blockDim.y == 8: four loads in flight per thread
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
         const int y = threadIdx.y + 8 * i, m = m0 + y, r = r0 + threadIdx.x;
-        v[i] = (m < nm && r < nr) ? src[(int64_t)m * nr + r] : make_float2(0.f, 0.f);
+        v[i] = (m < nm && r < re) ? src[(int64_t)m * nr + r] : make_float2(0.f, 0.f);
     }
 #pragma unroll
     for (int i = 0; i < 4; ++i) tile[threadIdx.y + 8 * i][threadIdx.x] = v[i];
     __syncthreads();
     for (int y = threadIdx.y; y < 32; y += blockDim.y) {
         const int r = r0 + y, m = m0 + threadIdx.x;
-        if (m < nm && r < nr) dst[(int64_t)r * nm + m] = tile[threadIdx.x][y];
+        if (m < nm && r < re) dst[(int64_t)r * nm + m] = tile[threadIdx.x][y];
     }
 }
 
@@ -578,11 +581,14 @@ static void ring_args(const glg_plan *P, const float2 *Ft, int nmaps, float *map
     a.npix = P->npix;
 }
 
+// Pairs lo .. lo+count-1 of bucket B (the whole bucket by default).
 static int launch_bucket(const glg_plan *P, const glg_ring_bucket &B, int threads, RingArgs a, const Epi32 &e,
-                         cudaStream_t st) {
-    a.pairs = P->bucket_pairs + B.first;
+                         cudaStream_t st, int lo = 0, int count = -1) {
+    if (count < 0) count = B.count;
+    if (count == 0) return GLG_OK;
+    a.pairs = P->bucket_pairs + B.first + lo;
     const size_t smem = glg_ring32_smem(B.kind, B.size, threads, B.fold != 0);
-    const unsigned grid = (unsigned)B.count * (unsigned)a.nmaps;
+    const unsigned grid = (unsigned)count * (unsigned)a.nmaps;
     if (B.kind == 1) {
         cudaFuncSetAttribute(k_ring32_blu, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         GLG_LAUNCH_SCOPE("k_ring32_blu", st);
@@ -602,11 +608,30 @@ static int launch_bucket(const glg_plan *P, const glg_ring_bucket &B, int thread
     return GLG_OK;
 }
 
+static int launch_transpose(const float2 *F, float2 *Ft, int nm, int nr, int rb, int re, int nmaps,
+                            cudaStream_t st) {
+    if (re <= rb) return GLG_OK;
+    dim3 grid((re - rb + 31) / 32, (nm + 31) / 32, nmaps);
+    GLG_LAUNCH_SCOPE("k_transpose32", st);
+    k_transpose32<<<grid, dim3(32, 8), 0, st>>>(F, Ft, nm, nr, rb, re);
+    GLG_CHECK_LAUNCH("k_transpose32");
+    return GLG_OK;
+}
+
 int glg_launch_ring_syn_f32(const glg_plan *P, const float2 *F, float2 *Ft, int nmaps, float *maps,
                             const glg_epilogue *epi_in, cudaStream_t st) {
+    return glg_launch_ring_syn_f32_range(P, F, Ft, nmaps, maps, epi_in, 0, P->npairs, st);
+}
+
+int glg_launch_ring_syn_f32_range(const glg_plan *P, const float2 *F, float2 *Ft, int nmaps, float *maps,
+                                  const glg_epilogue *epi_in, int p0, int p1, cudaStream_t st) {
     if (nmaps > EPI_MAX) {
         glg_set_error("fast ring FFT: at most 40 maps per call");
         return GLG_ERR_UNSUPPORTED;
+    }
+    if (p0 < 0 || p1 > P->npairs || p0 >= p1) {
+        glg_set_error("fast ring FFT: empty or out-of-range ring-pair range");
+        return GLG_ERR_INVALID;
     }
     const int nm = P->mmax + 1, nr = P->nrings;
     for (int b = 0; b < P->nbuckets; ++b)
@@ -614,12 +639,11 @@ int glg_launch_ring_syn_f32(const glg_plan *P, const float2 *F, float2 *Ft, int 
             glg_set_error("fast ring FFT: ring length too large for shared memory (nside <= 2048)");
             return GLG_ERR_UNSUPPORTED;
         }
-    {
-        dim3 grid((nr + 31) / 32, (nm + 31) / 32, nmaps);
-        GLG_LAUNCH_SCOPE("k_transpose32", st);
-        k_transpose32<<<grid, dim3(32, 8), 0, st>>>(F, Ft, nm, nr);
-        GLG_CHECK_LAUNCH("k_transpose32");
-    }
+    // north rings p0 .. p1-1 and their south partners nr-p1 .. nr-1-p0 (the
+    // equator ring, pair npairs-1, is its own partner)
+    int rc = launch_transpose(F, Ft, nm, nr, p0, p1, nmaps, st);
+    if (!rc) rc = launch_transpose(F, Ft, nm, nr, nr - p1 > p1 ? nr - p1 : p1, nr - p0, nmaps, st);
+    if (rc) return rc;
     RingArgs a;
     ring_args(P, Ft, nmaps, maps, a);
     Epi32 e;
@@ -629,8 +653,16 @@ int glg_launch_ring_syn_f32(const glg_plan *P, const float2 *F, float2 *Ft, int 
         e.hvar[k] = (on && epi_in->var) ? (float)(0.5 * epi_in->var[k]) : 0.f;
         e.lam[k] = (on && epi_in->lamda) ? (float)epi_in->lamda[k] : 1.f;
     }
+    const bool whole = p0 == 0 && p1 == P->npairs;
     for (int b = 0; b < P->nbuckets; ++b) {
-        const int rc = launch_bucket(P, P->buckets[b], P->buckets[b].threads, a, e, st);
+        const glg_ring_bucket &B = P->buckets[b];
+        int lo = 0, hi = B.count;
+        if (!whole) {  // a bucket's pairs ascend: the range is one slice of them
+            const int *bp = P->bucket_pairs_host + B.first;
+            lo = (int)(std::lower_bound(bp, bp + B.count, p0) - bp);
+            hi = (int)(std::lower_bound(bp, bp + B.count, p1) - bp);
+        }
+        const int rc = launch_bucket(P, B, B.threads, a, e, st, lo, hi - lo);
         if (rc) return rc;
     }
     return GLG_OK;

@@ -55,7 +55,8 @@ extern "C" int glg_alm2map(const glg_plan *P, const void *alm, int nmaps, int fo
         cudaError_t e = cudaMemsetAsync(err, 0, GLG_WS_STATUS_BYTES, st);
         if (e != cudaSuccess) return glg_cuda_status(e, "glg_alm2map: status reset");
         float2 *Ft = F + (size_t)nmaps * P->nrings * (P->mmax + 1);
-        rc = glg_launch_leg_tc(P, (const float2 *)alm, nmaps, bpack, F, err, st);
+        const glg_tile_run all{0, (P->npairs + 127) / 128, 0, true};
+        rc = glg_launch_leg_tc(P, (const float2 *)alm, nmaps, bpack, F, err, all, st);
         if (rc) return rc;
         return glg_launch_ring_syn_f32(P, F, Ft, nmaps, (float *)maps, epi, st);
     }
@@ -63,6 +64,98 @@ extern "C" int glg_alm2map(const glg_plan *P, const void *alm, int nmaps, int fo
     int rc = glg_launch_leg_syn(P, (const double2 *)alm, nmaps, F, st);
     if (rc) return rc;
     return glg_launch_ring_syn(P, F, nmaps, (double *)maps, epi, st);
+}
+
+extern "C" size_t glg_alm2map_host_workspace(const glg_plan *P, int nmaps) {
+    if (!P || nmaps <= 0) return 0;
+    return glg_alm2map_workspace(P, nmaps, GLG_FORM_FAST) + sizeof(float) * (size_t)nmaps * P->npix;
+}
+
+namespace {
+
+// HEALPix RING first pixel of the north and south rings of pair p (the
+// formulas of the plan's ring table, on the host).
+int64_t ring_startN(const glg_plan *P, int p) {
+    const int64_t ir = p + 1, ns = P->nside;
+    return ir < ns ? 2 * ir * (ir - 1) : 2 * ns * (ns - 1) + (ir - ns) * 4 * ns;
+}
+int64_t ring_startS(const glg_plan *P, int p) {
+    const int64_t ir = p + 1, ns = P->nside;
+    return ir < ns ? P->npix - 2 * ir * (ir + 1) : 2 * ns * (ns - 1) + (3 * ns - ir) * 4 * ns;
+}
+int64_t ring_nph(const glg_plan *P, int p) { return p + 1 < P->nside ? 4LL * (p + 1) : 4LL * P->nside; }
+
+}  // namespace
+
+extern "C" int glg_alm2map_host(const glg_plan *P, const void *alm, int nmaps, void *maps_host,
+                                const glg_epilogue *epi, void *ws, size_t ws_bytes, void *stream) {
+    GLG_REQUIRE(P != nullptr, "glg_alm2map_host: null plan");
+    GLG_REQUIRE(nmaps >= 0 && nmaps <= 40, "glg_alm2map_host: nmaps must be in [0, 40]");
+    if (nmaps == 0) return GLG_OK;
+    GLG_REQUIRE(alm && maps_host, "glg_alm2map_host: null pointer");
+    GLG_REQUIRE(ws && ws_bytes >= glg_alm2map_host_workspace(P, nmaps), "glg_alm2map_host: workspace too small");
+    cudaStream_t st = (cudaStream_t)stream;
+    int rc = glg_plan_prepare_fast(const_cast<glg_plan *>(P), st);
+    if (rc) return rc;
+    int *err = (int *)ws;
+    float *bpack = (float *)((char *)ws + GLG_WS_STATUS_BYTES);
+    float2 *F = (float2 *)((char *)ws + GLG_WS_STATUS_BYTES + fast_pack_bytes(P, nmaps));
+    float2 *Ft = F + (size_t)nmaps * P->nrings * (P->mmax + 1);
+    float *stage = (float *)(Ft + (size_t)nmaps * P->nrings * (P->mmax + 1));
+    cudaError_t e = cudaMemsetAsync(err, 0, GLG_WS_STATUS_BYTES, st);
+    if (e != cudaSuccess) return glg_cuda_status(e, "glg_alm2map_host: status reset");
+
+    // Ring tiles in runs from the equator to the poles: each run's maps go to
+    // the host on a copy stream while the next run computes, and the last
+    // run (the polar caps) has the fewest pixels left to copy at the end.
+    const int ntiles = (P->npairs + 127) / 128;
+    const int nrun = ntiles < 8 ? ntiles : 8;
+    cudaStream_t cs = nullptr;
+    cudaEvent_t ev[9] = {};
+    int made = 0;
+    e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+    for (; e == cudaSuccess && made <= nrun; ++made) e = cudaEventCreateWithFlags(&ev[made], cudaEventDisableTiming);
+    if (e != cudaSuccess) rc = glg_cuda_status(e, "glg_alm2map_host: copy stream");
+    // every run's sums and ring FFTs first, then every run's copies (a copy
+    // into pageable memory returns only when done: it must not hold back the
+    // launches of later runs)
+    int started = 0;
+    for (int k = 0; !rc && k < nrun; ++k) {
+        const int t1 = ntiles - (int)((int64_t)ntiles * k / nrun), t0 = ntiles - (int)((int64_t)ntiles * (k + 1) / nrun);
+        const int p0 = t0 * 128, p1 = t1 * 128 < P->npairs ? t1 * 128 : P->npairs;
+        const glg_tile_run run{t0, t1 - t0, k, k == 0};
+        rc = glg_launch_leg_tc(P, (const float2 *)alm, nmaps, bpack, F, err, run, st);
+        if (!rc) rc = glg_launch_ring_syn_f32_range(P, F, Ft, nmaps, stage, epi, p0, p1, st);
+        if (!rc && (e = cudaEventRecord(ev[k], st)) != cudaSuccess) rc = glg_cuda_status(e, "glg_alm2map_host: event");
+        if (!rc) ++started;
+    }
+    const size_t pitch = sizeof(float) * (size_t)P->npix;
+    for (int k = 0; k < started && !rc; ++k) {
+        const int t1 = ntiles - (int)((int64_t)ntiles * k / nrun), t0 = ntiles - (int)((int64_t)ntiles * (k + 1) / nrun);
+        const int p0 = t0 * 128, p1 = t1 * 128 < P->npairs ? t1 * 128 : P->npairs;
+        // north rings p0 .. p1-1, then the south rings of pairs p0 .. q1-1
+        // (all but the equator, which is its own south ring)
+        const int q1 = p1 < P->npairs ? p1 : P->npairs - 1;
+        int64_t band[2][2] = {{ring_startN(P, p0), ring_startN(P, p1 - 1) + ring_nph(P, p1 - 1)}, {0, 0}};
+        if (q1 > p0) band[1][0] = ring_startS(P, q1 - 1), band[1][1] = ring_startS(P, p0) + ring_nph(P, p0);
+        e = cudaStreamWaitEvent(cs, ev[k], 0);
+        for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
+            const int64_t a0 = band[b][0], a1 = band[b][1];
+            if (a1 > a0)
+                e = cudaMemcpy2DAsync((float *)maps_host + a0, pitch, stage + a0, pitch, sizeof(float) * (size_t)(a1 - a0),
+                                      (size_t)nmaps, cudaMemcpyDeviceToHost, cs);
+        }
+        if (e != cudaSuccess) rc = glg_cuda_status(e, "glg_alm2map_host: map copy");
+    }
+    // the caller's stream resumes after the last copy (also after a failure:
+    // nothing may still be reading the workspace when it is reused)
+    if (cs && made > nrun) {
+        if (cudaEventRecord(ev[nrun], cs) == cudaSuccess) cudaStreamWaitEvent(st, ev[nrun], 0);
+        else cudaStreamSynchronize(cs);
+    }
+    for (int k = 0; k < made; ++k) cudaEventDestroy(ev[k]);  // released once complete
+    if (cs) cudaStreamDestroy(cs);
+    return rc;
 }
 
 extern "C" int glg_host_device_pointer(const void *host, void **dev) {

@@ -354,22 +354,10 @@ def _generate_grf(gls, nside: int, *, ncorr=None, rng=None, form: str | None = N
             raise ValueError(b.bad_msg)
 
 
-_HOST_MAPPED: list[bool] = []  # whether pinned host memory is device-addressable here
-
-
-def _pinned_maps(nmaps: int, npix: int) -> torch.Tensor | None:
-    """Pinned float32 [nmaps, npix] host buffer that kernels can write into
-    directly, or None where pinned memory is not mapped into the device."""
-    if _HOST_MAPPED == [False]:
-        return None
-    out = torch.empty((nmaps, npix), dtype=torch.float32, pin_memory=True)
-    try:
-        _lib.host_device_pointer(out)
-    except ValueError:
-        _HOST_MAPPED[:] = [False]
-        return None
-    _HOST_MAPPED[:] = [True]
-    return out
+def _pinned_maps(nmaps: int, npix: int) -> torch.Tensor:
+    """Pinned float32 [nmaps, npix] host buffer (recycled by torch's caching
+    host allocator) for the fast form's host-output synthesis."""
+    return torch.empty((nmaps, npix), dtype=torch.float32, pin_memory=True)
 
 
 def _to_host(maps: torch.Tensor) -> list[np.ndarray]:
@@ -421,8 +409,8 @@ def _generate(fields, gls, nside, ncorr, rng, form):
                    [kinds[t][1] if fused[s] else 1.0 for s, t in enumerate(range(t0, t0 + cnt))])
             host = _pinned_maps(cnt, 12 * b.nside * b.nside) if b.numpy_out and form == "fast" else None
             if host is not None:
-                # the ring FFTs store the float32 maps straight into pinned
-                # host memory while they run: no device-to-host copy after
+                # each run of ring tiles is copied to the pinned buffer while
+                # the next run computes: little copying is left after the last
                 b.maps(t0, cnt, epi=epi, out=host)
                 torch.cuda.current_stream(b.device).synchronize()
                 maps = [h.numpy() for h in host]

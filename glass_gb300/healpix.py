@@ -157,8 +157,9 @@ def buckets(nside: int, lmax: int) -> list[dict]:
 
 def _synth_fast(alm: torch.Tensor, nside: int, lmax: int, epilogue, out: torch.Tensor | None = None) -> torch.Tensor:
     """Fast-form synthesis into new device maps, or into ``out``: float32
-    [nmaps, npix] on the device or in pinned host memory, which the ring FFTs
-    then write across the CPU-GPU link while they run (no separate copy)."""
+    [nmaps, npix] on the device, or in host memory (pinned, for the copies to
+    overlap), which glg_alm2map_host fills run by run while the next run of
+    ring tiles computes."""
     plan = get_plan(nside, lmax, alm.device)
     alm = alm.to(torch.complex64).contiguous()
     nmaps = alm.shape[0]
@@ -167,10 +168,14 @@ def _synth_fast(alm: torch.Tensor, nside: int, lmax: int, epilogue, out: torch.T
     else:
         if out.dtype != torch.float32 or tuple(out.shape) != (nmaps, plan.npix) or not out.is_contiguous():
             raise ValueError("out must be a contiguous float32 [nmaps, npix] tensor")
+        if not (out.is_cuda or out.device.type == "cpu"):
+            raise ValueError("out must be a CUDA or CPU tensor")
         maps = out
-    base = ptr(maps) if maps.is_cuda else _lib.host_device_pointer(maps)
+    to_host = not maps.is_cuda
+    base = ptr(maps) if maps.is_cuda else maps.data_ptr()
     step = min(nmaps, FAST_MAX_MAPS)
-    ws_bytes = int(lib().glg_alm2map_workspace(plan.handle, step, _lib.FORM_FAST))
+    ws_bytes = int(lib().glg_alm2map_host_workspace(plan.handle, step) if to_host else
+                   lib().glg_alm2map_workspace(plan.handle, step, _lib.FORM_FAST))
     ws = torch.empty(ws_bytes, dtype=torch.uint8, device=alm.device)
     stream = c_p(stream_ptr(alm.device))
     if not getattr(plan, "tuned", False):  # time the FFT buckets on device maps
@@ -183,9 +188,14 @@ def _synth_fast(alm: torch.Tensor, nside: int, lmax: int, epilogue, out: torch.T
             kind, var, lam = epilogue
             kinds = list(kind) if isinstance(kind, (list, tuple)) else [int(kind)] * nmaps
             epi = _make_epilogue((kinds[m0:m0 + cnt], var[m0:m0 + cnt], lam[m0:m0 + cnt]), cnt)
-        check(lib().glg_alm2map(plan.handle, c_p(ptr(alm[m0:m0 + cnt])), cnt, _lib.FORM_FAST,
-                                c_p(base + 4 * m0 * plan.npix), ctypes.byref(epi) if epi is not None else None,
-                                c_p(ptr(ws)), ws_bytes, stream), "glg_alm2map (fast)")
+        epi_p = ctypes.byref(epi) if epi is not None else None
+        if to_host:
+            check(lib().glg_alm2map_host(plan.handle, c_p(ptr(alm[m0:m0 + cnt])), cnt, c_p(base + 4 * m0 * plan.npix),
+                                         epi_p, c_p(ptr(ws)), ws_bytes, stream), "glg_alm2map_host")
+        else:
+            check(lib().glg_alm2map(plan.handle, c_p(ptr(alm[m0:m0 + cnt])), cnt, _lib.FORM_FAST,
+                                    c_p(base + 4 * m0 * plan.npix), epi_p, c_p(ptr(ws)), ws_bytes, stream),
+                  "glg_alm2map (fast)")
     check(lib().glg_workspace_status(c_p(ptr(ws)), stream), "glg_alm2map (fast)")
     return maps
 

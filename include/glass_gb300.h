@@ -238,6 +238,25 @@ int glg_alm2map(const glg_plan *plan, const void *alm, int nmaps, int form, void
  * GLG_ERR_INVALID for any other pointer.  No counterpart in the reference. */
 int glg_host_device_pointer(const void *host, void **dev);
 
+/*
+ * Fast-form spin-0 synthesis into HOST maps: float32 [nmaps][npix] at
+ * maps_host, alm complex64 [nmaps][nalm] on the device, at most 40 maps.
+ * Same result as glg_alm2map(GLG_FORM_FAST) into device maps, then copied.
+ * The transform runs in ring-tile runs from the equator to the poles; each
+ * run's pixel bands are copied to the host (one 2-D copy per band on a copy
+ * stream of the call) while the next run computes, so most of the copy hides
+ * behind the computation.  maps_host should be page-locked (cudaHostAlloc or
+ * cudaHostRegister) for the copies to overlap; pageable memory works, but
+ * the call then returns only after its copies end.  The caller's stream
+ * waits for the last copy.  workspace: glg_alm2map_host_workspace() bytes
+ * (the fast-form workspace plus device staging maps); its status word is
+ * read by glg_workspace_status() as for glg_alm2map.  Host-side entry of
+ * glass/fields.py:839-894 (generate) when numpy maps are wanted.
+ */
+size_t glg_alm2map_host_workspace(const glg_plan *plan, int nmaps);
+int glg_alm2map_host(const glg_plan *plan, const void *alm, int nmaps, void *maps_host,
+                     const glg_epilogue *epi, void *workspace, size_t workspace_bytes, void *stream);
+
 /* Status word of a fast-form workspace (synchronises `stream`): GLG_OK or
  * GLG_ERR_TIMEOUT.  No counterpart in the reference (no device waits there). */
 int glg_workspace_status(const void *workspace, void *stream);

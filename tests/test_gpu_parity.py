@@ -550,28 +550,33 @@ def test_autotuner_picks_block_sizes(g):
     assert rel_rms(got.cpu().numpy(), osht.alm2map(alm, nside, lmax)) < FAST_RMS
 
 
-def test_fast_maps_written_to_pinned_host_memory(g):
-    """Fast synthesis into a pinned host buffer (the ring FFTs store across
-    the CPU-GPU link) gives the same bits as into device memory; generate
-    with numpy spectra (which takes that route) equals it with torch spectra."""
+@pytest.mark.parametrize(("nside", "lmax"), [(64, 128), (256, 512), (512, 1024)])
+def test_fast_maps_written_to_host_memory(g, nside, lmax):
+    """Fast synthesis into host memory (glg_alm2map_host: ring-tile runs from
+    the equator to the poles, each copied while the next computes; 1, 4 and
+    8 runs here) gives the same bits as into device memory, pinned or
+    pageable, with a fused epilogue; generate with numpy spectra (which takes
+    that route) equals it with torch spectra."""
     import torch
 
     from glass_gb300 import healpix as hp
 
-    nside, lmax, nm = 64, 128, 3
+    nm = 3
+    epi = ([g._lib.EPI_LOGNORMAL, g._lib.EPI_NONE, g._lib.EPI_LOGNORMAL], [0.2, 0.0, 0.5], [1.0, 1.0, 2.0])
     alm = torch.as_tensor(random_alm(lmax, seed=8, nmaps=nm) * 0.1, device="cuda").to(torch.complex64)
-    ref = hp.synth(alm, nside, lmax, form="fast")
-    host = torch.empty((nm, 12 * nside * nside), dtype=torch.float32, pin_memory=True)
-    try:
-        g._lib.host_device_pointer(host)
-    except ValueError:
-        pytest.skip("pinned host memory is not mapped into the device here")
-    got = hp.synth(alm, nside, lmax, form="fast", out=host)
-    torch.cuda.synchronize()
-    assert got is host
-    torch.testing.assert_close(host, ref.cpu(), rtol=0, atol=0)
+    ref = hp.synth(alm, nside, lmax, epilogue=epi, form="fast").cpu()
+    for pinned in (True, False):
+        host = torch.full((nm, 12 * nside * nside), float("nan"), dtype=torch.float32, pin_memory=pinned)
+        got = hp.synth(alm, nside, lmax, epilogue=epi, form="fast", out=host)
+        torch.cuda.synchronize()
+        assert got is host
+        torch.testing.assert_close(host, ref, rtol=0, atol=0)
+    if nside != 64:
+        return
+    pinned = torch.empty((nm, 12 * nside * nside), dtype=torch.float32, pin_memory=True)
+    g._lib.host_device_pointer(pinned)  # mapped pinned memory has a device address
     with pytest.raises(ValueError):
-        g._lib.host_device_pointer(torch.empty(4))  # pageable memory is refused
+        g._lib.host_device_pointer(torch.empty(4))  # pageable memory has none
     gls, lam = spectra_cfg2(4, 2 * nside)
     fields = [g.grf.Lognormal(float(x)) for x in lam]
     a = list(g.generate(fields, gls, nside, rng=g.rng.Generator(3), form="fast"))
