@@ -248,7 +248,9 @@ int glg_host_device_pointer(const void *host, void **dev);
  * behind the computation.  maps_host should be page-locked (cudaHostAlloc or
  * cudaHostRegister) for the copies to overlap; pageable memory works, but
  * the call then returns only after its copies end.  The caller's stream
- * waits for the last copy.  workspace: glg_alm2map_host_workspace() bytes
+ * waits for the last copy.  The call creates and destroys its copy stream:
+ * do not capture it into a CUDA graph (glg_alm2map into device maps can
+ * be).  workspace: glg_alm2map_host_workspace() bytes
  * (the fast-form workspace plus device staging maps); its status word is
  * read by glg_workspace_status() as for glg_alm2map.  Host-side entry of
  * glass/fields.py:839-894 (generate) when numpy maps are wanted.
