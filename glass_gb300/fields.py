@@ -253,11 +253,13 @@ class _FieldBatcher:
         # concatenated spectra, then iternorm of every field in one launch
         offs = np.concatenate([[0], np.cumsum(lens)]).astype(np.int64)
         if self.numpy_out:
-            if all(isinstance(g, np.ndarray) and g.dtype == np.float64 and g.ndim == 1 for g in gls):
-                flat_h = np.concatenate(gls)
-            else:
-                flat_h = np.concatenate([np.asarray(g, dtype=np.float64).reshape(-1) for g in gls if g is not None])
-            flat = torch.from_numpy(flat_h).to(self.device)
+            # concatenated straight into pinned memory: one asynchronous copy
+            # (the caching host allocator keeps the buffer until it is done)
+            parts = gls if all(isinstance(g, np.ndarray) and g.dtype == np.float64 and g.ndim == 1 for g in gls) \
+                else [np.asarray(g, dtype=np.float64).reshape(-1) for g in gls if g is not None]
+            flat_h = torch.empty(int(offs[-1]), dtype=torch.float64, pin_memory=True)
+            np.concatenate(parts, out=flat_h.numpy())
+            flat = flat_h.to(self.device, non_blocking=True)
         else:
             dev, f64 = self.device, torch.float64
             flat = torch.cat([g if (isinstance(g, torch.Tensor) and g.dtype == f64 and g.device == dev
