@@ -112,9 +112,13 @@ extern "C" int glg_alm2map_host(const glg_plan *P, const void *alm, int nmaps, v
     const int nrun = ntiles < 8 ? ntiles : 8;
     cudaStream_t cs = nullptr;
     cudaEvent_t ev[9] = {};
-    int made = 0;
+    int made = 0;  // events created: one per run and one for the final join
     e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
-    for (; e == cudaSuccess && made <= nrun; ++made) e = cudaEventCreateWithFlags(&ev[made], cudaEventDisableTiming);
+    if (e != cudaSuccess) cs = nullptr;
+    while (e == cudaSuccess && made <= nrun) {
+        e = cudaEventCreateWithFlags(&ev[made], cudaEventDisableTiming);
+        if (e == cudaSuccess) ++made;
+    }
     if (e != cudaSuccess) rc = glg_cuda_status(e, "glg_alm2map_host: copy stream");
     // every run's sums and ring FFTs first, then every run's copies (a copy
     // into pageable memory returns only when done: it must not hold back the
