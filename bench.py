@@ -386,6 +386,8 @@ def run_ours(args, rank: int, world: int) -> dict | None:
         ngal = 5.0 * npix / g.points.ARCMIN2_SPHERE
         gen = g.rng.Generator(7)
         g.points.counts_from_delta(ngal, maps[0], rng=gen)  # warm-up
+        for _ in g.points.positions_from_delta(ngal, maps[1], batch=100_000_000, rng=gen):
+            pass  # warm-up: the batches' buffers come from the allocator's cache in the timed pass
         torch.cuda.synchronize()
         _lib.timing_enable(True)
         _lib.timing_reset()
