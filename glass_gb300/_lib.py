@@ -74,6 +74,7 @@ _SIGNATURES = {
     "glg_alm2map": ([c_p, c_p, c_i, c_i, c_p, ctypes.POINTER(Epilogue), c_p, c_sz, c_p], c_i),
     "glg_alm2map_host_workspace": ([c_p, c_i], c_sz),
     "glg_alm2map_host": ([c_p, c_p, c_i, c_p, ctypes.POINTER(Epilogue), c_p, c_sz, c_p], c_i),
+    "glg_host_output_runs": ([c_i, c_p, c_i], c_i),
     "glg_workspace_status": ([c_p, c_p], c_i),
     "glg_alm2map_noalloc": ([c_i, c_i, c_p, c_i, c_p, c_p], c_i),
     "glg_peak_tf32": ([c_i, c_i, c_p, c_p], c_i),

@@ -73,19 +73,64 @@ extern "C" size_t glg_alm2map_host_workspace(const glg_plan *P, int nmaps) {
 
 namespace {
 
-// HEALPix RING first pixel of the north and south rings of pair p (the
-// formulas of the plan's ring table, on the host).
-int64_t ring_startN(const glg_plan *P, int p) {
-    const int64_t ir = p + 1, ns = P->nside;
+// HEALPix RING first pixel and length of the north and south rings of pair p
+// (the formulas of the plan's ring table, on the host).
+int64_t ring_startN(int nside, int p) {
+    const int64_t ir = p + 1, ns = nside;
     return ir < ns ? 2 * ir * (ir - 1) : 2 * ns * (ns - 1) + (ir - ns) * 4 * ns;
 }
-int64_t ring_startS(const glg_plan *P, int p) {
-    const int64_t ir = p + 1, ns = P->nside;
-    return ir < ns ? P->npix - 2 * ir * (ir + 1) : 2 * ns * (ns - 1) + (3 * ns - ir) * 4 * ns;
+int64_t ring_startS(int nside, int p) {
+    const int64_t ir = p + 1, ns = nside;
+    return ir < ns ? 12 * ns * ns - 2 * ir * (ir + 1) : 2 * ns * (ns - 1) + (3 * ns - ir) * 4 * ns;
 }
-int64_t ring_nph(const glg_plan *P, int p) { return p + 1 < P->nside ? 4LL * (p + 1) : 4LL * P->nside; }
+int64_t ring_nph(int nside, int p) { return p + 1 < nside ? 4LL * (p + 1) : 4LL * nside; }
+
+// Run k of the host-output synthesis: ring tiles t0 .. t1-1 (128 pairs each,
+// counted from the equator end), ring pairs p0 .. p1-1, and its two pixel
+// bands [band[b][0], band[b][1]) in every map: the north rings p0 .. p1-1,
+// then the south rings of pairs p0 .. q1-1 (all but the equator, which is its
+// own south ring; an empty band is [0, 0)).
+constexpr int kHostRuns = 8;
+struct HostRun {
+    int t0, t1, p0, p1;
+    int64_t band[2][2];
+};
+int host_run_count(int nside) {
+    const int ntiles = (2 * nside + 127) / 128;
+    return ntiles < kHostRuns ? ntiles : kHostRuns;
+}
+HostRun host_run(int nside, int k) {
+    const int npairs = 2 * nside, ntiles = (npairs + 127) / 128, nrun = host_run_count(nside);
+    HostRun r;
+    r.t1 = ntiles - (int)((int64_t)ntiles * k / nrun);
+    r.t0 = ntiles - (int)((int64_t)ntiles * (k + 1) / nrun);
+    r.p0 = r.t0 * 128;
+    r.p1 = r.t1 * 128 < npairs ? r.t1 * 128 : npairs;
+    const int q1 = r.p1 < npairs ? r.p1 : npairs - 1;
+    r.band[0][0] = ring_startN(nside, r.p0);
+    r.band[0][1] = ring_startN(nside, r.p1 - 1) + ring_nph(nside, r.p1 - 1);
+    r.band[1][0] = r.band[1][1] = 0;
+    if (q1 > r.p0) {
+        r.band[1][0] = ring_startS(nside, q1 - 1);
+        r.band[1][1] = ring_startS(nside, r.p0) + ring_nph(nside, r.p0);
+    }
+    return r;
+}
 
 }  // namespace
+
+extern "C" int glg_host_output_runs(int nside, int64_t *out, int max_runs) {
+    GLG_REQUIRE(nside >= 1 && nside <= 8192, "glg_host_output_runs: nside must be in [1, 8192]");
+    GLG_REQUIRE(out != nullptr, "glg_host_output_runs: null pointer");
+    const int nrun = host_run_count(nside);
+    GLG_REQUIRE(max_runs >= nrun, "glg_host_output_runs: max_runs below the run count");
+    for (int k = 0; k < nrun; ++k) {
+        const HostRun r = host_run(nside, k);
+        const int64_t row[8] = {r.t0, r.t1, r.p0, r.p1, r.band[0][0], r.band[0][1], r.band[1][0], r.band[1][1]};
+        for (int j = 0; j < 8; ++j) out[8 * k + j] = row[j];
+    }
+    return nrun;
+}
 
 extern "C" int glg_alm2map_host(const glg_plan *P, const void *alm, int nmaps, void *maps_host,
                                 const glg_epilogue *epi, void *ws, size_t ws_bytes, void *stream) {
@@ -108,10 +153,9 @@ extern "C" int glg_alm2map_host(const glg_plan *P, const void *alm, int nmaps, v
     // Ring tiles in runs from the equator to the poles: each run's maps go to
     // the host on a copy stream while the next run computes, and the last
     // run (the polar caps) has the fewest pixels left to copy at the end.
-    const int ntiles = (P->npairs + 127) / 128;
-    const int nrun = ntiles < 8 ? ntiles : 8;
+    const int nrun = host_run_count(P->nside);
     cudaStream_t cs = nullptr;
-    cudaEvent_t ev[9] = {};
+    cudaEvent_t ev[kHostRuns + 1] = {};
     int made = 0;  // events created: one per run and one for the final join
     e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
     if (e != cudaSuccess) cs = nullptr;
@@ -125,26 +169,19 @@ extern "C" int glg_alm2map_host(const glg_plan *P, const void *alm, int nmaps, v
     // launches of later runs)
     int started = 0;
     for (int k = 0; !rc && k < nrun; ++k) {
-        const int t1 = ntiles - (int)((int64_t)ntiles * k / nrun), t0 = ntiles - (int)((int64_t)ntiles * (k + 1) / nrun);
-        const int p0 = t0 * 128, p1 = t1 * 128 < P->npairs ? t1 * 128 : P->npairs;
-        const glg_tile_run run{t0, t1 - t0, k, k == 0};
+        const HostRun r = host_run(P->nside, k);
+        const glg_tile_run run{r.t0, r.t1 - r.t0, k, k == 0};
         rc = glg_launch_leg_tc(P, (const float2 *)alm, nmaps, bpack, F, err, run, st);
-        if (!rc) rc = glg_launch_ring_syn_f32_range(P, F, Ft, nmaps, stage, epi, p0, p1, st);
+        if (!rc) rc = glg_launch_ring_syn_f32_range(P, F, Ft, nmaps, stage, epi, r.p0, r.p1, st);
         if (!rc && (e = cudaEventRecord(ev[k], st)) != cudaSuccess) rc = glg_cuda_status(e, "glg_alm2map_host: event");
         if (!rc) ++started;
     }
     const size_t pitch = sizeof(float) * (size_t)P->npix;
     for (int k = 0; k < started && !rc; ++k) {
-        const int t1 = ntiles - (int)((int64_t)ntiles * k / nrun), t0 = ntiles - (int)((int64_t)ntiles * (k + 1) / nrun);
-        const int p0 = t0 * 128, p1 = t1 * 128 < P->npairs ? t1 * 128 : P->npairs;
-        // north rings p0 .. p1-1, then the south rings of pairs p0 .. q1-1
-        // (all but the equator, which is its own south ring)
-        const int q1 = p1 < P->npairs ? p1 : P->npairs - 1;
-        int64_t band[2][2] = {{ring_startN(P, p0), ring_startN(P, p1 - 1) + ring_nph(P, p1 - 1)}, {0, 0}};
-        if (q1 > p0) band[1][0] = ring_startS(P, q1 - 1), band[1][1] = ring_startS(P, p0) + ring_nph(P, p0);
+        const HostRun r = host_run(P->nside, k);
         e = cudaStreamWaitEvent(cs, ev[k], 0);
         for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
-            const int64_t a0 = band[b][0], a1 = band[b][1];
+            const int64_t a0 = r.band[b][0], a1 = r.band[b][1];
             if (a1 > a0)
                 e = cudaMemcpy2DAsync((float *)maps_host + a0, pitch, stage + a0, pitch, sizeof(float) * (size_t)(a1 - a0),
                                       (size_t)nmaps, cudaMemcpyDeviceToHost, cs);

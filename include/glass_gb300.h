@@ -259,6 +259,14 @@ size_t glg_alm2map_host_workspace(const glg_plan *plan, int nmaps);
 int glg_alm2map_host(const glg_plan *plan, const void *alm, int nmaps, void *maps_host,
                      const glg_epilogue *epi, void *workspace, size_t workspace_bytes, void *stream);
 
+/* The runs glg_alm2map_host makes at this nside (host arithmetic only, no
+ * device): per run 8 int64 into out[8 * max_runs]: ring tiles t0, t1
+ * (128 ring pairs each), ring pairs p0, p1, then the pixel bands [n0, n1)
+ * (north rings) and [s0, s1) (south rings; [0, 0) when empty).  Returns the
+ * run count, or GLG_ERR_INVALID (nside outside [1, 8192], max_runs below the
+ * count).  No counterpart in the reference. */
+int glg_host_output_runs(int nside, int64_t *out, int max_runs);
+
 /* Status word of a fast-form workspace (synchronises `stream`): GLG_OK or
  * GLG_ERR_TIMEOUT.  No counterpart in the reference (no device waits there). */
 int glg_workspace_status(const void *workspace, void *stream);

@@ -53,3 +53,36 @@ def test_invalid_arguments_report_errors_without_gpu():
     assert rc == _lib.GLG_ERR_INVALID
     assert "null plan" in _lib.last_error()
     assert lib.glg_alm2map_host_workspace(None, 3) == 0
+
+
+def test_host_output_runs_tile_the_rings_and_pixels():
+    """The runs of glg_alm2map_host (host arithmetic of the C library): tiles
+    and ring pairs from the equator end down to pair 0, and pixel bands that
+    hold exactly each run's rings and together cover every pixel once."""
+    import numpy as np
+
+    from glass_gb300 import _lib
+
+    lib = _lib.load_library(require_gpu=False)
+    out = np.zeros(8 * 8, dtype=np.int64)
+    for nside in [2 ** e for e in range(14)]:
+        n = lib.glg_host_output_runs(nside, out.ctypes.data, 8)
+        npairs, npix = 2 * nside, 12 * nside * nside
+        ntiles = (npairs + 127) // 128
+        assert n == min(ntiles, 8)
+        runs = out[:8 * n].reshape(n, 8)
+        nph = np.array([4 * (p + 1) if p + 1 < nside else 4 * nside for p in range(npairs)], dtype=np.int64)
+        assert runs[0, 1] == ntiles and runs[-1, 0] == 0 and runs[0, 3] == npairs and runs[-1, 2] == 0
+        bands = []
+        for k, (t0, t1, p0, p1, n0, n1, s0, s1) in enumerate(runs):
+            assert t0 < t1 and p0 == 128 * t0 and p1 == min(128 * t1, npairs)
+            if k:
+                assert t1 == runs[k - 1, 0] and p1 == runs[k - 1, 2]
+            q1 = p1 if p1 < npairs else npairs - 1  # the equator has no separate south ring
+            assert n1 - n0 == nph[p0:p1].sum() and s1 - s0 == nph[p0:q1].sum()
+            bands += [(n0, n1)] + ([(s0, s1)] if s1 > s0 else [])
+        bands.sort()
+        assert bands[0][0] == 0 and bands[-1][1] == npix
+        assert all(a[1] == b[0] for a, b in zip(bands, bands[1:]))
+    assert lib.glg_host_output_runs(0, out.ctypes.data, 8) == _lib.GLG_ERR_INVALID
+    assert lib.glg_host_output_runs(2048, out.ctypes.data, 7) == _lib.GLG_ERR_INVALID
