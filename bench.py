@@ -214,9 +214,10 @@ def measured_peaks() -> dict:
 
 def tf32_peak_tflops(peaks: dict) -> tuple[float, str]:
     """Dense TF32 tensor peak: the tcgen05 kind::tf32 rate measured by
-    ``bench.py --peaks`` (kept in peaks_tf32_fp64.json), else half the
-    measured dense bf16 rate (same tensor pipe, tf32 at half the bf16 rate)."""
-    p = ROOT / "peaks_tf32_fp64.json"
+    ``bench.py --peaks`` (kept in profiles/peaks_tf32_fp64.json), else half
+    the measured dense bf16 rate (same tensor pipe, tf32 at half the bf16
+    rate)."""
+    p = ROOT / "profiles" / "peaks_tf32_fp64.json"
     if p.exists():
         return float(json.loads(p.read_text())["tf32_tflops"]), "tf32 tcgen05 loop (of measured)"
     bf = peaks.get("bf16_tflops", 1900.0)
@@ -357,6 +358,12 @@ def run_ours(args, rank: int, world: int) -> dict | None:
                 "traffic": traffic, "traffic_unit": "bytes per launch", "peak_note": peak_note, "passes": 3,
                 "issued_frac": (3 * achieved / peak_tf) if achieved else None,
                 "algorithmic_flops_per_launch": flops}
+    # the same figure against the measured bf16 GEMM rate halved (the
+    # tensor pipe's tf32 rate is half its bf16 rate)
+    bf_half = peaks.get("bf16_tflops", 1900.0) / 2.0
+    roofline["vs_bf16_half"] = {"peak": bf_half, "frac": (achieved / bf_half) if achieved else None,
+                                "issued_frac": (3 * achieved / bf_half) if achieved else None,
+                                "note": "of measured" if "fallback" not in peaks else "of fallback"}
     if rank != 0:
         return None
 

@@ -1,9 +1,9 @@
 """Generate the golden fixtures of the field-generation path from the reference.
 
 Runs the reference's OWN Python (glass.fields, glass.harmonics, glass.grf)
-unmodified, imported from a GLASS checkout given by ``--reference`` (default
-``/root/reference``), with the small stand-in modules of
-``tests/golden/shims/`` on ``sys.path`` for dependencies that are not
+unmodified, imported from a GLASS checkout given by ``--reference``, with
+the small stand-in modules of ``tests/golden/shims/`` on ``sys.path`` for
+dependencies that are not
 installed offline (array_api_compat, array_api_extra, transformcl, healpy,
 healpix, cosmology).  healpy's transform is replaced by ``oracle.sht`` while
 capturing exactly the alm the reference hands to it, so the fixtures pin:
@@ -59,7 +59,7 @@ def spectra_cfg2(nshell: int, lmax: int, seed: int = 0):
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", required=True, help="path of a GLASS source checkout")
     ap.add_argument("--out", default=str(HERE / "glass_fields.npz"))
     args = ap.parse_args()
 

@@ -1,6 +1,6 @@
 """Golden C_l file written by the reference's own ``glass.user.save_cls``
 (glass/user.py:42-64), imported unmodified from a GLASS checkout
-(``--reference``, default ``/root/reference``) with the stand-in modules of
+(``--reference``) with the stand-in modules of
 ``tests/golden/shims/``.  The spectra are seeded (4 spectra of lengths 5, 7,
 7, 3), so the file pins the reference's on-disk layout for
 ``glass_gb300.save_cls`` / ``load_cls``.
@@ -27,7 +27,7 @@ def spectra():
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", required=True, help="path of a GLASS source checkout")
     ap.add_argument("--out", default=str(HERE / "glass_cls_ref.npz"))
     args = ap.parse_args()
     sys.path[:0] = [str(HERE / "shims"), args.reference]

@@ -3,7 +3,7 @@
 Runs the reference's OWN glass.lensing.MultiPlaneConvergence
 (glass/lensing.py:511-586) and glass.galaxies.galaxy_shear
 (glass/galaxies.py:271-347), imported unmodified from a GLASS checkout
-(``--reference``, default ``/root/reference``) with the stand-in modules of
+(``--reference``) with the stand-in modules of
 ``tests/golden/shims/``, the flat LambdaCDM of ``tests/golden/cosmo_stub.py``
 as the cosmology, and healpy's ang2pix / npix2nside (healpy is not installed
 offline) replaced by the oracle's RING restatement.  The fixtures pin the
@@ -37,7 +37,7 @@ def planes(dtype, nside: int = 16, n: int = 6, seed: int = 3):
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", required=True, help="path of a GLASS source checkout")
     ap.add_argument("--out", default=str(HERE / "glass_lensing.npz"))
     args = ap.parse_args()
     sys.path[:0] = [str(HERE / "shims"), args.reference, str(ROOT), str(HERE)]
