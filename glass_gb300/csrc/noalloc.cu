@@ -2,17 +2,18 @@
 // device memory.
 //
 // Some callers cannot call cudaMalloc at the point where they need a map:
-// code running inside CUDA stream capture (allocation is not capturable),
-// real-time or embedded loops whose memory is fixed at start-up, or hosts
-// whose device memory is owned by another allocator that must not be
-// bypassed.  This entry point serves them: it needs no plan and no workspace
+// real-time or embedded loops whose device memory is fixed at start-up (an
+// allocation there can fail or stall the loop), or host programs whose device
+// memory is owned by another allocator (a framework's caching pool, a memory
+// budget enforced per process) that must not be bypassed.  This entry point serves them: it needs no plan and no workspace
 // and calls no allocating routine.  Ring geometry, Legendre coefficients and
 // Fourier phases are computed on the fly in FP64, and the per-ring Legendre
 // sums go into one fixed scratch array that lives in the library's own
 // device memory (GLG_NOALLOC_SCRATCH_BYTES, held by every GPU that loads the
 // library until the process exits).
 //
-// Limits: nside <= 256 (ring length <= 1024) and
+// Limits: nside <= 256 (ring length <= 1024), lmax + 1 <= 65535 and
+// nmaps <= 65535 (the grid's y dimensions) and
 // nmaps * (4 nside - 1) * (lmax + 1) * 16 bytes <= GLG_NOALLOC_SCRATCH_BYTES;
 // larger requests are rejected with GLG_ERR_UNSUPPORTED.  All calls share the
 // scratch array, so calls whose kernels overlap on the GPU (different
@@ -20,7 +21,9 @@
 // entry a call reads is written earlier in the same call, so nothing has to
 // start at zero.  The first call on a device looks up the array's device
 // address (cudaGetSymbolAddress); make that first call before any stream
-// capture begins.
+// capture begins.  The address is kept per device index, so the entry point
+// assumes the CUDA runtime's primary context of each device (the context
+// every runtime-API caller shares).
 #include <cuda_runtime.h>
 #include <math.h>
 
@@ -201,6 +204,10 @@ extern "C" int glg_alm2map_noalloc(int nside, int lmax, const void *alm, int nma
     GLG_REQUIRE(lmax >= 0 && nmaps >= 1, "glg_alm2map_noalloc: bad lmax or nmaps");
     if (nside > NA_MAX_NSIDE) {
         glg_set_error("glg_alm2map_noalloc: nside above 256 (the fixed-size path's limit)");
+        return GLG_ERR_UNSUPPORTED;
+    }
+    if (lmax + 1 > 65535 || nmaps > 65535) {
+        glg_set_error("glg_alm2map_noalloc: lmax + 1 and nmaps must each be at most 65535 (grid y limit)");
         return GLG_ERR_UNSUPPORTED;
     }
     const size_t need = sizeof(double2) * (size_t)nmaps * (4 * nside - 1) * (size_t)(lmax + 1);

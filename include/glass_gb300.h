@@ -292,20 +292,41 @@ int glg_map2alm(const glg_plan *plan, const void *maps, int nmaps, int niter, vo
                 void *workspace, size_t workspace_bytes, void *stream);
 
 /*
+ * HEALPix pixel window functions, replacing healpy.pixwin as called at
+ * glass/healpix.py:351 (and used by glass/lensing.py:360-362 for discretized
+ * shear).  healpy reads them from data files; here they are computed on the
+ * device from their definition: pw0_l^2 = mean over pixels of the pair
+ * average <<P_l(cos gamma)>> over two uniform points of the pixel (the
+ * pixel-averaged harmonics' power), pw2_l^2 the same with the spin-2 kernel
+ * d^l_22 (pw2_l = 0 for l < 2).  One pass accumulates the pixels' pair
+ * moments <<sin^2(gamma/2)^k>> (8 x 8 Gauss-Legendre nodes on each half of
+ * every pixel's diamond in the equal-area HEALPix projection, one pixel per
+ * congruence class); every l follows from the hypergeometric series of the
+ * kernels in sin^2(gamma/2).  pw0, pw2: float64 [lmax+1] (pw2 may be NULL).
+ * Limits: 1 <= nside <= 8192, lmax <= 4 nside.  Parity with healpy's
+ * tables is not established (they are not available offline).
+ */
+size_t glg_pixwin_workspace(int nside);
+int glg_pixwin(int nside, int lmax, double *pw0, double *pw2, void *ws, size_t ws_bytes, void *stream);
+
+/*
  * Spin-0 synthesis that allocates nothing.  No counterpart in the reference:
  * it exists for callers that cannot call cudaMalloc where they need a map --
- * code inside CUDA stream capture (allocation cannot be captured), loops
- * whose device memory is fixed at start-up, or programs whose device memory
- * belongs to an allocator that must not be bypassed.  It needs no plan and no
+ * loops whose device memory is fixed at start-up (an allocation there can
+ * fail or stall the loop), or programs whose device memory belongs to an
+ * allocator (a framework's caching pool, a per-process memory budget) that
+ * must not be bypassed.  It needs no plan and no
  * workspace: alm complex128 [nmaps][nalm] (HEALPix order, lmax), maps float64
  * [nmaps][npix]; FP64 throughout, same result as glg_alm2map's plain form.
  * Its scratch is one fixed array of GLG_NOALLOC_SCRATCH_BYTES in the
  * library's device memory, held by every GPU that loads the library until
- * the process exits.  Limits: nside <= 256 and
- * nmaps * (4 nside - 1) * (lmax + 1) * 16 <= GLG_NOALLOC_SCRATCH_BYTES, else
- * GLG_ERR_UNSUPPORTED.  All calls share that array: calls that overlap on the
- * GPU race, so serialise them.  The first call on each device looks up the
- * array's address; make it before any stream capture begins.
+ * the process exits.  Limits: nside <= 256, lmax + 1 <= 65535, nmaps <= 65535
+ * and nmaps * (4 nside - 1) * (lmax + 1) * 16 <= GLG_NOALLOC_SCRATCH_BYTES,
+ * else GLG_ERR_UNSUPPORTED.  All calls share that array: calls that overlap
+ * on the GPU race, so serialise them.  The first call on each device looks up
+ * the array's address; make it before any stream capture begins.  The
+ * address is kept per device index: the entry point assumes the CUDA
+ * runtime's primary context of each device.
  */
 #define GLG_NOALLOC_SCRATCH_BYTES (16u << 20)
 int glg_alm2map_noalloc(int nside, int lmax, const void *alm, int nmaps, void *maps, void *stream);

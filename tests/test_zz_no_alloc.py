@@ -1,13 +1,14 @@
 """GPU test of glg_alm2map_noalloc, the synthesis entry point that allocates nothing.
 
-It serves callers that cannot call cudaMalloc where they need a map (code
-inside CUDA stream capture, fixed-memory loops, programs whose device memory
-belongs to another allocator).  This test calls it through the C ABI and
-checks it against the plan-and-workspace entry point glg_alm2map (plain FP64
-form) to the plain form's tolerance, 1e-12 relative, on two calls in a row
-with different inputs -- the second call must not see the first call's
-scratch contents.  The file is collected last so that a run stopping at the
-first failure has already run every other test.
+It serves callers that cannot call cudaMalloc where they need a map (loops
+whose device memory is fixed at start-up, programs whose device memory belongs
+to another allocator).  This test calls it through the C ABI and checks it
+against the plan-and-workspace entry point glg_alm2map (plain FP64 form) to
+the plain form's tolerance, 1e-12 relative, on two calls in a row with
+different inputs -- the second call must not see the first call's scratch
+contents -- and on a small call right after a large one.  The file is
+collected last so that a run stopping at the first failure has already run
+every other test.
 """
 
 from __future__ import annotations
@@ -56,6 +57,15 @@ def test_noalloc_matches_alm2map_twice(cuda_lib, nside, lmax, nmaps):
         assert rel_err(got, ref) < TOL
 
 
+def test_noalloc_small_after_large(cuda_lib):
+    # the large call fills more of the shared scratch array than the small
+    # one writes: the small call must read only entries it wrote itself
+    big = random_alm(150, seed=11, nmaps=3)
+    assert rel_err(_noalloc(cuda_lib, big, 64, 150), _plain(big, 64, 150)) < TOL
+    small = random_alm(20, seed=12, nmaps=1)
+    assert rel_err(_noalloc(cuda_lib, small, 16, 20), _plain(small, 16, 20)) < TOL
+
+
 def test_noalloc_rejects_oversize(cuda_lib):
     import torch
 
@@ -69,3 +79,10 @@ def test_noalloc_rejects_oversize(cuda_lib):
     rc = cuda_lib.glg_alm2map_noalloc(256, 1500, ctypes.c_void_p(a.data_ptr()), 8,
                                       ctypes.c_void_p(out.data_ptr()), None)
     assert rc == _lib.GLG_ERR_UNSUPPORTED and "scratch" in _lib.last_error()
+    # fits the scratch array at nside 1 but not the launch grid
+    rc = cuda_lib.glg_alm2map_noalloc(1, 70000, ctypes.c_void_p(a.data_ptr()), 1,
+                                      ctypes.c_void_p(out.data_ptr()), None)
+    assert rc == _lib.GLG_ERR_UNSUPPORTED and "65535" in _lib.last_error()
+    rc = cuda_lib.glg_alm2map_noalloc(1, 0, ctypes.c_void_p(a.data_ptr()), 70000,
+                                      ctypes.c_void_p(out.data_ptr()), None)
+    assert rc == _lib.GLG_ERR_UNSUPPORTED and "65535" in _lib.last_error()
