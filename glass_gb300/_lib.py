@@ -77,6 +77,10 @@ _SIGNATURES = {
     "glg_host_output_runs": ([c_i, c_p, c_i], c_i),
     "glg_workspace_status": ([c_p, c_p], c_i),
     "glg_alm2map_noalloc": ([c_i, c_i, c_p, c_i, c_p, c_p], c_i),
+    "glg_pixwin_workspace": ([c_i], c_sz),
+    "glg_pixwin": ([c_i, c_i, c_p, c_p, c_p, c_sz, c_p], c_i),
+    "glg_test_fail_plan_alloc": ([c_i], c_i),
+    "glg_test_stall_contraction": ([c_i, ctypes.c_uint], c_i),
     "glg_peak_tf32": ([c_i, c_i, c_p, c_p], c_i),
     "glg_host_device_pointer": ([c_p, ctypes.POINTER(c_p)], c_i),
     "glg_peak_fma": ([c_i, c_i, c_i, c_p, c_p], c_i),
@@ -234,6 +238,15 @@ def get_plan(nside: int, lmax: int, device: torch.device | None = None) -> Plan:
 def clear_plans() -> None:
     with _PLAN_LOCK:
         _PLANS.clear()
+
+
+def drop_plan(nside: int, lmax: int, device: torch.device | None = None) -> None:
+    """Remove one plan from the cache (its device memory is freed once no
+    caller holds the Plan object any more)."""
+    device = torch.device("cuda", torch.cuda.current_device()) if device is None else device
+    key = (device.index if device.index is not None else torch.cuda.current_device(), nside, lmax)
+    with _PLAN_LOCK:
+        _PLANS.pop(key, None)
 
 
 # -------------------------------------------------------------- conversion

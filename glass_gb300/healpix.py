@@ -105,23 +105,31 @@ FAST_MAX_MAPS = 40  # maps per fast-form launch (N = 80 tensor-core columns)
 
 
 def synth(alm: torch.Tensor, nside: int, lmax: int, *, epilogue=None, form: str = "plain",
-          out: torch.Tensor | None = None) -> torch.Tensor:
+          out: torch.Tensor | None = None, ws: torch.Tensor | None = None,
+          status: torch.Tensor | None = None) -> torch.Tensor:
     """Spin-0 synthesis of alm [nmaps, nalm] -> maps [nmaps, npix].
 
     ``form="plain"``: complex128 alm, float64 maps (FP64 throughout).
     ``form="fast"``: complex64 alm, float32 maps (tensor-core Legendre sums);
     ``out`` may be a float32 [nmaps, npix] device tensor or pinned host
     tensor to write the maps into.
+    ``ws``: a caller-owned uint8 device workspace of at least
+    ``workspace_bytes(...)`` bytes (allocated per call otherwise).
+    ``status`` (fast form, device maps): a pinned int32 host tensor of one
+    element that receives the call's device-wait status asynchronously
+    instead of the call synchronising to check it (the caller reads it once
+    the stream has passed the call; non-zero = a bounded wait timed out).
     """
     if form == "fast":
-        return _synth_fast(alm, nside, lmax, epilogue, out)
+        return _synth_fast(alm, nside, lmax, epilogue, out, ws, status)
     if out is not None:
         raise ValueError("out is supported by the fast form only")
     plan = get_plan(nside, lmax, alm.device)
     nmaps = alm.shape[0]
     maps = torch.empty((nmaps, plan.npix), dtype=torch.float64, device=alm.device)
     ws_bytes = int(lib().glg_alm2map_workspace(plan.handle, nmaps, _lib.FORM_PLAIN))
-    ws = torch.empty(max(ws_bytes, 1), dtype=torch.uint8, device=alm.device)
+    if ws is None or ws.numel() < ws_bytes:
+        ws = torch.empty(max(ws_bytes, 1), dtype=torch.uint8, device=alm.device)
     epi = _make_epilogue(epilogue, nmaps)
     check(lib().glg_alm2map(plan.handle, c_p(ptr(alm)), nmaps, _lib.FORM_PLAIN, c_p(ptr(maps)),
                             ctypes.byref(epi) if epi is not None else None, c_p(ptr(ws)), ws_bytes,
@@ -155,7 +163,15 @@ def buckets(nside: int, lmax: int) -> list[dict]:
                  ms=float(ms[i])) for i in range(n)]
 
 
-def _synth_fast(alm: torch.Tensor, nside: int, lmax: int, epilogue, out: torch.Tensor | None = None) -> torch.Tensor:
+def workspace_bytes(nside: int, lmax: int, nmaps: int, form: str = "fast", device=None) -> int:
+    """Device workspace of one synthesis call of ``nmaps`` maps (device maps)."""
+    plan = get_plan(nside, lmax, device)
+    f = _lib.FORM_FAST if form == "fast" else _lib.FORM_PLAIN
+    return int(lib().glg_alm2map_workspace(plan.handle, min(nmaps, FAST_MAX_MAPS) if form == "fast" else nmaps, f))
+
+
+def _synth_fast(alm: torch.Tensor, nside: int, lmax: int, epilogue, out: torch.Tensor | None = None,
+                ws: torch.Tensor | None = None, status: torch.Tensor | None = None) -> torch.Tensor:
     """Fast-form synthesis into new device maps, or into ``out``: float32
     [nmaps, npix] on the device, or in host memory (pinned, for the copies to
     overlap), which glg_alm2map_host fills run by run while the next run of
@@ -176,7 +192,10 @@ def _synth_fast(alm: torch.Tensor, nside: int, lmax: int, epilogue, out: torch.T
     step = min(nmaps, FAST_MAX_MAPS)
     ws_bytes = int(lib().glg_alm2map_host_workspace(plan.handle, step) if to_host else
                    lib().glg_alm2map_workspace(plan.handle, step, _lib.FORM_FAST))
-    ws = torch.empty(ws_bytes, dtype=torch.uint8, device=alm.device)
+    if ws is None or ws.numel() < ws_bytes:
+        ws = torch.empty(ws_bytes, dtype=torch.uint8, device=alm.device)
+    else:
+        ws_bytes = ws.numel()
     stream = c_p(stream_ptr(alm.device))
     if not getattr(plan, "tuned", False):  # time the FFT buckets on device maps
         autotune(plan, step, maps[:step] if maps.is_cuda else
@@ -196,7 +215,10 @@ def _synth_fast(alm: torch.Tensor, nside: int, lmax: int, epilogue, out: torch.T
             check(lib().glg_alm2map(plan.handle, c_p(ptr(alm[m0:m0 + cnt])), cnt, _lib.FORM_FAST,
                                     c_p(base + 4 * m0 * plan.npix), epi_p, c_p(ptr(ws)), ws_bytes, stream),
                   "glg_alm2map (fast)")
-    check(lib().glg_workspace_status(c_p(ptr(ws)), stream), "glg_alm2map (fast)")
+    if status is not None and not to_host and nmaps <= step:  # one call: one status word
+        status.copy_(ws[:4].view(torch.int32), non_blocking=True)
+    else:
+        check(lib().glg_workspace_status(c_p(ptr(ws)), stream), "glg_alm2map (fast)")
     return maps
 
 
@@ -271,12 +293,9 @@ def alm2map(alms, nside: int, *, inplace: bool = False, lmax: int | None = None,
 
     ``alms`` is one complex array, or a sequence of them; with ``pol=True``
     and three arrays they are (T, E, B) and (T, Q, U) maps are returned.
-    ``pixwin=True`` needs HEALPix pixel-window tables and is not supported.
+    ``pixwin=True`` multiplies the alm by the pixel window (temperature
+    window for spin 0, polarisation window for E and B), as healpy does.
     """
-    if pixwin:
-        raise NotImplementedError(
-            "pixwin=True needs HEALPix pixel-window tables, which are not available"
-        )
     seq = isinstance(alms, (list, tuple))
     items = list(alms) if seq else [alms]
     numpy_out = all(_lib.is_numpy_like(a) for a in items)
@@ -289,6 +308,12 @@ def alm2map(alms, nside: int, *, inplace: bool = False, lmax: int | None = None,
     n = dev[0].shape[-1]
     lmax_in = _lmax_from_size(n)
     lmax = lmax_in if lmax is None else int(lmax)
+    if pixwin:
+        pw0, pw2 = pixwin_device(nside, lmax, dev[0].device)
+        pw0 = pw0[: min(lmax, lmax_in) + 1]
+        pw2 = pw2[: min(lmax, lmax_in) + 1]
+        pols = seq and pol and len(dev) == 3
+        dev = [almxfl(d, pw2 if (pols and i > 0) else pw0) for i, d in enumerate(dev)]
     if seq and pol and len(dev) == 3:
         t = synth(_resize_alm(dev[0], lmax_in, lmax)[None], nside, lmax)[0]
         q, u = _spin_synth(_resize_alm(dev[1], lmax_in, lmax), _resize_alm(dev[2], lmax_in, lmax),
@@ -402,8 +427,47 @@ def almxfl(alm, fl, *, inplace: bool = False):
     return res
 
 
+_PIXWIN: dict[tuple[int, int, int], tuple[torch.Tensor, torch.Tensor]] = {}
+
+
+def pixwin_device(nside: int, lmax: int, device: torch.device | None = None):
+    """(pw0, pw2) float64 [lmax+1] device tensors, computed once per
+    (device, nside, lmax) by glg_pixwin and cached."""
+    device = torch.device("cuda", torch.cuda.current_device()) if device is None else device
+    key = (device.index if device.index is not None else torch.cuda.current_device(), int(nside), int(lmax))
+    hit = _PIXWIN.get(key)
+    if hit is not None:
+        return hit
+    pw0 = torch.empty(lmax + 1, dtype=torch.float64, device=device)
+    pw2 = torch.empty_like(pw0)
+    ws_bytes = int(lib().glg_pixwin_workspace(int(nside)))
+    if ws_bytes == 0:
+        raise ValueError("pixwin: nside must be in [1, 8192]")
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device=device)
+    check(lib().glg_pixwin(int(nside), int(lmax), c_p(ptr(pw0)), c_p(ptr(pw2)), c_p(ptr(ws)), ws_bytes,
+                           c_p(stream_ptr(device))), "glg_pixwin")
+    _PIXWIN[key] = (pw0, pw2)
+    return pw0, pw2
+
+
 def pixwin(nside: int, *, lmax: int | None = None, pol: bool = False, xp=None):
-    """HEALPix pixel window functions: the tables are not available here."""
-    raise NotImplementedError(
-        "HEALPix pixel-window tables are not available; use discretized=False"
-    )
+    """Pixel window function(s) of HEALPix pixels at ``nside``
+    (glass/healpix.py:313-356, healpy.pixwin): the temperature window, or
+    (temperature, polarisation) with ``pol=True``; ``lmax`` defaults to
+    3 nside - 1.
+
+    healpy reads these from data files that are not available offline; they
+    are computed on the GPU from their definition instead (the pixel-averaged
+    harmonics' power, spin 0 and spin 2), see ``glg_pixwin`` in
+    include/glass_gb300.h.  ``xp``: the array namespace of the result
+    (numpy by default; ``torch`` gives CUDA tensors).
+    """
+    lmax = 3 * int(nside) - 1 if lmax is None else int(lmax)
+    pw0, pw2 = pixwin_device(nside, lmax)
+    if xp is not None and xp is torch:
+        return (pw0.clone(), pw2.clone()) if pol else pw0.clone()
+    a0 = pw0.cpu().numpy()
+    if not pol:
+        return a0 if xp is None else xp.asarray(a0, dtype=xp.float64)
+    a2 = pw2.cpu().numpy()
+    return (a0, a2) if xp is None else (xp.asarray(a0, dtype=xp.float64), xp.asarray(a2, dtype=xp.float64))

@@ -24,8 +24,9 @@ def from_convergence(kappa, lmax: int | None = None, *, potential: bool = False,
                      deflection: bool = False, shear: bool = False, discretized: bool = True):
     """Potential, deflection and/or shear from a convergence map (glass/lensing.py:185-371).
 
-    ``discretized=True`` needs the HEALPix pixel-window tables (pw2 / pw0),
-    which are not available: pass ``discretized=False``.
+    ``discretized=True`` (the default) scales the shear's harmonic kernel by
+    the ratio of the spin-2 and spin-0 pixel windows pw2 / pw0
+    (glass/lensing.py:360-362), computed on the GPU by ``healpix.pixwin``.
     """
     if not (potential or deflection or shear):
         return ()
@@ -34,8 +35,6 @@ def from_convergence(kappa, lmax: int | None = None, *, potential: bool = False,
     nside = hp.get_nside(k)
     if lmax is None:
         lmax = 3 * nside - 1
-    if shear and discretized:
-        hp.pixwin(nside, lmax=lmax, pol=True)  # raises: tables unavailable
     alm = hp.analysis(k.reshape(1, -1), lmax, 3)[0]
     ell = _ell(lmax, k)
     results: tuple = ()
@@ -63,7 +62,11 @@ def from_convergence(kappa, lmax: int | None = None, *, potential: bool = False,
     # deflection -> shear: sqrt((l-1)(l+2)) / 2, 0 at l = 0
     fl = np.zeros_like(ell)
     fl[1:] = np.sqrt((ell[1:] - 1) * (ell[1:] + 2)) / 2
-    alm = hp.almxfl(alm, torch.as_tensor(fl, device=alm.device))
+    flt = torch.as_tensor(fl, device=alm.device)
+    if discretized:  # factor out the spin-0 pixel window, apply the spin-2 one
+        pw0, pw2 = hp.pixwin_device(nside, lmax, alm.device)
+        flt = flt * (pw2 / pw0)
+    alm = hp.almxfl(alm, flt)
     q, u = hp._spin_synth(alm, None, nside, 2, lmax)
     results += (out(torch.complex(q, u)),)
     return results
@@ -76,14 +79,16 @@ def shear_from_convergence(kappa, lmax: int | None = None, *, discretized: bool 
     nside = hp.get_nside(k)
     if lmax is None:
         lmax = 3 * nside - 1
-    if discretized:
-        hp.pixwin(nside, lmax=lmax, pol=True)
     alm = hp.analysis(k.reshape(1, -1), lmax, 3)[0]
     ell = np.arange(lmax + 1)
     fl = np.sqrt((ell + 2.0) * (ell + 1) * ell * (ell - 1))
     fl /= np.clip(ell * (ell + 1), 1, None)
     fl *= -1
-    alm = hp.almxfl(alm, torch.as_tensor(fl, device=alm.device))
+    flt = torch.as_tensor(fl, device=alm.device)
+    if discretized:
+        pw0, pw2 = hp.pixwin_device(nside, lmax, alm.device)
+        flt = flt * (pw2 / pw0)
+    alm = hp.almxfl(alm, flt)
     q, u = hp._spin_synth(alm, None, nside, 2, lmax)
     return [q.cpu().numpy(), u.cpu().numpy()] if numpy_out else [q, u]
 

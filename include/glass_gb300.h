@@ -332,6 +332,21 @@ int glg_pixwin(int nside, int lmax, double *pw0, double *pw2, void *ws, size_t w
 int glg_alm2map_noalloc(int nside, int lmax, const void *alm, int nmaps, void *maps, void *stream);
 
 /*
+ * Failure injection for tests (no counterpart in the reference).
+ * glg_test_fail_plan_alloc(n): the n-th device allocation of plan creation
+ * from now (1 = the next) fails as if cudaMalloc had run out of memory, so
+ * the caller sees GLG_ERR_NOMEM (0 clears it).
+ * glg_test_stall_contraction(on, polls): while on, the fast contraction's B
+ * streamer issues no copies, so its MMA warps' waits run out after `polls`
+ * polls; the kernel then records GLG_ERR_TIMEOUT in the workspace status
+ * word, retires what it started, frees its tensor memory and returns (no
+ * fault, no trap; the context stays usable).  Off restores the normal wait
+ * limit.  Process-wide settings, for tests only.
+ */
+int glg_test_fail_plan_alloc(int nth);
+int glg_test_stall_contraction(int on, unsigned int polls);
+
+/*
  * Launch accounting (no counterpart in the reference, which has no GPU
  * code): every kernel launch of this library is counted; with timing
  * enabled each launch is bracketed by CUDA events on its own stream and
