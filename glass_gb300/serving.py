@@ -70,21 +70,59 @@ class Request:
         return None if self.finished is None else self.finished - self.arrival
 
 
+def _ngroups(lmax: int) -> int:
+    """16-l groups of the fast contraction's B operand: sum_m ceil((lmax-m+1)/16)."""
+    return sum((lmax - m + 16) // 16 for m in range(lmax + 1))
+
+
 def request_bytes(nside: int, lmax: int, nshell: int, form: str = "fast") -> int:
-    """Device bytes a request holds: alm, maps and w/cov (twice as many alm
-    and map bytes in the FP64 form)."""
-    nalm = (lmax + 1) * (lmax + 2) // 2
+    """Device bytes a request holds while it is served: its spectra, cls2cov
+    rows, iternorm rows (and their float32 copy), alm and maps (alm complex128
+    and maps float64 in the FP64 form)."""
+    n = lmax + 1
+    nalm = n * (n + 1) // 2
     npix = 12 * nside * nside
     f = 2 if form == "plain" else 1
-    return nshell * f * (8 * nalm + 4 * npix) + 2 * 8 * nshell * (lmax + 1) * nshell
+    nspec = nshell * (nshell + 1) // 2
+    return (8 * nspec * n + 2 * 8 * nshell * n * nshell + 4 * nshell * n * nshell
+            + nshell * f * (8 * nalm + 4 * npix))
 
 
-def launch_bytes(nside: int, lmax: int, nmaps: int) -> int:
-    """Workspace of one fast transform launch (B pack + Legendre sums)."""
-    nalm = (lmax + 1) * (lmax + 2) // 2
-    ngroups = nalm // 16 + lmax + 1
-    n = ((2 * nmaps + 15) // 16) * 16
-    return ngroups * 128 * n + 8 * nmaps * (4 * nside - 1) * (lmax + 1) + nmaps * (lmax + 1) * 8
+def launch_bytes(nside: int, lmax: int, nmaps: int, form: str = "fast") -> int:
+    """Device bytes of one (nside, lmax) group's launch buffers for up to
+    ``nmaps`` maps: the transform workspace (fast: status block, B pack and two
+    copies of the Legendre sums; plain: the FP64 sums), the staged alm and the
+    staged maps."""
+    n = lmax + 1
+    nalm = n * (n + 1) // 2
+    nrings = 4 * nside - 1
+    npix = 12 * nside * nside
+    if form == "fast":
+        nn = ((2 * nmaps + 15) // 16) * 16
+        ws = 256 + _ngroups(lmax) * 128 * nn + 2 * 8 * nmaps * nrings * n
+        return ws + nmaps * (8 * nalm + 4 * npix)
+    return 16 * nmaps * nrings * n + nmaps * (16 * nalm + 8 * npix)
+
+
+def plan_bytes(nside: int, lmax: int, fast: bool = True) -> int:
+    """Upper bound of the device bytes of a transform plan (glg_plan_create)
+    and of its fast-form tables (built on the first fast transform): ring
+    geometry, recurrence tables, lambda_mm starts, FFT twiddles; seeds,
+    FP32 coefficients, first-l tables and the FP32 ring-FFT tables (each
+    Bluestein length M < 16 i for a ring of 4 i pixels)."""
+    n = lmax + 1
+    nalm = n * (n + 1) // 2
+    npairs = 2 * nside
+    ntw = 4 * nside * (nside + 1)
+    b = (npairs * 40 + 8 * (n + 1) + 16 * nalm + 12 * n * npairs + 84 * (nside + 1) + 8 * (nside + 2)
+         + 16 * ntw)
+    if fast:
+        tiles = (npairs + 127) // 128
+        b += (8 * npairs + 8 * ntw + 16 * (nalm + 16) + 8 * (n + 1) + 8 * _ngroups(lmax) * tiles * 128
+              + 4 * n * npairs + 4 * n * tiles)
+        b += (4 * npairs + 8 * (nside + 2) + 2 * ntw + 20 * (nside + 1) + 8 * 8 * ntw + 8 * ntw
+              + 8 * (16 * nside + 1))
+    return b
 
 
 class _Active:
@@ -102,8 +140,36 @@ class _Active:
         self.var = self.batcher.variances
         self.alm = self.batcher.alm(0, req.nshell)  # [nshell][nalm] complex64, device
         self.next_shell = 0
-        self.maps: list[torch.Tensor | None] = [None] * req.nshell
+        mdt = torch.float32 if form == "fast" else torch.float64
+        self.out = torch.empty((req.nshell, 12 * req.nside * req.nside), dtype=mdt, device=device)
         self.done_event: torch.cuda.Event | None = None
+
+
+class _Group:
+    """Launch buffers of one (nside, lmax): the plan, a stream, the transform
+    workspace and the staged alm / maps of one launch, reused by every
+    launch of the group (launches on one stream run in order)."""
+
+    def __init__(self, nside: int, lmax: int, nmaps: int, form: str, device: torch.device):
+        self.nside, self.lmax, self.nmaps, self.form = nside, lmax, nmaps, form
+        self.plan = _lib.get_plan(nside, lmax, device)
+        self.stream = torch.cuda.Stream(device)
+        n = lmax + 1
+        nalm = n * (n + 1) // 2
+        npix = 12 * nside * nside
+        cdt = torch.complex64 if form == "fast" else torch.complex128
+        self.alm = torch.empty((nmaps, nalm), dtype=cdt, device=device)
+        self.maps = torch.empty((nmaps, npix), dtype=torch.float32, device=device) if form == "fast" else None
+        self.ws = torch.empty(hp.workspace_bytes(nside, lmax, nmaps, form, device), dtype=torch.uint8,
+                              device=device)
+        self.bytes = launch_bytes(nside, lmax, nmaps, form)
+        self.plan_bytes = plan_bytes(nside, lmax, form == "fast")  # until the fast tables exist
+        self.active = 0
+        self.last_used = 0.0
+        # device-wait status of each launch, copied asynchronously (one slot
+        # per launch in flight, checked when the launch's requests retire)
+        self.status = torch.zeros(64, dtype=torch.int32, pin_memory=True)
+        self.slot = 0
 
 
 class Server:
@@ -112,6 +178,15 @@ class Server:
     ``form="fast"`` with ``batching=True`` is the serving configuration;
     ``form="plain", batching=False`` (one map per transform launch, no
     sharing across requests) is the comparison point of the FP64 form.
+
+    Device memory: the budget covers every device byte the server causes --
+    the requests' spectra, iternorm rows, alm and maps (``request_bytes``),
+    each (nside, lmax) group's launch buffers (``launch_bytes``: transform
+    workspace, staged alm and maps) and the cached plans with their fast
+    tables (``plan_bytes`` until a plan's tables exist, its measured size
+    after).  A request waits in the queue until all of that fits; idle
+    groups (no request in service) give up their buffers and plans, least
+    recently used first, when a new request needs the room.
     """
 
     def __init__(self, hbm_budget: int = 120 << 30, max_maps_per_launch: int = 40,
@@ -122,16 +197,25 @@ class Server:
         self.budget = int(hbm_budget)
         self.form = form
         self.batching = bool(batching)
-        self.max_maps = int(max_maps_per_launch) if batching else 1
-        self.used = 0
+        self.max_maps = min(int(max_maps_per_launch), hp.FAST_MAX_MAPS) if batching else 1
         self.queue: collections.deque[Request] = collections.deque()
         self.active: list[_Active] = []
         self.finished: list[Request] = []
-        self.streams: dict[tuple[int, int], torch.cuda.Stream] = {}
+        self.groups: dict[tuple[int, int], _Group] = {}
         self.lock = threading.Lock()
         self._next_id = 0
+        self._req_bytes = 0
+        self.peak_active = 0  # most requests in service at once
+
+    @property
+    def used(self) -> int:
+        """Device bytes currently accounted: requests + group buffers + plans."""
+        return self._req_bytes + sum(g.bytes + g.plan_bytes for g in self.groups.values())
 
     # ------------------------------------------------------------- intake
+
+    def _fixed_bytes(self, nside: int, lmax: int) -> int:
+        return launch_bytes(nside, lmax, self.max_maps, self.form) + plan_bytes(nside, lmax, self.form == "fast")
 
     def submit(self, req: Request) -> Request:
         with self.lock:
@@ -139,31 +223,48 @@ class Server:
             self._next_id += 1
             if req.arrival == 0.0:
                 req.arrival = time.perf_counter()
-            need = request_bytes(req.nside, req.lmax, req.nshell, self.form)
+            need = request_bytes(req.nside, req.lmax, req.nshell, self.form) + self._fixed_bytes(req.nside, req.lmax)
             if need > self.budget:
                 raise MemoryError(f"request {req.id} needs {need} bytes, over the HBM budget {self.budget}")
             self.queue.append(req)
         return req
 
+    def _evict_idle(self, need: int, keep: tuple[int, int]) -> None:
+        """Free idle groups (least recently used first) until `need` fits."""
+        idle = sorted((g.last_used, k) for k, g in self.groups.items() if g.active == 0 and k != keep)
+        for _, k in idle:
+            if self.used + need <= self.budget:
+                break
+            g = self.groups.pop(k)
+            g.stream.synchronize()  # its last launch has left the buffers
+            _lib.drop_plan(g.nside, g.lmax, self.device)
+            del g
+
     def _admit(self) -> None:
         while self.queue:
             req = self.queue[0]
+            key = (req.nside, req.lmax)
             need = request_bytes(req.nside, req.lmax, req.nshell, self.form)
+            if key not in self.groups:
+                need += self._fixed_bytes(req.nside, req.lmax)
             if self.used + need > self.budget:
-                break
+                self._evict_idle(need, key)
+                if self.used + need > self.budget:
+                    break
             self.queue.popleft()
-            self.used += need
-            req.reserved = need
+            g = self.groups.get(key)
+            if g is None:
+                g = self.groups[key] = _Group(req.nside, req.lmax, self.max_maps, self.form, self.device)
+            req.reserved = request_bytes(req.nside, req.lmax, req.nshell, self.form)
+            self._req_bytes += req.reserved
+            g.active += 1
             req.admitted = time.perf_counter()
-            stream = self._stream(req.nside, req.lmax)
-            with torch.cuda.stream(stream):
+            with torch.cuda.stream(g.stream):
                 self.active.append(_Active(req, self.device, self.form))
+            self.peak_active = max(self.peak_active, len(self.active))
 
     def _stream(self, nside: int, lmax: int) -> torch.cuda.Stream:
-        key = (nside, lmax)
-        if key not in self.streams:
-            self.streams[key] = torch.cuda.Stream(self.device)
-        return self.streams[key]
+        return self.groups[(nside, lmax)].stream
 
     # ------------------------------------------------------------ batching
 
@@ -177,22 +278,33 @@ class Server:
         launched = False
         for key, items in groups.items():
             nside, lmax = key[0], key[1]
-            stream = self._stream(nside, lmax)
+            g = self.groups[(nside, lmax)]
             for c0 in range(0, len(items), self.max_maps):
                 chunk = items[c0:c0 + self.max_maps]
-                with torch.cuda.stream(stream):
-                    alm = torch.stack([a.alm[s] for a, s in chunk])
+                cnt = len(chunk)
+                with torch.cuda.stream(g.stream):
+                    torch.stack([a.alm[s] for a, s in chunk], out=g.alm[:cnt])
                     epi = ([a.kinds[s] for a, s in chunk], [a.var[s] for a, s in chunk],
                            [a.lam[s] for a, s in chunk])
-                    maps = hp.synth(alm, nside, lmax, epilogue=epi, form=self.form)
-                for k, (a, s) in enumerate(chunk):
-                    a.maps[s] = maps[k]
+                    if self.form == "fast":
+                        st = g.status[g.slot % g.status.numel():][:1]
+                        g.slot += 1
+                        maps = hp.synth(g.alm[:cnt], nside, lmax, epilogue=epi, form="fast",
+                                        out=g.maps[:cnt], ws=g.ws, status=st)
+                    else:
+                        maps = hp.synth(g.alm[:cnt], nside, lmax, epilogue=epi, form="plain", ws=g.ws)
+                    for k, (a, s) in enumerate(chunk):
+                        a.out[s].copy_(maps[k])
+                for a, s in chunk:
                     a.next_shell = max(a.next_shell, s + 1)
+                g.last_used = time.perf_counter()
                 launched = True
+            if self.form == "fast" and g.plan_bytes and getattr(g.plan, "tuned", False):
+                g.plan_bytes = int(_lib.lib().glg_plan_device_bytes(g.plan.handle))  # measured now
             for a in {id(x[0]): x[0] for x in items}.values():
                 if a.next_shell == a.req.nshell and a.done_event is None:
                     ev = torch.cuda.Event()
-                    ev.record(stream)
+                    ev.record(g.stream)
                     a.done_event = ev
         return launched
 
@@ -200,9 +312,13 @@ class Server:
         keep = []
         for a in self.active:
             if a.done_event is not None and a.done_event.query():
-                a.req.maps = a.maps
+                g = self.groups[(a.req.nside, a.req.lmax)]
+                if self.form == "fast" and bool(torch.any(g.status != 0)):
+                    raise RuntimeError("a bounded device wait of the fast Legendre contraction timed out")
+                a.req.maps = list(a.out)
                 a.req.finished = time.perf_counter()
-                self.used -= a.req.reserved
+                self._req_bytes -= a.req.reserved
+                g.active -= 1
                 self.finished.append(a.req)
             else:
                 keep.append(a)

@@ -48,19 +48,48 @@ def test_result_alone_equals_result_in_mix(cuda_lib):
         assert len(r.maps) == r.nshell
 
 
-def test_admission_within_budget(cuda_lib):
-    from glass_gb300 import serving
+def test_admission_within_measured_budget(cuda_lib):
+    """The budget bounds the device memory the server really uses: the
+    allocator's peak over the run plus the plans' device tables."""
+    import torch
 
-    need = serving.request_bytes(64, 128, 6)
-    srv = serving.Server(hbm_budget=int(2.5 * need))  # at most two requests resident
-    reqs = [srv.submit(_request(serving, 64, 6, seed=s)) for s in range(5)]
-    peak = 0
+    from glass_gb300 import _lib, serving
+
+    nside, lmax, nshell = 64, 128, 6
+    _lib.clear_plans()
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    fixed = serving.launch_bytes(nside, lmax, 40) + serving.plan_bytes(nside, lmax)
+    need = serving.request_bytes(nside, lmax, nshell)
+    budget = fixed + int(2.5 * need)  # room for two requests at a time
+    torch.cuda.reset_peak_memory_stats()
+    base = torch.cuda.memory_allocated()
+    srv = serving.Server(hbm_budget=budget)
+    reqs = [srv.submit(_request(serving, nside, nshell, seed=s)) for s in range(5)]
     while srv.queue or srv.active:
         srv.step()
-        peak = max(peak, srv.used)
         assert srv.used <= srv.budget
+    torch.cuda.synchronize()
     assert all(r.finished is not None for r in reqs)
-    assert peak <= 2 * need
-    assert serving.request_bytes(1024, 2048, 20) > srv.budget
+    assert srv.peak_active == 2  # the budget holds two requests, never three
+    plans = sum(int(_lib.lib().glg_plan_device_bytes(g.plan.handle)) for g in srv.groups.values())
+    assert plans <= serving.plan_bytes(nside, lmax)
+    measured = torch.cuda.max_memory_allocated() - base + plans
+    assert measured <= budget, (measured, budget)
     with pytest.raises(MemoryError, match="over the HBM budget"):
         srv.submit(_request(serving, 1024, 20, seed=1))
+
+
+def test_idle_group_evicted_for_new_request(cuda_lib):
+    from glass_gb300 import serving
+
+    a = serving.launch_bytes(32, 64, 40) + serving.plan_bytes(32, 64) + serving.request_bytes(32, 64, 3)
+    b = serving.launch_bytes(64, 128, 40) + serving.plan_bytes(64, 128) + serving.request_bytes(64, 128, 3)
+    srv = serving.Server(hbm_budget=max(a, b) + min(a, b) // 2)  # never both groups at once
+    r1 = srv.submit(_request(serving, 32, 3, seed=1))
+    srv.drain()
+    assert list(srv.groups) == [(32, 64)]
+    r2 = srv.submit(_request(serving, 64, 3, seed=2))
+    srv.drain()
+    assert list(srv.groups) == [(64, 128)]
+    assert r1.finished is not None and r2.finished is not None
