@@ -83,7 +83,15 @@ struct LegTcArgs {
     float2 *F;  // [map][m][ring]
     int *err;
     unsigned long long *ucount;  // next unit to hand out (zeroed before the launch)
+    uint32_t wait_limit;         // polls of one pipeline wait before it gives up
+    int stall;                   // test hook: the B streamer issues no copies
 };
+
+// Test hook (glg_test_stall_contraction): with `stall` set, the B streamer
+// never fills its slots, so the MMA warps' waits for B run out after
+// `wait_limit` polls and the kernel takes its time-out path.
+uint32_t g_test_wait_limit = 0;
+int g_test_stall = 0;
 
 __device__ __forceinline__ uint32_t tf32_rna(float x) {
     // round the magnitude to 10 fraction bits, ties away from zero (the
@@ -194,7 +202,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
         atomicExch(a.err, GLG_ERR_TIMEOUT);
     };
     auto wait = [&](uint64_t *bar, uint32_t parity) -> bool {
-        for (uint32_t i = 0; i < WAIT_LIMIT; ++i) {
+        for (uint32_t i = 0; i < a.wait_limit; ++i) {
             if (mbar_try_wait(bar, parity)) return true;
             if (*abort_flag) return false;
         }
@@ -459,6 +467,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
                     const uint32_t bsl = cc % NBC, use = cc / NBC;
                     if (use > 0 && !wait(&S.bempty[bsl], (use - 1) & 1u)) { ok = false; break; }
                     const int ng = G - g0 < CH ? G - g0 : CH;
+                    if (a.stall) continue;  // test hook: the slot is never filled
                     mbar_arrive_expect_tx(&S.full_b[bsl], ng * BBYTES);
                     bulk_g2s(S.bs[bsl].b, a.bpack + (size_t)(gb + g0) * BBYTES, ng * BBYTES, &S.full_b[bsl]);
                     last_use[bsl] = use;
@@ -619,6 +628,8 @@ int launch_tc(const glg_plan *P, const float2 *alm, int nmaps, float *bpack, flo
     a.err = err;
     // one zeroed counter per launch of a call (the status block is cleared once per call)
     a.ucount = reinterpret_cast<unsigned long long *>(reinterpret_cast<char *>(err) + 64) + run.slot;
+    a.wait_limit = g_test_wait_limit ? g_test_wait_limit : WAIT_LIMIT;
+    a.stall = g_test_stall;
     // more than half of the SM's shared memory: one CTA per SM, so no two
     // CTAs contend for the 512 tensor-memory columns
     size_t smem = sizeof(Smem<N>) + 128;
@@ -635,6 +646,12 @@ int launch_tc(const glg_plan *P, const float2 *alm, int nmaps, float *bpack, flo
 }
 
 }  // namespace
+
+extern "C" int glg_test_stall_contraction(int on, unsigned int wait_limit) {
+    g_test_stall = on ? 1 : 0;
+    g_test_wait_limit = on ? (wait_limit ? wait_limit : 1u) : 0u;
+    return GLG_OK;
+}
 
 size_t glg_leg_tc_pack_bytes(const glg_plan *P, int nmaps) {
     const int N = ((2 * nmaps + 15) / 16) * 16;

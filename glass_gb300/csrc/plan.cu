@@ -5,6 +5,8 @@
 // reference reaches through healpy/healpix (glass/healpix.py:38-78,
 // :293-310).
 #include <cuda_runtime.h>
+
+#include <atomic>
 #include <math.h>
 
 #include <algorithm>
@@ -191,8 +193,23 @@ static void factor_ring(int n, int *radix, int *nst) {
     *nst = k;
 }
 
+// Failure injection for tests: the n-th plan allocation from now (1 = the
+// next) reports cudaErrorMemoryAllocation without calling cudaMalloc.
+static std::atomic<int> g_fail_alloc{0};
+
+extern "C" int glg_test_fail_plan_alloc(int nth) {
+    GLG_REQUIRE(nth >= 0, "glg_test_fail_plan_alloc: negative count");
+    g_fail_alloc.store(nth);
+    return GLG_OK;
+}
+
 template <typename T>
 static int dalloc(glg_plan *P, T **ptr, size_t count) {
+    const int f = g_fail_alloc.load();
+    if (f > 0 && g_fail_alloc.fetch_sub(1) == 1) {
+        *ptr = nullptr;
+        return glg_cuda_status(cudaErrorMemoryAllocation, "glg_plan_create: cudaMalloc (injected failure)");
+    }
     cudaError_t e = cudaMalloc((void **)ptr, sizeof(T) * (count ? count : 1));
     if (e != cudaSuccess) return glg_cuda_status(e, "glg_plan_create: cudaMalloc");
     P->bytes += sizeof(T) * count;
