@@ -48,6 +48,7 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "shell-maps/sec and pixels/sec at nside 2048 vs plain FP64 GPU @1e-6; p50/p99 latency"
 UNIT = "shell-maps/s"
+PASSES = 4  # tensor-core products per Legendre term (A_lo B_lo, A_hi B_lo, A_lo B_hi, A_hi B_hi)
 WORKLOAD = dict(workload="40-shell lognormal field generation, nside 2048, lmax 4096", nshell=40, nside=2048,
                 lmax=4096)
 
@@ -150,6 +151,52 @@ def run_serving(args) -> dict:
         res = _serve(_serving_requests(n, seed=3), 0.7 * cap, form, batching)
         res["capacity_req_per_s"] = cap
         out[f"{form}{'_batched' if batching else '_unbatched'}"] = res
+    return out
+
+
+def run_cfg2(steps: int = 3) -> dict:
+    """Config 2: 10 correlated lognormal shells at nside 512 / lmax 1024
+    (spectra A_i (l+1)^-1.2 e^{-(l/800)^2}, correlation e^{-|i-j|/1.5},
+    shifts in [0.5, 2], from seed 0), device-resident.  Plain FP64 and fast
+    forms timed with CUDA events (best of `steps`), the fast form's error per
+    shell against the FP64 form (accuracy_report), and the spin-2 shear of
+    the summed convergence (from_convergence, discretized, FP64 form)."""
+    import torch
+
+    import glass_gb300 as g
+
+    nshell, nside, lmax = 10, 512, 1024
+    gls_np, lam = spectra_cfg2(nshell, lmax, seed=0)
+    gls = [torch.as_tensor(c, device="cuda") for c in gls_np]
+    fields = [g.grf.Lognormal(float(x)) for x in lam]
+    out = {"workload": "10-shell lognormal field generation, nside 512, lmax 1024", "nshell": nshell,
+           "nside": nside, "lmax": lmax}
+    stream = torch.cuda.current_stream()
+    for form in ("plain", "fast"):
+        maps = list(g.generate(fields, gls, nside, rng=g.rng.Generator(42), form=form))  # warm-up
+        best = None
+        for _ in range(steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            maps = list(g.generate(fields, gls, nside, rng=g.rng.Generator(42), form=form))
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+            best = ms if best is None else min(best, ms)
+        out[form] = {"ms_per_step": best, "shell_maps_per_s": nshell / (best / 1e3)}
+    out["fast_speedup"] = out["plain"]["ms_per_step"] / out["fast"]["ms_per_step"]
+    rep = g.accuracy_report(fields, gls_np, nside, seed=42)
+    out["fast_error_per_shell"] = rep
+    out["fast_rel_rms_max"] = max(r["rms_rel"] for r in rep)
+    kappa = torch.stack(maps).double().mean(dim=0)  # summed convergence (mean of the shells)
+    g.from_convergence(kappa, shear=True)  # warm-up (plans, pixel windows)
+    torch.cuda.synchronize()
+    a = time.perf_counter()
+    (gamma,) = g.from_convergence(kappa, shear=True)
+    torch.cuda.synchronize()
+    out["shear"] = {"ms": (time.perf_counter() - a) * 1e3, "form": "plain FP64 (map2alm iter 3 + spin-2 synthesis)",
+                    "discretized": True, "lmax": 3 * nside - 1, "finite": bool(torch.isfinite(gamma).all())}
     return out
 
 
@@ -301,6 +348,8 @@ def run_ours(args, rank: int, world: int) -> dict | None:
     nshell, nside, lmax = args.nshell, args.nside, args.lmax
     gls_np, lam = spectra_cfg3(nshell, lmax)
     gls_dev = [torch.as_tensor(c, device=dev) for c in gls_np]
+    ell = np.arange(lmax + 1)
+    shell_variances = [np.sum((2 * ell + 1) * gls_np[k * (k + 1) // 2]) / (4 * np.pi) for k in range(nshell)]
     fields = [g.grf.Lognormal(float(x)) for x in lam]
     npix = 12 * nside * nside
 
@@ -355,14 +404,14 @@ def run_ours(args, rank: int, world: int) -> dict | None:
     traffic = 17.684237568e9 + 10.706691328e9 if (nshell, nside, lmax) == (40, 2048, 4096) else None
     roofline = {"bound": "tensor", "kernel": "k_leg_tc", "achieved": achieved, "peak": peak_tf,
                 "unit": "TFLOP/s", "frac": (achieved / peak_tf) if achieved else None,
-                "traffic": traffic, "traffic_unit": "bytes per launch", "peak_note": peak_note, "passes": 3,
-                "issued_frac": (3 * achieved / peak_tf) if achieved else None,
+                "traffic": traffic, "traffic_unit": "bytes per launch", "peak_note": peak_note, "passes": PASSES,
+                "issued_frac": (PASSES * achieved / peak_tf) if achieved else None,
                 "algorithmic_flops_per_launch": flops}
     # the same figure against the measured bf16 GEMM rate halved (the
     # tensor pipe's tf32 rate is half its bf16 rate)
     bf_half = peaks.get("bf16_tflops", 1900.0) / 2.0
     roofline["vs_bf16_half"] = {"peak": bf_half, "frac": (achieved / bf_half) if achieved else None,
-                                "issued_frac": (3 * achieved / bf_half) if achieved else None,
+                                "issued_frac": (PASSES * achieved / bf_half) if achieved else None,
                                 "note": "of measured" if "fallback" not in peaks else "of fallback"}
     if rank != 0:
         return None
@@ -376,12 +425,15 @@ def run_ours(args, rank: int, world: int) -> dict | None:
         torch.cuda.synchronize()
         plain_s = time.perf_counter() - a
         fm = step_device("fast")
-        errs = []
+        errs, maxs = [], []
         for x, y in zip(fm, pm):
             d = x.double() - y
             errs.append(float(torch.sqrt(torch.mean(d * d)) / torch.sqrt(torch.mean(y * y))))
+            maxs.append(float(d.abs().max() / y.abs().max()))
         plain = {"value": nshell / plain_s, "unit": UNIT, "ms_per_step": plain_s * 1e3,
                  "fast_vs_plain_rel_rms_max": max(errs), "fast_vs_plain_rel_rms_median": float(np.median(errs)),
+                 "fast_vs_plain_rel_rms_per_shell": errs, "fast_vs_plain_rel_max_per_shell": maxs,
+                 "shell_variances": [float(v) for v in shell_variances],
                  "speedup": (nshell / plain_s) and value / (nshell / plain_s)}
         del pm, fm
 
@@ -433,6 +485,7 @@ def run_ours(args, rank: int, world: int) -> dict | None:
                "d2h_bytes_per_step": d2h}
 
     serving = run_serving(args) if (args.serving > 0 or args.serving_plain > 0) else None
+    cfg2 = run_cfg2() if args.cfg2 else None
     cpu = cpu_baseline(args) if args.cpu_baseline else None
     res = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -444,7 +497,7 @@ def run_ours(args, rank: int, world: int) -> dict | None:
         "pixels_per_sec": value * npix, "e2e": e2e, "plain_fp64": plain, "roofline": roofline, "points": points,
         "kernel_ms_per_step": {k: v[0] for k, v in kt.items()},
         "kernel_launches_per_step": {k: v[1] for k, v in kt.items()}, "gpu_launches": launches,
-        "clocks": clk.summary(), "cpu_baseline": cpu, "serving": serving,
+        "clocks": clk.summary(), "cpu_baseline": cpu, "serving": serving, "cfg2": cfg2,
     }
     return res
 
@@ -537,6 +590,8 @@ def main() -> None:
     ap.add_argument("--serving-plain", type=int, default=60,
                     help="requests of the FP64 unbatched serving comparison (0: off)")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--no-cfg2", dest="cfg2", action="store_false",
+                    help="skip the config-2 record (10 shells, nside 512)")
     ap.add_argument("--no-points", dest="points", action="store_false",
                     help="skip the galaxy counts / positions aside")
     ap.add_argument("--ncu-case", nargs="?", const="sht", choices=["sht", "alm"],

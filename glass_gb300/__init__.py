@@ -13,6 +13,7 @@ from __future__ import annotations
 
 from . import galaxies, grf, harmonics, healpix, points, rng, user
 from .fields import (
+    accuracy_report,
     cls2cov,
     enumerate_spectra,
     generate,
@@ -30,6 +31,7 @@ from .lensing import MultiPlaneConvergence, from_convergence, shear_from_converg
 
 __all__ = [
     "MultiPlaneConvergence",
+    "accuracy_report",
     "cls2cov",
     "enumerate_spectra",
     "from_convergence",

@@ -53,6 +53,8 @@ _SIGNATURES = {
     "glg_plan_create": ([c_i, c_i, c_p, ctypes.POINTER(c_p)], c_i),
     "glg_plan_destroy": ([c_p], None),
     "glg_plan_device_bytes": ([c_p], c_sz),
+    "glg_set_plm_table_budget": ([c_sz], c_i),
+    "glg_plan_has_plm_table": ([c_p], c_i),
     "glg_plan_info": ([c_p, ctypes.POINTER(c_i), ctypes.POINTER(c_i), ctypes.POINTER(c_i),
                        ctypes.POINTER(c_i64), ctypes.POINTER(c_i64)], c_i),
     "glg_iternorm": ([c_p, c_i64, c_i64, c_i, c_p, c_p, c_p], c_i),
@@ -117,6 +119,8 @@ def load_library(require_gpu: bool = True) -> ctypes.CDLL:
                 fn = getattr(L, name)
                 fn.argtypes = args
                 fn.restype = res
+            if "GLASS_GB300_PLM_TABLE_BYTES" in os.environ:  # P_lm table budget of the fast form
+                L.glg_set_plm_table_budget(int(os.environ["GLASS_GB300_PLM_TABLE_BYTES"]))
             _LIB = L
     if require_gpu and not torch.cuda.is_available():
         raise RuntimeError("glass_gb300 needs a CUDA device; none is available (no CPU fallback)")
@@ -201,7 +205,15 @@ class Plan:
         self.nrings = 4 * nside - 1
         self.npix = 12 * nside * nside
         self.nalm = (lmax + 1) * (lmax + 2) // 2
-        self.bytes = int(lib().glg_plan_device_bytes(h))
+
+    @property
+    def bytes(self) -> int:
+        """Device bytes of the plan's tables (grows when the fast tables are built)."""
+        return int(lib().glg_plan_device_bytes(self.handle))
+
+    @property
+    def has_plm_table(self) -> bool:
+        return bool(lib().glg_plan_has_plm_table(self.handle))
 
     def __del__(self):
         h = getattr(self, "handle", None)
@@ -216,7 +228,7 @@ class Plan:
 
 _PLANS: dict[tuple[int, int, int], Plan] = {}
 _PLAN_LOCK = threading.Lock()
-_PLAN_BUDGET = int(os.environ.get("GLASS_GB300_PLAN_BYTES", str(64 << 30)))
+_PLAN_BUDGET = int(os.environ.get("GLASS_GB300_PLAN_BYTES", str(200 << 30)))
 
 
 def get_plan(nside: int, lmax: int, device: torch.device | None = None) -> Plan:

@@ -95,6 +95,12 @@ struct glg_plan {
     int64_t seed_stride;     // npairs rounded up to whole 128-pair tiles
     int *lstart;             // [mmax+1][npairs] first l with |lambda| >= 2^-40
     int *tfirst;             // [mmax+1][ntiles] first group with a lambda >= 2^-40 in the tile
+    // P_lm table (built instead of the seeds when it fits the table budget):
+    // per (group, ring tile) one 8 KB tile [l quad][128 ring pairs][4] of
+    // mu_l = lambda_l / d_l as FP32 (the FP64 recurrence rounded once), zero
+    // beyond lmax and beyond the last ring pair.  nullptr: recurrence path.
+    float4 *plm;
+    size_t plm_bytes;
 
     // FP32 ring FFTs of the fast form.  Class 0: ring lengths whose prime
     // factors are all <= 13 (mixed-radix DIF, output order from pos16).
@@ -151,6 +157,9 @@ size_t glg_ring32_smem(int kind, int n_or_M, int threads, bool fold);
 
 int glg_plan_prepare_fast(glg_plan *P, cudaStream_t st);
 
+// Bytes of one group's P_lm tile (128 ring pairs x 16 l, FP32).
+#define GLG_PLM_TILE_BYTES (128 * GLG_GROUP * 4)
+
 // ---------------------------------------------------------- device helpers
 
 __host__ __device__ inline int64_t glg_nalm(int lmax) {
@@ -174,8 +183,21 @@ int glg_launch_ring_ana(const glg_plan *P, const double *maps, int nmaps, double
                         cudaStream_t st);
 int glg_launch_leg_ana(const glg_plan *P, const double2 *G, int nmaps, double2 *alm, int accumulate,
                        cudaStream_t st);
+// Tail refinement list of the fast form (in the fast workspace): hdr[0]
+// entries appended by the ring FFTs, hdr[1] entries already refined; items
+// (map, ring, pixel within the ring).
+struct glg_refine_list {
+    int *hdr;
+    int cap;
+    int4 *items;
+};
 int glg_launch_ring_syn_f32(const glg_plan *P, const float2 *F, float2 *Ft, int nmaps, float *maps,
-                            const glg_epilogue *epi, cudaStream_t st);
+                            const glg_epilogue *epi, const glg_refine_list *rl, cudaStream_t st);
+// FP64 recomputation of the listed pixels (no launch when no map of the call
+// qualifies); returns GLG_OK.
+bool glg_refine_wanted(const glg_epilogue *epi, int nmaps);
+int glg_launch_refine(const glg_plan *P, const float2 *Ft, int nmaps, float *maps, const glg_epilogue *epi,
+                      const glg_refine_list &rl, cudaStream_t st);
 // One size bucket of the FP32 ring FFTs from transposed sums Ft, with
 // `threads` per block (0: the bucket's own), no epilogue (autotuning).
 int glg_launch_ring_bucket_f32(const glg_plan *P, int bucket, int threads, const float2 *Ft, int nmaps,
@@ -192,7 +214,8 @@ int glg_launch_leg_tc(const glg_plan *P, const float2 *alm, int nmaps, float *bp
                       int *err, const glg_tile_run &run, cudaStream_t st);
 // Ring FFTs of the ring pairs [p0, p1) only (transpose included).
 int glg_launch_ring_syn_f32_range(const glg_plan *P, const float2 *F, float2 *Ft, int nmaps, float *maps,
-                                  const glg_epilogue *epi, int p0, int p1, cudaStream_t st);
+                                  const glg_epilogue *epi, int p0, int p1, const glg_refine_list *rl,
+                                  cudaStream_t st);
 
 // Fast-form workspace: [status ints | B pack | F (float2 [map][m][ring])]
 // The status block holds the error word and, from byte 64, the unit

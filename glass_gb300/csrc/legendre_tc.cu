@@ -1,5 +1,5 @@
 // Fast form of the Legendre sums: a shells-batched contraction on the
-// sm_103a tensor cores (tcgen05, split-precision 3xTF32).
+// sm_103a tensor cores (tcgen05, split-precision TF32: 3xTF32 plus the lo x lo term).
 //
 // For one ring tile (128 ring pairs, one per TMEM lane) and one m:
 //   D_E[p][n] = sum_{l-m even} lambda_lm(x_p) B[l][n],
@@ -11,23 +11,24 @@
 // lambda is generated on the fly in FP32 by producer warps, restarting every
 // 16 l (one "group") from seeds computed once per plan by an FP64
 // recurrence, split into TF32 hi + lo parts and written straight into tensor
-// memory as the MMA's A operand (hi rounded to nearest; lo = v - hi, which
-// the tensor core truncates to TF32: |lo| <= half a TF32 ulp of v with
-// either sign, so the truncation is unbiased and below 2^-21 |v|).  Within a group the producers carry the
+// memory as the MMA's A operand (hi and lo = v - hi both rounded to nearest
+// TF32).  Within a group the producers carry the
 // scaled mu_l = lambda_l / d_l, d = 1 at the group's first two l and
 // d_l = B_l d_{l-2} after, whose recurrence mu_l = alpha_l x mu_{l-1} -
 // mu_{l-2} (alpha_l = A_l d_{l-1} / d_l) has no second product; the alm
 // carry d_l instead (B[l][n] = a_lm d_l), so the sums are unchanged.  B (the alm, split the same way), the
 // group's seeds and its recurrence coefficients are streamed into shared
 // memory with 1-D bulk copies.  Each group issues, per parity,
-//   D += A_hi B_lo + A_lo B_hi + A_hi B_hi     (M = 128, N = 2 * maps, K = 8).
+//   D += A_lo B_lo + A_hi B_lo + A_lo B_hi + A_hi B_hi   (M = 128, N = 2 * maps, K = 8),
+// with both lo parts rounded to nearest TF32 (4 passes).
 //
 // Groups before the first one where some ring of the tile has |lambda| >=
 // 2^-40 are zero on the whole tile and are skipped (the dense algorithmic
 // count is still the one reported).
 //
 // Pipeline.  The groups of a (tile, m) unit are processed in chunks of
-// CH = 3 groups, one per producer warp set; a chunk is the unit of every
+// CH = 3 groups, one per producer warp set, from the unit's highest l down
+// (smallest terms first into the running sums); a chunk is the unit of every
 // hand-off: its lambda goes to one of two TMEM chunk slots, its B tiles come
 // in one bulk copy into one of NBC shared-memory chunk slots, its MMAs
 // accumulate into one of two TMEM accumulator sets, and one commit per chunk
@@ -48,6 +49,8 @@
 // returns.
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "glg_internal.cuh"
 #include "tc_ptx.cuh"
 
@@ -57,11 +60,24 @@ namespace {
 
 constexpr int CH = 3;             // groups per chunk = producer warp sets
 constexpr int NSEED = 16;         // slots of the seed / coefficient ring (groups)
+constexpr int NPLM = 6;           // slots of the P_lm tile ring (groups), table path
 constexpr int NU = 8;             // slots of the unit ring
 constexpr int NCONSUMERS = 19;    // warps that read the unit ring (all but the seed streamer)
 constexpr int TMEM_COLS = 512;
 constexpr int THREADS = 20 * 32;
 constexpr uint32_t WAIT_LIMIT = 1u << 22;
+// The tensor core's FP32 accumulation rounds toward zero, so every chunk sum
+// comes out smaller in magnitude than the exact one, on average by the same
+// fraction: measured on GB300 as a regression slope of -7.0e-8 (+-0.2e-8)
+// of these sums against FP64 ones, the same at nside 512 and 2048, for every
+// map, with the recurrence or the P_lm table.  The packed alm are scaled up by
+// that fraction (k_pack_b adds it to the lo part, whose TF32 precision is
+// 2^-22 of the value: a scaling of 7e-8 is carried to ~3%), which removes the
+// systematic part -- a bias that the lognormal transform amplifies at its
+// largest pixels -- and leaves the random part of the rounding.  (Scaling the
+// FP32 sums themselves cannot do it: 7e-8 is below one FP32 ulp, so
+// v + 7e-8 v rounds to v plus one whole ulp.)
+constexpr float ACC_BIAS = 7.0e-8f;
 constexpr int W_DRAIN = 12, W_MMA = 16, W_LOAD = 17, W_SEED = 18, W_MMA2 = 19;
 static_assert(W_DRAIN == 4 * CH, "one producer warp set per group of a chunk");
 static_assert((W_MMA2 + 1) * 32 == THREADS, "one warp per role after the producers and drains");
@@ -79,6 +95,7 @@ struct LegTcArgs {
     int64_t seed_stride;
     const int *lstart;
     const int *tfirst;  // [m][tile] first group holding a lambda >= 2^-40
+    const float4 *plm;  // P_lm tiles (table path)
     const unsigned char *bpack;
     float2 *F;  // [map][m][ring]
     int *err;
@@ -115,6 +132,16 @@ __device__ __forceinline__ float rec_step(const float4 c, const float2 x, float 
     return __fadd_rn(__fsub_rn(ph, lm2), pe);
 }
 
+// Chunk k of a (tile, m) unit, groups [c0, c1): chunks are taken from the
+// top of the unit down (k = 0 ends at the unit's last group), so the running
+// sums receive the small high-l terms first and the large ones last -- the
+// rounding of each drained addition is relative to a running sum that is
+// still small for most of the unit.  The partial chunk, if any, is the last.
+__device__ __forceinline__ void chunk_range(int k, int gf, int G, int &c0, int &c1) {
+    c1 = G - CH * k;
+    c0 = c1 - CH > gf ? c1 - CH : gf;
+}
+
 __device__ __forceinline__ int unit_m(int64_t mi, int lmax) {
     return (mi & 1) ? lmax - (int)(mi >> 1) : (int)(mi >> 1);
 }
@@ -122,29 +149,38 @@ __device__ __forceinline__ int unit_m(int64_t mi, int lmax) {
 // B chunk slots in shared memory: as many as fit beside the accumulators and
 // the seed ring (up to 6), so the alm of a chunk are requested several chunks
 // before the MMAs that read them.
-template <int N>
+template <int N, bool T>
 constexpr int nbc_slots() {
-    constexpr int room = (226 * 1024 - 512 * (2 * N + 4) - NSEED * 1280 - 1024) / (CH * 128 * N);
+    constexpr int ring = T ? NPLM * GLG_PLM_TILE_BYTES : NSEED * 1280;
+    constexpr int room = (226 * 1024 - 512 * (2 * N + 4) - ring - 1024) / (CH * 128 * N);
     return room > 6 ? 6 : room;
 }
 
-template <int N>
+struct SeedSlot {
+    float2 seed[128];        // seeds of the group's 128 ring pairs
+    float4 coef[GLG_GROUP];  // (alpha_hi, alpha_lo, d, 0) of l = l0 .. l0+15
+};
+struct PlmSlot {
+    float4 v[4][128];  // P_lm tile: [l quad][ring pair], 4 l per float4
+};
+
+// T: lambda from the plan's P_lm table (tiles streamed into a ring of
+// shared-memory slots), else from the FP32 recurrence and its seeds.
+template <int N, bool T>
 struct Smem {
     static constexpr uint32_t BBYTES = 128 * N;  // one group: 4 tiles of N x 8 tf32
-    static constexpr int NBC = nbc_slots<N>();
+    static constexpr int NBC = nbc_slots<N, T>();
+    static constexpr int NS = T ? NPLM : NSEED;  // group slots of the lambda source
     static_assert(NBC >= 2, "at least two B chunk slots");
     struct BSlot {
         unsigned char b[CH * BBYTES];
     } bs[NBC];
-    struct SeedSlot {
-        float2 seed[128];        // seeds of the group's 128 ring pairs
-        float4 coef[GLG_GROUP];  // (alpha_hi, alpha_lo, d, 0) of l = l0 .. l0+15
-    } sd[NSEED];
+    std::conditional_t<T, PlmSlot, SeedSlot> sd[NS];
     static constexpr int ACC_LD = 2 * N + 4;  // floats per lane row (odd count of float4)
     float acc[128][ACC_LD];    // FP32 sums of drained chunks, [lane][column]
     uint64_t full_a[2], cdone[2], empty_d[2];
     uint64_t full_b[NBC], bempty[NBC];
-    uint64_t sfull[NSEED], sempty[NSEED];
+    uint64_t sfull[NS], sempty[NS];
     uint64_t ufull[NU], uempty[NU];
     int64_t unit[NU];  // units handed out to this CTA, in order
     uint64_t drain;
@@ -152,12 +188,14 @@ struct Smem {
     int abort;
 };
 
-template <int N>
+template <int N, bool T>
 __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    Smem<N> &S = *reinterpret_cast<Smem<N> *>(smem_raw);
-    constexpr int NBC = Smem<N>::NBC;
-    constexpr uint32_t BBYTES = Smem<N>::BBYTES;
+    using SM = Smem<N, T>;
+    SM &S = *reinterpret_cast<SM *>(smem_raw);
+    constexpr int NBC = SM::NBC;
+    constexpr int NS = SM::NS;
+    constexpr uint32_t BBYTES = SM::BBYTES;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     constexpr uint32_t IDESC = idesc_tf32(128, N);
     constexpr uint32_t SEED_TX = 128 * 8 + GLG_GROUP * 16;
@@ -175,7 +213,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
             mbar_init(&S.full_b[k], 1);
             mbar_init(&S.bempty[k], 2);
         }
-        for (int q = 0; q < NSEED; ++q) {
+        for (int q = 0; q < NS; ++q) {
             mbar_init(&S.sfull[q], 1);
             mbar_init(&S.sempty[q], 4);
         }
@@ -187,7 +225,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
         S.abort = 0;
         fence_barrier_init();
     }
-    for (int i = threadIdx.x; i < 128 * Smem<N>::ACC_LD; i += THREADS) (&S.acc[0][0])[i] = 0.f;
+    for (int i = threadIdx.x; i < 128 * SM::ACC_LD; i += THREADS) (&S.acc[0][0])[i] = 0.f;
     if (warp == 0) {
         tmem_alloc(&S.tmem_base, TMEM_COLS);
         tmem_relinquish();
@@ -249,22 +287,45 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
             const float2 x = a.cth32[pp];
             const int ls = live ? a.lstart[(int64_t)m * a.npairs + pp] : lmax + 1;
             const int gf = a.tfirst[(int64_t)m * a.ntiles + tile];
-            for (int g0 = gf; g0 < G; g0 += CH, ++cc) {
+            for (int kc = 0, nch = (G - gf + CH - 1) / CH; kc < nch; ++kc, ++cc) {
+                int g0, g1;
+                chunk_range(kc, gf, G, g0, g1);
                 const uint32_t slot = cc & 1u;
                 // lambda slot free: chunk cc - 2 has retired
                 if (cc >= 2 && !wait(&S.cdone[slot], ((cc >> 1) - 1) & 1u)) { ok = false; break; }
                 const int g = g0 + set;
-                if (g < G) {
-                    const uint32_t gg = gc + (uint32_t)(g - gf);
-                    const int q = (int)(gg % NSEED);
-                    if (!wait(&S.sfull[q], (gg / NSEED) & 1u)) { ok = false; break; }
+                if (g < g1) {
+                    const uint32_t gg = gc + (uint32_t)(CH * kc + set);  // groups in hand-out order
+                    const int q = (int)(gg % NS);
+                    if (!wait(&S.sfull[q], (gg / NS) & 1u)) { ok = false; break; }
                     fence_after_sync();
-                    const typename Smem<N>::SeedSlot &sd = S.sd[q];
+                    uint32_t ehi[8], elo[8], ohi[8], olo[8];
+                    if constexpr (T) {
+                        // the lane's 16 lambda of the group from the staged P_lm tile
+#pragma unroll
+                        for (int qq = 0; qq < 4; ++qq) {
+                            const float4 t4 = S.sd[q].v[qq][r];
+                            const float vv[4] = {t4.x, t4.y, t4.z, t4.w};
+#pragma unroll
+                            for (int i = 0; i < 4; ++i) {
+                                const int j = 4 * qq + i;
+                                const uint32_t hi = tf32_rna(vv[i]);
+                                const uint32_t lo = tf32_rna(vv[i] - __uint_as_float(hi));
+                                if (j & 1) {
+                                    ohi[j >> 1] = hi;
+                                    olo[j >> 1] = lo;
+                                } else {
+                                    ehi[j >> 1] = hi;
+                                    elo[j >> 1] = lo;
+                                }
+                            }
+                        }
+                    } else {
+                    const SeedSlot &sd = S.sd[q];
                     const int l0 = m + g * GLG_GROUP;
                     const int s0 = l0 > ls ? l0 : ls;
                     const float2 seed = sd.seed[r];
                     float lm2 = 0.f, lm1 = 0.f;
-                    uint32_t ehi[8], elo[8], ohi[8], olo[8];
                     // every lane starts at l0 and the group ends inside lmax: no per-step tests
                     const bool regular = __all_sync(0xffffffffu, s0 == l0) && l0 + GLG_GROUP - 1 <= lmax;
                     if (regular) {
@@ -274,7 +335,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
                             lm2 = lm1;
                             lm1 = v;
                             const uint32_t hi = tf32_rna(v);
-                            const uint32_t lo = __float_as_uint(v - __uint_as_float(hi));
+                            const uint32_t lo = tf32_rna(v - __uint_as_float(hi));
                             if (j & 1) {
                                 ohi[j >> 1] = hi;
                                 olo[j >> 1] = lo;
@@ -297,7 +358,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
                             lm2 = lm1;
                             lm1 = v;
                             const uint32_t hi = tf32_rna(v);
-                            const uint32_t lo = __float_as_uint(v - __uint_as_float(hi));
+                            const uint32_t lo = tf32_rna(v - __uint_as_float(hi));
                             if (j & 1) {
                                 ohi[j >> 1] = hi;
                                 olo[j >> 1] = lo;
@@ -306,6 +367,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
                                 elo[j >> 1] = lo;
                             }
                         }
+                    }
                     }
                     __syncwarp();
                     if (lane == 0) mbar_arrive(&S.sempty[q]);  // seed slot read
@@ -335,7 +397,9 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
             const int m = unit_m(u / a.nrun, lmax);
             const int G = (lmax - m + GLG_GROUP) / GLG_GROUP;
             const int gf = a.tfirst[(int64_t)m * a.ntiles + tile];
-            for (int g0 = gf; g0 < G; g0 += CH, ++cc) {
+            for (int kc = 0, nch = (G - gf + CH - 1) / CH; kc < nch; ++kc, ++cc) {
+                int g0, g1;
+                chunk_range(kc, gf, G, g0, g1);
                 const uint32_t d = cc & 1u;
                 if (!wait(&S.cdone[d], (cc >> 1) & 1u)) { ok = false; break; }
                 fence_after_sync();
@@ -402,7 +466,9 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
                 const int m = unit_m(u / a.nrun, lmax);
                 const int G = (lmax - m + GLG_GROUP) / GLG_GROUP;
                 const int gf = a.tfirst[(int64_t)m * a.ntiles + tile];
-                for (int g0 = gf; g0 < G; g0 += CH, ++cc) {
+                for (int kc = 0, nch = (G - gf + CH - 1) / CH; kc < nch; ++kc, ++cc) {
+                int g0, g1;
+                chunk_range(kc, gf, G, g0, g1);
                     const uint32_t k = cc & 1u, bsl = cc % NBC;
                     if (cc >= 2 && !wait(&S.empty_d[k], ((cc >> 1) - 1) & 1u)) { ok = false; break; }
                     if (!wait(&S.full_b[bsl], (cc / NBC) & 1u) || !wait(&S.full_a[k], (cc >> 1) & 1u)) {
@@ -410,7 +476,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
                         break;
                     }
                     fence_after_sync();
-                    const int ng = G - g0 < CH ? G - g0 : CH;
+                    const int ng = g1 - g0;
                     const uint32_t dD = tb + 2 * N * k + N * par;              // this parity's accumulator
                     const uint32_t a0 = tb + A_COL0 + k * A_SLOT + 16 * par;   // its (A_hi, A_lo) columns
                     // descriptor of the slot's first tile; the 14-bit start
@@ -424,7 +490,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
 #pragma unroll
                     for (int q = 0; q < CH; ++q) {
                         if (q < ng) {
-                            mma_tf32_ts(dD, a0 + 32 * q + 0, d0 + q * GT + TT, IDESC, q > 0 ? 1u : 0u);
+                            mma_tf32_ts(dD, a0 + 32 * q + 8, d0 + q * GT + TT, IDESC, q > 0 ? 1u : 0u);
+                            mma_tf32_ts(dD, a0 + 32 * q + 0, d0 + q * GT + TT, IDESC, 1u);
                             mma_tf32_ts(dD, a0 + 32 * q + 8, d0 + q * GT, IDESC, 1u);
                         }
                     }
@@ -463,10 +530,12 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
                 const int G = (lmax - m + GLG_GROUP) / GLG_GROUP;
                 const int gf = a.tfirst[(int64_t)m * a.ntiles + tile];
                 const int64_t gb = a.goff[m];
-                for (int g0 = gf; g0 < G; g0 += CH, ++cc) {
+                for (int kc = 0, nch = (G - gf + CH - 1) / CH; kc < nch; ++kc, ++cc) {
+                int g0, g1;
+                chunk_range(kc, gf, G, g0, g1);
                     const uint32_t bsl = cc % NBC, use = cc / NBC;
                     if (use > 0 && !wait(&S.bempty[bsl], (use - 1) & 1u)) { ok = false; break; }
-                    const int ng = G - g0 < CH ? G - g0 : CH;
+                    const int ng = g1 - g0;
                     if (a.stall) continue;  // test hook: the slot is never filled
                     mbar_arrive_expect_tx(&S.full_b[bsl], ng * BBYTES);
                     bulk_g2s(S.bs[bsl].b, a.bpack + (size_t)(gb + g0) * BBYTES, ng * BBYTES, &S.full_b[bsl]);
@@ -488,8 +557,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
         if (lane == 0) {
             uint32_t gc = 0;
             bool ok = true;
-            int64_t last_use[NSEED];
-            for (int q = 0; q < NSEED; ++q) last_use[q] = -1;
+            int64_t last_use[NS];
+            for (int q = 0; q < NS; ++q) last_use[q] = -1;
             for (uint32_t ui = 0; ok; ++ui) {
                 const uint32_t uq = ui % NU;
                 if (ui >= NU && !wait(&S.uempty[uq], ((ui / NU) - 1) & 1u)) { ok = false; break; }
@@ -503,21 +572,31 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
                 const int64_t gb = a.goff[m];
                 const int64_t cb = a.mofs[m];
                 const int gf = a.tfirst[(int64_t)m * a.ntiles + tile];
-                for (int g = gf; g < G; ++g) {
-                    const uint32_t gg = gc + (uint32_t)(g - gf);
-                    const int q = (int)(gg % NSEED);
-                    const uint32_t use = gg / NSEED;
+                for (int gi = 0; gi < G - gf; ++gi) {  // groups in the order the producers take them
+                    int c0, c1;
+                    chunk_range(gi / CH, gf, G, c0, c1);
+                    const int g = c0 + gi % CH;
+                    const uint32_t gg = gc + (uint32_t)gi;
+                    const int q = (int)(gg % NS);
+                    const uint32_t use = gg / NS;
                     if (use > 0 && !wait(&S.sempty[q], (use - 1) & 1u)) { ok = false; break; }
-                    typename Smem<N>::SeedSlot &sd = S.sd[q];
-                    mbar_arrive_expect_tx(&S.sfull[q], SEED_TX);
-                    bulk_g2s(sd.seed, a.seeds + (gb + g) * a.seed_stride + (int64_t)tile * 128, 128 * 8, &S.sfull[q]);
-                    bulk_g2s(sd.coef, a.coef32 + cb + (int64_t)g * GLG_GROUP, GLG_GROUP * 16, &S.sfull[q]);
+                    if constexpr (T) {
+                        mbar_arrive_expect_tx(&S.sfull[q], GLG_PLM_TILE_BYTES);
+                        bulk_g2s(&S.sd[q], a.plm + ((gb + g) * a.ntiles + tile) * (GLG_PLM_TILE_BYTES / 16),
+                                 GLG_PLM_TILE_BYTES, &S.sfull[q]);
+                    } else {
+                        SeedSlot &sd = S.sd[q];
+                        mbar_arrive_expect_tx(&S.sfull[q], SEED_TX);
+                        bulk_g2s(sd.seed, a.seeds + (gb + g) * a.seed_stride + (int64_t)tile * 128, 128 * 8,
+                                 &S.sfull[q]);
+                        bulk_g2s(sd.coef, a.coef32 + cb + (int64_t)g * GLG_GROUP, GLG_GROUP * 16, &S.sfull[q]);
+                    }
                     last_use[q] = use;
                 }
                 gc += (uint32_t)(G - gf);
             }
             if (!ok) fail();
-            for (int q = 0; q < NSEED; ++q)
+            for (int q = 0; q < NS; ++q)
                 if (last_use[q] >= 0)
                     for (uint32_t i = 0; i < WAIT_LIMIT && !mbar_try_wait(&S.sfull[q], (uint32_t)(last_use[q] & 1)); ++i) {
                     }
@@ -536,9 +615,9 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
 
 // Bpack[goff[m] + g] = 4 tiles (E_hi, E_lo, O_hi, O_lo) of N x 8 tf32 values,
 // element (n, k) of a tile at float index (n/8)*64 + (k/4)*32 + (n%8)*4 + k%4,
-// holding the re (n even) or im (n odd) part of a_lm d_l of map n/2 at
-// l = m + 16 g + 2 k + parity (d_l the group scale of the recurrence; the
-// product's rounding error is carried into the lo part).  One thread per (group, parity, map, k/4): it
+// holding the re (n even) or im (n odd) part of a_lm d_l (1 + ACC_BIAS) of
+// map n/2 at l = m + 16 g + 2 k + parity (d_l the group scale of the
+// recurrence; the product's rounding error is carried into the lo part).  One thread per (group, parity, map, k/4): it
 // loads the 4 alm of its k quad and writes re and im of the hi and lo tiles
 // as 16-byte stores; consecutive threads take consecutive maps and quads, so
 // a warp writes 1 KB of a tile contiguously.
@@ -580,8 +659,10 @@ __global__ void __launch_bounds__(256) k_pack_b(int mmax, int lmax, int nmaps, i
         const uint32_t zr = tf32_rna(pr), zi = tf32_rna(pi);
         r4[kk] = __uint_as_float(zr);
         i4[kk] = __uint_as_float(zi);
-        rl4[kk] = __uint_as_float(tf32_rna(__fadd_rn(__fsub_rn(pr, __uint_as_float(zr)), er)));
-        il4[kk] = __uint_as_float(tf32_rna(__fadd_rn(__fsub_rn(pi, __uint_as_float(zi)), ei)));
+        // lo = the remainder of the hi part, the product's rounding error and
+        // the accumulator-bias scaling pr * ACC_BIAS
+        rl4[kk] = __uint_as_float(tf32_rna(fmaf(pr, ACC_BIAS, __fadd_rn(__fsub_rn(pr, __uint_as_float(zr)), er))));
+        il4[kk] = __uint_as_float(tf32_rna(fmaf(pi, ACC_BIAS, __fadd_rn(__fsub_rn(pi, __uint_as_float(zi)), ei))));
     }
     float *dst = bpack + gg * (int64_t)(32 * N) + ng * 64 + j * 32 + mi * 8;
     float *th = dst + (2 * par) * (8 * N), *tl = dst + (2 * par + 1) * (8 * N);
@@ -630,17 +711,22 @@ int launch_tc(const glg_plan *P, const float2 *alm, int nmaps, float *bpack, flo
     a.ucount = reinterpret_cast<unsigned long long *>(reinterpret_cast<char *>(err) + 64) + run.slot;
     a.wait_limit = g_test_wait_limit ? g_test_wait_limit : WAIT_LIMIT;
     a.stall = g_test_stall;
-    // more than half of the SM's shared memory: one CTA per SM, so no two
-    // CTAs contend for the 512 tensor-memory columns
-    size_t smem = sizeof(Smem<N>) + 128;
-    if (smem < 120 * 1024) smem = 120 * 1024;
-    cudaFuncSetAttribute(k_leg_tc<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    a.plm = P->plm;
     int nsm = 0, dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     const int64_t grid = a.nunits < nsm ? a.nunits : nsm;
-    GLG_LAUNCH_SCOPE("k_leg_tc", st);
-    k_leg_tc<N><<<(unsigned)grid, THREADS, smem, st>>>(a);
+    // more than half of the SM's shared memory: one CTA per SM, so no two
+    // CTAs contend for the 512 tensor-memory columns
+    auto go = [&](auto kern, size_t bytes) {
+        size_t smem = bytes + 128;
+        if (smem < 120 * 1024) smem = 120 * 1024;
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        GLG_LAUNCH_SCOPE("k_leg_tc", st);
+        kern<<<(unsigned)grid, THREADS, smem, st>>>(a);
+    };
+    if (P->plm) go(k_leg_tc<N, true>, sizeof(Smem<N, true>));
+    else go(k_leg_tc<N, false>, sizeof(Smem<N, false>));
     GLG_CHECK_LAUNCH("k_leg_tc");
     return GLG_OK;
 }

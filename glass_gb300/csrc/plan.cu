@@ -193,6 +193,14 @@ static void factor_ring(int n, int *radix, int *nst) {
     *nst = k;
 }
 
+// Device bytes a plan's P_lm table may take (glg_set_plm_table_budget).
+static std::atomic<size_t> g_plm_budget{(size_t)160 << 30};
+
+extern "C" int glg_set_plm_table_budget(size_t bytes) {
+    g_plm_budget.store(bytes);
+    return GLG_OK;
+}
+
 // Failure injection for tests: the n-th plan allocation from now (1 = the
 // next) reports cudaErrorMemoryAllocation without calling cudaMalloc.
 static std::atomic<int> g_fail_alloc{0};
@@ -222,7 +230,8 @@ extern "C" void glg_plan_destroy(glg_plan *P) {
                     P->mofs,  P->coef,      P->lmm,     P->lmm_scale, P->fft_radix,
                     P->fft_nst, P->tw_ofs,  P->tw,      P->cth32,  P->tw32,   P->coef32,
                     P->goff,  P->seeds,     P->lstart,  P->tfirst, P->bucket_pairs, P->chirp_ofs,
-                    P->chirp, P->pos_ofs, P->pos16,   P->blu_ofs, P->blu_M,  P->blu_H,  P->twM};
+                    P->chirp, P->pos_ofs, P->pos16,   P->blu_ofs, P->blu_M,  P->blu_H,  P->twM,
+                    P->plm};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     delete[] P->bucket_pairs_host;
@@ -282,7 +291,7 @@ __global__ void k_plan_seeds(int lmax, int npairs, const double *__restrict__ ct
         const int j = (l - m) / GLG_GROUP;
         const int lg0 = m + j * GLG_GROUP;
         if (pend >= 0) {  // l == s0 + 1 of the pending seed
-            seeds[pend * sstride + p] = make_float2(sx, (float)tv);
+            if (seeds) seeds[pend * sstride + p] = make_float2(sx, (float)tv);
             pend = -1;
         }
         if (ls >= 0 && l == (lg0 > ls ? lg0 : ls)) {
@@ -290,9 +299,9 @@ __global__ void k_plan_seeds(int lmax, int npairs, const double *__restrict__ ct
             pend = g0 + j;
         }
         const bool group_end = ((l - m) % GLG_GROUP == GLG_GROUP - 1) || l == lmax;
-        if (group_end && ls < 0) seeds[(g0 + j) * sstride + p] = make_float2(0.f, 0.f);
+        if (group_end && ls < 0 && seeds) seeds[(g0 + j) * sstride + p] = make_float2(0.f, 0.f);
     }
-    if (pend >= 0) seeds[pend * sstride + p] = make_float2(sx, 0.f);
+    if (pend >= 0 && seeds) seeds[pend * sstride + p] = make_float2(sx, 0.f);
     lstart[(int64_t)m * npairs + p] = ls < 0 ? lmax + 1 : ls;
 }
 
@@ -337,6 +346,58 @@ __global__ void k_plan_coef32(int lmax, const int64_t *__restrict__ mofs, const 
         dst[base + l - m] = make_float4(al.x, al.y, (float)d, 0.f);
         d2 = d1;
         d1 = d;
+    }
+}
+
+// P_lm table of the fast contraction: for every (m, group g, ring tile) one
+// tile [l quad q][ring pair r][4] of mu_l = lambda_l / d_l, l = m + 16 g +
+// 4 q + i, d_l the FP32 group scale of coef32 (the B operand carries d_l),
+// from the FP64 extended-range recurrence rounded once to FP32; zero beyond
+// lmax and for ring pairs beyond the last.  One thread per (m, ring pair of
+// a whole tile), float4 stores coalesced across the tile's ring pairs.
+__global__ void k_plan_plm(int lmax, int npairs, int ntiles, const double *__restrict__ cth,
+                           const int64_t *__restrict__ mofs, const double2 *__restrict__ coef,
+                           const double *__restrict__ lmm, const int *__restrict__ lmm_scale,
+                           const int64_t *__restrict__ goff, const float4 *__restrict__ coef32,
+                           float4 *__restrict__ plm) {
+    const int m = blockIdx.y;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;  // < ntiles * 128
+    const bool live = p < npairs;
+    const int pp = live ? p : npairs - 1;
+    const double x = cth[pp];
+    double l0 = 0.0, l1 = lmm[(int64_t)m * npairs + pp];
+    int sc = lmm_scale[(int64_t)m * npairs + pp];
+    const int64_t base = mofs[m];
+    const int G = (lmax - m + GLG_GROUP) / GLG_GROUP;
+    float4 q4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    float *qv = &q4.x;
+    for (int t = 0; t < G * GLG_GROUP; ++t) {
+        const int l = m + t;
+        float v = 0.f;
+        if (l <= lmax) {
+            if (l > m) {
+                double nl;
+                if (l == m + 1) {
+                    nl = sqrt(2.0 * m + 3.0) * x * l1;
+                } else {
+                    const double2 ab = coef[base + t];
+                    nl = ab.x * (x * l1) - ab.y * l0;
+                }
+                l0 = l1;
+                l1 = nl;
+                if (sc < 0 && fabs(nl) > GLG_TWO_P400) {
+                    l0 *= GLG_TWO_M800;
+                    l1 *= GLG_TWO_M800;
+                    sc += 1;
+                }
+            }
+            if (live && sc == 0) v = (float)(l1 / (double)coef32[base + t].z);
+        }
+        qv[t & 3] = v;
+        if ((t & 3) == 3) {
+            const int64_t gt = (goff[m] + t / GLG_GROUP) * ntiles + p / 128;
+            plm[(gt * 4 + (t % GLG_GROUP) / 4) * 128 + p % 128] = q4;
+        }
     }
 }
 
@@ -540,13 +601,30 @@ int glg_plan_prepare_fast(glg_plan *P, cudaStream_t st) {
     int rc;
     if ((rc = dalloc(P, &P->cth32, np)) || (rc = dalloc(P, &P->tw32, ntw)) ||
         (rc = dalloc(P, &P->coef32, P->nalm + GLG_GROUP)) || (rc = dalloc(P, &P->goff, lmax + 2)) ||
-        (rc = dalloc(P, &P->seeds, (size_t)P->ngroups * P->seed_stride)) ||
         (rc = dalloc(P, &P->lstart, (size_t)(lmax + 1) * np)) ||
         (rc = dalloc(P, &P->tfirst, (size_t)(lmax + 1) * ((np + 127) / 128))))
         return rc;
+    // the P_lm table when it fits the budget and the free device memory
+    // (with 4 GiB to spare), else the seeds of the FP32 recurrence
+    const int ntiles = (np + 127) / 128;
+    const size_t tbytes = (size_t)GLG_PLM_TILE_BYTES * (size_t)P->ngroups * ntiles;
+    size_t free_b = 0, total_b = 0;
+    bool table = tbytes <= g_plm_budget.load() && cudaMemGetInfo(&free_b, &total_b) == cudaSuccess &&
+                 tbytes + ((size_t)4 << 30) <= free_b;
+    if (table && cudaMalloc((void **)&P->plm, tbytes) != cudaSuccess) {
+        cudaGetLastError();  // not enough room after all: recurrence path
+        P->plm = nullptr;
+        table = false;
+    }
+    if (table) {
+        P->plm_bytes = tbytes;
+        P->bytes += tbytes;
+    } else if ((rc = dalloc(P, &P->seeds, (size_t)P->ngroups * P->seed_stride))) {
+        return rc;
+    }
     cudaError_t e = cudaMemcpyAsync(P->goff, goff.data(), sizeof(int64_t) * goff.size(),
                                     cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess)
+    if (e == cudaSuccess && !table)
         e = cudaMemsetAsync(P->seeds, 0, sizeof(float2) * (size_t)P->ngroups * P->seed_stride, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(P->coef32, 0, sizeof(float4) * (size_t)(P->nalm + GLG_GROUP), st);
     if (e != cudaSuccess) return glg_cuda_status(e, "glg_plan_prepare_fast: upload");
@@ -559,6 +637,9 @@ int glg_plan_prepare_fast(glg_plan *P, cudaStream_t st) {
                                      P->goff, P->seeds, P->seed_stride, P->lstart);
     k_plan_tfirst<<<dim3((np + 127) / 128, lmax + 1), 128, 0, st>>>(lmax, np, (np + 127) / 128, P->lstart,
                                                                    P->tfirst);
+    if (table)
+        k_plan_plm<<<dim3(ntiles, lmax + 1), 128, 0, st>>>(lmax, np, ntiles, P->cth, P->mofs, P->coef, P->lmm,
+                                                          P->lmm_scale, P->goff, P->coef32, P->plm);
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return glg_cuda_status(e, "glg_plan_prepare_fast");
@@ -640,6 +721,8 @@ extern "C" int glg_plan_create(int nside, int lmax, void *stream, glg_plan **out
 }
 
 extern "C" size_t glg_plan_device_bytes(const glg_plan *P) { return P ? P->bytes : 0; }
+
+extern "C" int glg_plan_has_plm_table(const glg_plan *P) { return P && P->plm ? 1 : 0; }
 
 extern "C" int glg_plan_info(const glg_plan *P, int *nside, int *lmax, int *nrings, int64_t *npix,
                              int64_t *nalm) {

@@ -33,6 +33,8 @@
 // blocks that share a ring's tables run together).
 #include <cuda_runtime.h>
 
+#include <math.h>
+
 #include <algorithm>
 
 #include "glg_internal.cuh"
@@ -88,6 +90,39 @@ constexpr float R2 = 0.70710678118654752440f;   // cos(pi/4)
 constexpr float C8 = 0.92387953251128675613f;   // cos(pi/8)
 constexpr float S8 = 0.38268343236508977173f;   // sin(pi/8)
 
+// Radix constants as FP32 (hi, lo) pairs: hi the float nearest to the exact
+// value, lo the float nearest to the remainder.  Products with them are taken
+// as fma(x, hi, x * lo), one rounding of the full product: the constants'
+// own rounding (cos(pi/4), cos(pi/8) and sin(pi/8) all round down in FP32)
+// would otherwise shrink every output of every radix-8/16 butterfly by the
+// same 2-3e-8, a bias that accumulates over the passes of a transform.
+constexpr float R2L = 1.21016175e-08f, C8L = 2.83074897e-08f, S8L = 6.22335072e-09f;
+// e^{2 pi i j / R} for the odd radices R = 3, 5, 7, 11, 13 (j = 0 .. R-1),
+// from odd_ofs(R) on in the tables.
+__constant__ float2 kOddHi[] = {
+    {1.0f, 0.0f}, {-0.5f, 0.866025388f}, {-0.5f, -0.866025388f},  // R = 3
+    {1.0f, 0.0f}, {0.309017003f, 0.95105654f}, {-0.809017003f, 0.587785244f}, {-0.809017003f, -0.587785244f}, {0.309017003f, -0.95105654f},  // R = 5
+    {1.0f, 0.0f}, {0.623489797f, 0.781831503f}, {-0.222520933f, 0.974927902f}, {-0.90096885f, 0.433883727f}, {-0.90096885f, -0.433883727f}, {-0.222520933f, -0.974927902f}, {0.623489797f, -0.781831503f},  // R = 7
+    {1.0f, 0.0f}, {0.841253519f, 0.540640831f}, {0.415415019f, 0.909631968f}, {-0.142314836f, 0.989821434f}, {-0.654860735f, 0.755749583f}, {-0.959492981f, 0.281732559f}, {-0.959492981f, -0.281732559f}, {-0.654860735f, -0.755749583f}, {-0.142314836f, -0.989821434f}, {0.415415019f, -0.909631968f}, {0.841253519f, -0.540640831f},  // R = 11
+    {1.0f, 0.0f}, {0.885456026f, 0.46472317f}, {0.568064749f, 0.822983861f}, {0.120536678f, 0.992708862f}, {-0.3546049f, 0.935016215f}, {-0.748510778f, 0.663122654f}, {-0.970941842f, 0.239315659f}, {-0.970941842f, -0.239315659f}, {-0.748510778f, -0.663122654f}, {-0.3546049f, -0.935016215f}, {0.120536678f, -0.992708862f}, {0.568064749f, -0.822983861f}, {0.885456026f, -0.46472317f},  // R = 13
+};
+__constant__ float2 kOddLo[] = {
+    {0.0f, 0.0f}, {0.0f, 1.55436251e-08f}, {0.0f, -1.55436251e-08f},  // R = 3
+    {0.0f, 0.0f}, {-8.2076026e-09f, -2.3717206e-08f}, {8.2076026e-09f, 8.30443625e-09f}, {8.2076026e-09f, -8.30443625e-09f}, {-8.2076026e-09f, 2.3717206e-08f},  // R = 5
+    {0.0f, 0.0f}, {4.74340744e-09f, -2.04463984e-08f}, {-1.40111578e-09f, 9.96014382e-09f}, {-1.8243453e-08f, 1.25207258e-08f}, {-1.8243453e-08f, -1.25207258e-08f}, {-1.40111578e-09f, -9.96014382e-09f}, {4.74340744e-09f, 2.04463984e-08f},  // R = 7
+    {0.0f, 0.0f}, {1.37729534e-08f, -1.35380551e-08f}, {-5.79503423e-09f, 2.78099623e-08f}, {-1.89041915e-09f, 7.8599367e-09f}, {9.94290095e-10f, -8.89006557e-09f}, {7.81937093e-09f, -2.36267184e-09f}, {7.81937093e-09f, 2.36267184e-09f}, {9.94290095e-10f, 8.89006557e-09f}, {-1.89041915e-09f, -7.8599367e-09f}, {-5.79503423e-09f, -2.78099623e-08f}, {1.37729534e-08f, 1.35380551e-08f},  // R = 11
+    {0.0f, 0.0f}, {5.2776547e-11f, 2.24014918e-09f}, {-2.50971954e-09f, 4.92411312e-09f}, {2.71597456e-09f, 1.22702035e-08f}, {1.28407347e-08f, 2.78378494e-08f}, {2.97791853e-08f, 4.27961355e-09f}, {2.41762734e-08f, 5.47980328e-09f}, {2.41762734e-08f, -5.47980328e-09f}, {2.97791853e-08f, -4.27961355e-09f}, {1.28407347e-08f, -2.78378494e-08f}, {2.71597456e-09f, -1.22702035e-08f}, {-2.50971954e-09f, -4.92411312e-09f}, {5.2776547e-11f, -2.24014918e-09f},  // R = 13
+};
+__device__ __forceinline__ int odd_ofs(int R) {
+    return R == 3 ? 0 : R == 5 ? 3 : R == 7 ? 8 : R == 11 ? 15 : 26;
+}
+__device__ __forceinline__ float mulc(float x, float h, float l) { return fmaf(x, h, x * l); }
+// a * (wh + wl) with one rounding per component
+__device__ __forceinline__ c32 cmulc(c32 a, c32 wh, c32 wl) {
+    const float pr = fmaf(a.x, wl.x, -(a.y * wl.y)), pi = fmaf(a.x, wl.y, a.y * wl.x);
+    return {fmaf(a.x, wh.x, fmaf(-a.y, wh.y, pr)), fmaf(a.x, wh.y, fmaf(a.y, wh.x, pi))};
+}
+
 template <int DIR>
 __device__ __forceinline__ void dft8(c32 *v) {
     c32 e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
@@ -95,9 +130,9 @@ __device__ __forceinline__ void dft8(c32 *v) {
     dft4<DIR>(e0, e1, e2, e3);
     dft4<DIR>(o0, o1, o2, o3);
     // o_k *= e^{DIR 2 pi i k / 8}
-    o1 = c32{R2 * (o1.x - DIR * o1.y), R2 * (o1.y + DIR * o1.x)};
+    o1 = c32{mulc(o1.x - DIR * o1.y, R2, R2L), mulc(o1.y + DIR * o1.x, R2, R2L)};
     o2 = mul_i<DIR>(o2);
-    o3 = c32{R2 * (-o3.x - DIR * o3.y), R2 * (DIR * o3.x - o3.y)};
+    o3 = c32{mulc(-o3.x - DIR * o3.y, R2, R2L), mulc(DIR * o3.x - o3.y, R2, R2L)};
     v[0] = cadd(e0, o0);
     v[4] = csub(e0, o0);
     v[1] = cadd(e1, o1);
@@ -126,15 +161,17 @@ __device__ __forceinline__ void dft16(c32 *v) {
     // u[4 k1 + j2] *= e^{DIR 2 pi i j2 k1 / 16}
     const c32 w1 = {C8, D * S8}, w2 = {R2, D * R2}, w3 = {S8, D * C8};
     const c32 w6 = {-R2, D * R2}, w9 = {-C8, -D * S8};
-    u[5] = cmul(u[5], w1);
-    u[6] = cmul(u[6], w2);
-    u[7] = cmul(u[7], w3);
-    u[9] = cmul(u[9], w2);
+    const c32 l1 = {C8L, D * S8L}, l2 = {R2L, D * R2L}, l3 = {S8L, D * C8L};
+    const c32 l6 = {-R2L, D * R2L}, l9 = {-C8L, -D * S8L};
+    u[5] = cmulc(u[5], w1, l1);
+    u[6] = cmulc(u[6], w2, l2);
+    u[7] = cmulc(u[7], w3, l3);
+    u[9] = cmulc(u[9], w2, l2);
     u[10] = mul_i<DIR>(u[10]);
-    u[11] = cmul(u[11], w6);
-    u[13] = cmul(u[13], w3);
-    u[14] = cmul(u[14], w6);
-    u[15] = cmul(u[15], w9);
+    u[11] = cmulc(u[11], w6, l6);
+    u[13] = cmulc(u[13], w3, l3);
+    u[14] = cmulc(u[14], w6, l6);
+    u[15] = cmulc(u[15], w9, l9);
 #pragma unroll
     for (int k1 = 0; k1 < 4; ++k1) dft4<DIR>(u[4 * k1], u[4 * k1 + 1], u[4 * k1 + 2], u[4 * k1 + 3]);
 #pragma unroll
@@ -143,16 +180,23 @@ __device__ __forceinline__ void dft16(c32 *v) {
         for (int k2 = 0; k2 < 4; ++k2) v[k1 + 4 * k2] = u[4 * k1 + k2];
 }
 
-// Odd prime radix with table twiddles e^{DIR 2 pi i (j k mod R) / R}.
+// Odd prime radix with the constant twiddles e^{DIR 2 pi i (j k mod R) / R}.
 template <int R, int DIR>
-__device__ __forceinline__ void dft_odd(c32 *v, const c32 *wh, int n) {
+__device__ __forceinline__ void dft_odd(c32 *v) {
     c32 y[R];
-    const int step = n / R;
 #pragma unroll
     for (int k = 0; k < R; ++k) {
         c32 acc = v[0];
 #pragma unroll
-        for (int j = 1; j < R; ++j) acc = cadd(acc, cmul(v[j], tw<DIR>(wh, n, ((j * k) % R) * step)));
+        for (int j = 1; j < R; ++j) {
+            const int q = odd_ofs(R) + (j * k) % R;
+            c32 h = {kOddHi[q].x, kOddHi[q].y}, l = {kOddLo[q].x, kOddLo[q].y};
+            if (DIR < 0) {
+                h.y = -h.y;
+                l.y = -l.y;
+            }
+            acc = cadd(acc, cmulc(v[j], h, l));
+        }
         y[k] = acc;
     }
 #pragma unroll
@@ -172,7 +216,7 @@ __device__ __forceinline__ void dft(c32 *v, const c32 *wh, int n) {
     } else if constexpr (R == 16) {
         dft16<DIR>(v);
     } else {
-        dft_odd<R, DIR>(v, wh, n);
+        dft_odd<R, DIR>(v);
     }
 }
 
@@ -299,7 +343,32 @@ __device__ __forceinline__ float epi(float v, int kind, float hv, float lam) {
 struct Epi32 {
     int kind[EPI_MAX];
     float hvar[EPI_MAX], lam[EPI_MAX];  // var / 2 and lambda per map
+    float thr[EPI_MAX];                 // tail-refinement threshold on the Gaussian value (+inf: none)
+    int *rcount;                        // tail-refinement list: entries appended, capacity, items
+    int rcap;
+    int4 *ritems;
 };
+
+// Tail refinement.  The lognormal map's relative RMS error is dominated by
+// its largest pixels (weight y^2 ~ e^{2 g}); at sigma^2 ~ 7 the top few
+// thousand of 50 M pixels carry ~90% of it, and there the FP32 transform's
+// rounding (~1.4e-7 of sigma, plus the rounding of g itself before the
+// exponential) is what is left.  The output loops list every pixel whose
+// Gaussian value exceeds thr = var/2 + log1p(sqrt(KAPPA expm1(var))), i.e.
+// whose lognormal value exceeds sqrt(KAPPA) times the map's RMS, on maps
+// whose variance reaches REFINE_MIN_VAR; k_refine then recomputes those
+// pixels from the Legendre sums by a direct FP64 sum over m and the FP64
+// transform.  Below REFINE_MIN_VAR the FP32 pipeline's error stays well
+// inside 1e-6 without it.
+constexpr double REFINE_KAPPA = 1000.0;
+constexpr double REFINE_MIN_VAR = 4.0;
+
+__device__ __forceinline__ void refine_note(const Epi32 &e, int map, float g, int ring, int k) {
+    if (g > e.thr[map]) {
+        const int slot = atomicAdd(e.rcount, 1);
+        if (slot < e.rcap) e.ritems[slot] = make_int4(map, ring, k, 0);
+    }
+}
 
 struct RingArgs {
     int nrings, mmax, nmaps;
@@ -473,6 +542,18 @@ __global__ void __launch_bounds__(POW2 ? TMAX_POW2 : TMAX) k_ring32(const RingAr
             return (sl & 1) ? csub(u0, u1) : cadd(u0, u1);
         };
         const c32 v0 = at(ps.x), v1 = at(ps.y), v2 = at(ps.z), v3 = at(ps.w);
+        if (kind == GLG_EPI_LOGNORMAL) {
+            refine_note(e, map, v0.x, rn, 4 * q);
+            refine_note(e, map, v1.x, rn, 4 * q + 1);
+            refine_note(e, map, v2.x, rn, 4 * q + 2);
+            refine_note(e, map, v3.x, rn, 4 * q + 3);
+            if (!equator) {
+                refine_note(e, map, v0.y, rs, 4 * q);
+                refine_note(e, map, v1.y, rs, 4 * q + 1);
+                refine_note(e, map, v2.y, rs, 4 * q + 2);
+                refine_note(e, map, v3.y, rs, 4 * q + 3);
+            }
+        }
         *reinterpret_cast<float4 *>(mp + sN + 4 * q) =
             make_float4(epi(v0.x, kind, hv, lam), epi(v1.x, kind, hv, lam), epi(v2.x, kind, hv, lam),
                         epi(v3.x, kind, hv, lam));
@@ -522,6 +603,18 @@ __global__ void __launch_bounds__(TMAX_POW2) k_ring32_blu(const RingArgs a, cons
         const c32 v1 = cscale(cmul(Z[zi(4 * q + 1)], c32{ca.z, ca.w}), invM);
         const c32 v2 = cscale(cmul(Z[zi(4 * q + 2)], c32{cb.x, cb.y}), invM);
         const c32 v3 = cscale(cmul(Z[zi(4 * q + 3)], c32{cb.z, cb.w}), invM);
+        if (kind == GLG_EPI_LOGNORMAL) {
+            refine_note(e, map, v0.x, rn, 4 * q);
+            refine_note(e, map, v1.x, rn, 4 * q + 1);
+            refine_note(e, map, v2.x, rn, 4 * q + 2);
+            refine_note(e, map, v3.x, rn, 4 * q + 3);
+            if (!equator) {
+                refine_note(e, map, v0.y, rs, 4 * q);
+                refine_note(e, map, v1.y, rs, 4 * q + 1);
+                refine_note(e, map, v2.y, rs, 4 * q + 2);
+                refine_note(e, map, v3.y, rs, 4 * q + 3);
+            }
+        }
         *reinterpret_cast<float4 *>(mp + sN + 4 * q) =
             make_float4(epi(v0.x, kind, hv, lam), epi(v1.x, kind, hv, lam), epi(v2.x, kind, hv, lam),
                         epi(v3.x, kind, hv, lam));
@@ -554,6 +647,58 @@ __global__ void k_transpose32(const float2 *__restrict__ F, float2 *__restrict__
         if (m < nm && r < re) dst[(int64_t)r * nm + m] = tile[threadIdx.x][y];
     }
 }
+
+struct RefineArgs {
+    int nrings, npairs, mmax;
+    int64_t npix;
+    const int *nph, *half;
+    const int64_t *startN, *startS;
+    const float2 *Ft;  // [map][ring][m]
+    float *maps;
+    const int *hdr;    // [0] entries appended, [1] entries already refined
+    int cap;
+    const int4 *items;  // (map, ring, pixel within the ring, -)
+    double hv[EPI_MAX], lam[EPI_MAX];
+};
+
+// One warp per listed pixel: g = F_0 + 2 Re sum_{m>0} F_m e^{i m phi} in FP64
+// from the FP32 Legendre sums of its ring (lane L takes m = L + 32 j, summed
+// by Horner in z^32 from the top, then times z^L; angles reduced exactly as
+// integer multiples of pi / nph), a fixed-order warp sum, and the lognormal
+// value in FP64 stored over the FP32 one.
+__global__ void __launch_bounds__(256) k_refine(const RefineArgs r) {
+    const int lane = threadIdx.x & 31;
+    const int n0 = r.hdr[1];
+    const int n1 = r.hdr[0] < r.cap ? r.hdr[0] : r.cap;
+    for (int it = n0 + blockIdx.x * 8 + (threadIdx.x >> 5); it < n1; it += gridDim.x * 8) {
+        const int4 e = r.items[it];
+        const int map = e.x, ring = e.y, k = e.z;
+        const int p = ring < r.npairs ? ring : r.nrings - 1 - ring;
+        const int64_t nph = r.nph[p], a1 = 2LL * k + r.half[p];  // phi = pi a1 / nph
+        const float2 *F = r.Ft + ((int64_t)map * r.nrings + ring) * (r.mmax + 1);
+        double zc, zs, lc, ls;
+        sincospi((double)((32 * a1) % (2 * nph)) / (double)nph, &zs, &zc);     // z^32
+        sincospi((double)((lane * a1) % (2 * nph)) / (double)nph, &ls, &lc);   // z^L
+        double sr = 0.0, si = 0.0;
+        const int jt = (r.mmax - lane) >= 0 ? (r.mmax - lane) / 32 : -1;
+        for (int j = jt; j >= 0; --j) {
+            const int m = lane + 32 * j;
+            const float2 f = F[m];
+            const double cm = m ? 2.0 : 1.0;
+            const double tr = fma(sr, zc, fma(-si, zs, cm * (double)f.x));
+            si = fma(sr, zs, fma(si, zc, cm * (double)f.y));
+            sr = tr;
+        }
+        double v = sr * lc - si * ls;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) {
+            const int64_t start = ring < r.npairs ? r.startN[p] : r.startS[p];
+            r.maps[(int64_t)map * r.npix + start + k] = (float)(r.lam[map] * expm1(v - r.hv[map]));
+        }
+    }
+}
+
+__global__ void k_refine_done(int *hdr, int cap) { hdr[1] = hdr[0] < cap ? hdr[0] : cap; }
 
 }  // namespace
 
@@ -619,12 +764,59 @@ static int launch_transpose(const float2 *F, float2 *Ft, int nm, int nr, int rb,
 }
 
 int glg_launch_ring_syn_f32(const glg_plan *P, const float2 *F, float2 *Ft, int nmaps, float *maps,
-                            const glg_epilogue *epi_in, cudaStream_t st) {
-    return glg_launch_ring_syn_f32_range(P, F, Ft, nmaps, maps, epi_in, 0, P->npairs, st);
+                            const glg_epilogue *epi_in, const glg_refine_list *rl, cudaStream_t st) {
+    return glg_launch_ring_syn_f32_range(P, F, Ft, nmaps, maps, epi_in, 0, P->npairs, rl, st);
+}
+
+// Lognormal threshold of the tail refinement of map k (+inf: none).
+static float refine_threshold(const glg_epilogue *epi, int k, int kind) {
+    if (kind != GLG_EPI_LOGNORMAL || !epi || !epi->var || epi->var[k] < REFINE_MIN_VAR) return INFINITY;
+    const double v = epi->var[k];
+    return (float)(0.5 * v + log1p(sqrt(REFINE_KAPPA * expm1(v))));
+}
+
+bool glg_refine_wanted(const glg_epilogue *epi, int nmaps) {
+    for (int k = 0; k < nmaps && epi; ++k) {
+        const int kind = epi->kinds ? epi->kinds[k] : epi->kind;
+        if (refine_threshold(epi, k, kind) < INFINITY) return true;
+    }
+    return false;
+}
+
+int glg_launch_refine(const glg_plan *P, const float2 *Ft, int nmaps, float *maps, const glg_epilogue *epi,
+                      const glg_refine_list &rl, cudaStream_t st) {
+    if (!glg_refine_wanted(epi, nmaps)) return GLG_OK;
+    RefineArgs r;
+    r.nrings = P->nrings;
+    r.npairs = P->npairs;
+    r.mmax = P->mmax;
+    r.npix = P->npix;
+    r.nph = P->nph;
+    r.half = P->half;
+    r.startN = P->startN;
+    r.startS = P->startS;
+    r.Ft = Ft;
+    r.maps = maps;
+    r.hdr = rl.hdr;
+    r.cap = rl.cap;
+    r.items = rl.items;
+    for (int k = 0; k < EPI_MAX; ++k) {
+        r.hv[k] = k < nmaps && epi->var ? 0.5 * epi->var[k] : 0.0;
+        r.lam[k] = k < nmaps && epi->lamda ? epi->lamda[k] : 1.0;
+    }
+    {
+        GLG_LAUNCH_SCOPE("k_refine", st);
+        k_refine<<<608, 256, 0, st>>>(r);
+        GLG_CHECK_LAUNCH("k_refine");
+    }
+    k_refine_done<<<1, 1, 0, st>>>(rl.hdr, rl.cap);
+    GLG_CHECK_LAUNCH("k_refine_done");
+    return GLG_OK;
 }
 
 int glg_launch_ring_syn_f32_range(const glg_plan *P, const float2 *F, float2 *Ft, int nmaps, float *maps,
-                                  const glg_epilogue *epi_in, int p0, int p1, cudaStream_t st) {
+                                  const glg_epilogue *epi_in, int p0, int p1, const glg_refine_list *rl,
+                                  cudaStream_t st) {
     if (nmaps > EPI_MAX) {
         glg_set_error("fast ring FFT: at most 40 maps per call");
         return GLG_ERR_UNSUPPORTED;
@@ -652,7 +844,11 @@ int glg_launch_ring_syn_f32_range(const glg_plan *P, const float2 *F, float2 *Ft
         e.kind[k] = !on ? GLG_EPI_NONE : (epi_in->kinds ? epi_in->kinds[k] : epi_in->kind);
         e.hvar[k] = (on && epi_in->var) ? (float)(0.5 * epi_in->var[k]) : 0.f;
         e.lam[k] = (on && epi_in->lamda) ? (float)epi_in->lamda[k] : 1.f;
+        e.thr[k] = (on && rl) ? refine_threshold(epi_in, k, e.kind[k]) : INFINITY;
     }
+    e.rcount = rl ? rl->hdr : nullptr;
+    e.rcap = rl ? rl->cap : 0;
+    e.ritems = rl ? rl->items : nullptr;
     const bool whole = p0 == 0 && p1 == P->npairs;
     for (int b = 0; b < P->nbuckets; ++b) {
         const glg_ring_bucket &B = P->buckets[b];
@@ -682,6 +878,10 @@ int glg_launch_ring_bucket_f32(const glg_plan *P, int bucket, int threads, const
         e.kind[k] = GLG_EPI_NONE;
         e.hvar[k] = 0.f;
         e.lam[k] = 1.f;
+        e.thr[k] = INFINITY;
     }
+    e.rcount = nullptr;
+    e.rcap = 0;
+    e.ritems = nullptr;
     return launch_bucket(P, B, threads, a, e, st);
 }

@@ -27,11 +27,49 @@ static size_t fast_pack_bytes(const glg_plan *P, int nmaps) {
     return (size_t)ng * 128 * N;
 }
 
+// Fast-form workspace: status block | B pack | F [map][m][ring] |
+// F [map][ring][m] | tail-refinement header (256 B) and list.
+namespace {
+constexpr int kRefinePerMap = 65536;  // listed pixels per map of a call
+struct FastWs {
+    int *err;
+    float *bpack;
+    float2 *F, *Ft;
+    glg_refine_list rl;
+    char *end;
+};
+size_t up256(size_t b) { return (b + 255) & ~(size_t)255; }
+// Offsets from the workspace's start (256-byte aligned blocks: the lists'
+// int4 items and the staged maps' float4 stores need 16-byte alignment).
+FastWs fast_ws(const glg_plan *P, int nmaps, void *ws) {
+    FastWs w;
+    char *c = (char *)ws;
+    const size_t fb = up256(sizeof(float2) * (size_t)nmaps * P->nrings * (P->mmax + 1));
+    w.err = (int *)c;
+    c += GLG_WS_STATUS_BYTES;
+    w.bpack = (float *)c;
+    c += up256(fast_pack_bytes(P, nmaps));
+    w.F = (float2 *)c;
+    c += fb;
+    w.Ft = (float2 *)c;
+    c += fb;
+    w.rl.hdr = (int *)c;
+    w.rl.cap = kRefinePerMap * nmaps;
+    c += 256;
+    w.rl.items = (int4 *)c;
+    c += up256(sizeof(int4) * (size_t)w.rl.cap);
+    w.end = c;
+    return w;
+}
+size_t fast_ws_bytes(const glg_plan *P, int nmaps) {
+    char base[1];
+    return (size_t)(fast_ws(P, nmaps, base).end - base);
+}
+}  // namespace
+
 extern "C" size_t glg_alm2map_workspace(const glg_plan *P, int nmaps, int form) {
     if (!P || nmaps <= 0) return 0;
-    if (form == GLG_FORM_FAST)  // status | B pack | F [map][m][ring] | F [map][ring][m]
-        return GLG_WS_STATUS_BYTES + fast_pack_bytes(P, nmaps) +
-               2 * sizeof(float2) * (size_t)nmaps * P->nrings * (P->mmax + 1);
+    if (form == GLG_FORM_FAST) return fast_ws_bytes(P, nmaps);
     return ring_coef_bytes(P, nmaps);
 }
 
@@ -49,16 +87,16 @@ extern "C" int glg_alm2map(const glg_plan *P, const void *alm, int nmaps, int fo
         GLG_REQUIRE(nmaps <= 40, "glg_alm2map: the fast form takes at most 40 maps per call");
         int rc = glg_plan_prepare_fast(const_cast<glg_plan *>(P), st);
         if (rc) return rc;
-        int *err = (int *)ws;
-        float *bpack = (float *)((char *)ws + GLG_WS_STATUS_BYTES);
-        float2 *F = (float2 *)((char *)ws + GLG_WS_STATUS_BYTES + fast_pack_bytes(P, nmaps));
-        cudaError_t e = cudaMemsetAsync(err, 0, GLG_WS_STATUS_BYTES, st);
+        const FastWs w = fast_ws(P, nmaps, ws);
+        cudaError_t e = cudaMemsetAsync(w.err, 0, GLG_WS_STATUS_BYTES, st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(w.rl.hdr, 0, 256, st);
         if (e != cudaSuccess) return glg_cuda_status(e, "glg_alm2map: status reset");
-        float2 *Ft = F + (size_t)nmaps * P->nrings * (P->mmax + 1);
         const glg_tile_run all{0, (P->npairs + 127) / 128, 0, true};
-        rc = glg_launch_leg_tc(P, (const float2 *)alm, nmaps, bpack, F, err, all, st);
+        rc = glg_launch_leg_tc(P, (const float2 *)alm, nmaps, w.bpack, w.F, w.err, all, st);
         if (rc) return rc;
-        return glg_launch_ring_syn_f32(P, F, Ft, nmaps, (float *)maps, epi, st);
+        rc = glg_launch_ring_syn_f32(P, w.F, w.Ft, nmaps, (float *)maps, epi, &w.rl, st);
+        if (rc) return rc;
+        return glg_launch_refine(P, w.Ft, nmaps, (float *)maps, epi, w.rl, st);
     }
     double2 *F = (double2 *)ws;
     int rc = glg_launch_leg_syn(P, (const double2 *)alm, nmaps, F, st);
@@ -142,12 +180,13 @@ extern "C" int glg_alm2map_host(const glg_plan *P, const void *alm, int nmaps, v
     cudaStream_t st = (cudaStream_t)stream;
     int rc = glg_plan_prepare_fast(const_cast<glg_plan *>(P), st);
     if (rc) return rc;
-    int *err = (int *)ws;
-    float *bpack = (float *)((char *)ws + GLG_WS_STATUS_BYTES);
-    float2 *F = (float2 *)((char *)ws + GLG_WS_STATUS_BYTES + fast_pack_bytes(P, nmaps));
-    float2 *Ft = F + (size_t)nmaps * P->nrings * (P->mmax + 1);
-    float *stage = (float *)(Ft + (size_t)nmaps * P->nrings * (P->mmax + 1));
+    const FastWs w = fast_ws(P, nmaps, ws);
+    int *err = w.err;
+    float *bpack = w.bpack;
+    float2 *F = w.F, *Ft = w.Ft;
+    float *stage = (float *)w.end;
     cudaError_t e = cudaMemsetAsync(err, 0, GLG_WS_STATUS_BYTES, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(w.rl.hdr, 0, 256, st);
     if (e != cudaSuccess) return glg_cuda_status(e, "glg_alm2map_host: status reset");
 
     // Ring tiles in runs from the equator to the poles: each run's maps go to
@@ -172,7 +211,8 @@ extern "C" int glg_alm2map_host(const glg_plan *P, const void *alm, int nmaps, v
         const HostRun r = host_run(P->nside, k);
         const glg_tile_run run{r.t0, r.t1 - r.t0, k, k == 0};
         rc = glg_launch_leg_tc(P, (const float2 *)alm, nmaps, bpack, F, err, run, st);
-        if (!rc) rc = glg_launch_ring_syn_f32_range(P, F, Ft, nmaps, stage, epi, r.p0, r.p1, st);
+        if (!rc) rc = glg_launch_ring_syn_f32_range(P, F, Ft, nmaps, stage, epi, r.p0, r.p1, &w.rl, st);
+        if (!rc) rc = glg_launch_refine(P, Ft, nmaps, stage, epi, w.rl, st);  // this run's listed pixels
         if (!rc && (e = cudaEventRecord(ev[k], st)) != cudaSuccess) rc = glg_cuda_status(e, "glg_alm2map_host: event");
         if (!rc) ++started;
     }
@@ -292,7 +332,7 @@ extern "C" int glg_autotune_fast(glg_plan *P, int nmaps, void *maps, void *ws, s
     int rc = glg_plan_prepare_fast(P, st);
     if (rc) return rc;
     const size_t fbytes = sizeof(float2) * (size_t)nmaps * P->nrings * (P->mmax + 1);
-    float2 *Ft = (float2 *)((char *)ws + GLG_WS_STATUS_BYTES + fast_pack_bytes(P, nmaps) + fbytes);
+    float2 *Ft = fast_ws(P, nmaps, ws).Ft;
     cudaError_t e = cudaMemsetAsync(Ft, 0, fbytes, st);
     if (e != cudaSuccess) return glg_cuda_status(e, "glg_autotune_fast");
     cudaEvent_t a, b;

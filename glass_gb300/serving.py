@@ -19,6 +19,7 @@ from __future__ import annotations
 
 import collections
 import dataclasses
+import os
 import threading
 import time
 
@@ -99,9 +100,20 @@ def launch_bytes(nside: int, lmax: int, nmaps: int, form: str = "fast") -> int:
     npix = 12 * nside * nside
     if form == "fast":
         nn = ((2 * nmaps + 15) // 16) * 16
-        ws = 256 + _ngroups(lmax) * 128 * nn + 2 * 8 * nmaps * nrings * n
+        up = lambda b: (b + 255) // 256 * 256  # noqa: E731 - 256-byte aligned blocks
+        ws = (256 + up(_ngroups(lmax) * 128 * nn) + 2 * up(8 * nmaps * nrings * n) + 256
+              + up(16 * 65536 * nmaps))  # + tail-refinement list
         return ws + nmaps * (8 * nalm + 4 * npix)
     return 16 * nmaps * nrings * n + nmaps * (16 * nalm + 8 * npix)
+
+
+PLM_TABLE_BUDGET = int(os.environ.get("GLASS_GB300_PLM_TABLE_BYTES", str(160 << 30)))
+
+
+def plm_table_bytes(nside: int, lmax: int) -> int:
+    """Bytes of a plan's P_lm table (FP32 lambda per (l, m, ring pair),
+    in 8 KB tiles of 16 l x 128 ring pairs)."""
+    return 8192 * _ngroups(lmax) * ((2 * nside + 127) // 128)
 
 
 def plan_bytes(nside: int, lmax: int, fast: bool = True) -> int:
@@ -118,7 +130,9 @@ def plan_bytes(nside: int, lmax: int, fast: bool = True) -> int:
          + 16 * ntw)
     if fast:
         tiles = (npairs + 127) // 128
-        b += (8 * npairs + 8 * ntw + 16 * (nalm + 16) + 8 * (n + 1) + 8 * _ngroups(lmax) * tiles * 128
+        plm = plm_table_bytes(nside, lmax)
+        lam = plm if plm <= PLM_TABLE_BUDGET else 8 * _ngroups(lmax) * tiles * 128  # table or seeds
+        b += (8 * npairs + 8 * ntw + 16 * (nalm + 16) + 8 * (n + 1) + lam
               + 4 * n * npairs + 4 * n * tiles)
         b += (4 * npairs + 8 * (nside + 2) + 2 * ntw + 20 * (nside + 1) + 8 * 8 * ntw + 8 * ntw
               + 8 * (16 * nside + 1))

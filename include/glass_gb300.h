@@ -62,6 +62,20 @@ const char *glg_last_error(void);
 int glg_plan_create(int nside, int lmax, void *stream, glg_plan **plan);
 void glg_plan_destroy(glg_plan *plan);
 size_t glg_plan_device_bytes(const glg_plan *plan);
+/*
+ * The fast form's Legendre values P_lm: when the first fast transform of a
+ * plan builds its tables, it keeps every lambda_lm(x_ring) resident in
+ * device memory as FP32 (the FP64 recurrence rounded once; 4 bytes per
+ * (l, m, ring pair), 138 GB at nside 2048 / lmax 4096) if that fits
+ * `bytes` (default 160 GiB) and the free device memory with 4 GiB to spare;
+ * otherwise the contraction recomputes lambda in FP32 from FP64 seeds every
+ * 16 l (less accurate: about 3e-7 instead of 1.4e-7 relative RMS of the
+ * Legendre sums).  No counterpart in the reference (healpy recomputes the
+ * Legendre functions in every transform).  glg_plan_has_plm_table: 1 once
+ * the plan's fast tables hold the P_lm table, else 0.
+ */
+int glg_set_plm_table_budget(size_t bytes);
+int glg_plan_has_plm_table(const glg_plan *plan);
 int glg_plan_info(const glg_plan *plan, int *nside, int *lmax, int *nrings, int64_t *npix,
                   int64_t *nalm);
 

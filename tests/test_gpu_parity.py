@@ -323,6 +323,28 @@ def test_alm2map_fast_vs_oracle(g, nside, lmax, nmaps):
     assert rel_err(got, ref) < 2e-5
 
 
+def test_alm2map_fast_table_and_recurrence_paths(g):
+    """The fast form with the resident P_lm table (default) and, with the
+    table budget at 0, with lambda from the FP32 recurrence and its seeds."""
+    from glass_gb300 import _lib
+
+    lib = _lib.lib()
+    cases = [(32, 64, 3), (64, 128, 8), (32, 300, 2)]
+    for budget, table in ((160 << 30, True), (0, False)):
+        lib.glg_set_plm_table_budget(budget)
+        _lib.clear_plans()
+        try:
+            for nside, lmax, nmaps in cases:
+                ell = np.concatenate([np.arange(m, lmax + 1) for m in range(lmax + 1)])
+                alm = random_alm(lmax, seed=8, nmaps=nmaps) * (ell + 1.0) ** -0.65
+                got = _fast_synth(alm, nside, lmax)
+                assert _lib.get_plan(nside, lmax).has_plm_table == table
+                assert rel_rms(got, osht.alm2map(alm, nside, lmax)) < FAST_RMS
+        finally:
+            lib.glg_set_plm_table_budget(160 << 30)
+            _lib.clear_plans()
+
+
 def test_generate_fast_vs_plain(g):
     """Same Philox stream: fast form within 1e-6 RMS of the FP64 plain form."""
     gls, lam = spectra_cfg2(6, 128, seed=1)

@@ -133,3 +133,32 @@ def test_cls_files_interchange_with_reference(tmp_path):
         for k in theirs.files:
             np.testing.assert_array_equal(mine[k], theirs[k])
             assert mine[k].dtype == theirs[k].dtype
+
+
+def test_fft_radix_constants_exact():
+    """The FP32 ring FFT's radix constants, written as (hi, lo) float pairs in
+    glass_gb300/csrc/ringfft32.cu: hi the nearest float of the exact value and
+    hi + lo within 1e-15 of it (products with them round once)."""
+    import re
+    from pathlib import Path
+
+    src = (Path(__file__).resolve().parent.parent / "glass_gb300" / "csrc" / "ringfft32.cu").read_text()
+
+    def table(name):
+        body = re.search(name + r"\[\] = \{(.*?)\n\};", src, re.S).group(1)
+        vals = [float(v) for v in re.findall(r"(-?[0-9.]+(?:e-?[0-9]+)?)f", body)]
+        return np.asarray(vals, dtype=np.float32).astype(np.float64).reshape(-1, 2)
+
+    hi, lo = table("kOddHi"), table("kOddLo")
+    k = 0
+    for r in (3, 5, 7, 11, 13):
+        for j in range(r):
+            ex = np.array([np.cos(2 * np.pi * j / r), np.sin(2 * np.pi * j / r)])
+            assert np.all(hi[k] == ex.astype(np.float32))
+            assert np.all(np.abs(hi[k] + lo[k] - ex) < 1e-15)
+            k += 1
+    assert k == hi.shape[0]
+    for name, val in (("R2", np.sqrt(0.5)), ("C8", np.cos(np.pi / 8)), ("S8", np.sin(np.pi / 8))):
+        h = np.float32(val)
+        lval = float(np.float32(re.search(name + r"L = (-?[0-9.]+(?:e-?[0-9]+)?)f", src).group(1)))
+        assert abs(float(h) + lval - val) < 1e-15
