@@ -200,6 +200,76 @@ def run_cfg2(steps: int = 3) -> dict:
     return out
 
 
+def run_cfg5(nshell: int = 60, nside: int = 4096, lmax: int = 8192) -> dict:
+    """Config 5: 60 lognormal shells at nside 4096 / lmax 8192 (config-3
+    spectra, seed 5) streamed through the fast form in groups of shells (as
+    many as a 48 GB workspace allows), each shell consumed as it comes: its
+    lognormal map added into the cumulative convergence (mean of the shells)
+    and, for the first two, Poisson galaxy counts (5 per pixel) drawn from it
+    as float32 and as float64 -- the counts must agree bit for bit, whichever
+    form produced the delta values.  Then the spin-2 shear of the cumulative
+    convergence (from_convergence, lmax 8192, FP64 form).  Device-resident;
+    the nside-2048 plans are dropped first (their P_lm table would not leave
+    room for this plan's 137 GB seed table)."""
+    import torch
+
+    import glass_gb300 as g
+    from glass_gb300 import _lib
+
+    _lib.clear_plans()
+    torch.cuda.empty_cache()
+    gls_np, lam = spectra_cfg3(nshell, lmax, seed=5)
+    gls = [torch.as_tensor(c, device="cuda") for c in gls_np]
+    fields = [g.grf.Lognormal(float(x)) for x in lam]
+    npix = 12 * nside * nside
+    out = {"workload": f"{nshell}-shell lognormal field generation streamed in groups, nside {nside}, lmax {lmax}",
+           "nshell": nshell, "nside": nside, "lmax": lmax}
+    a = time.perf_counter()
+    next(iter(g.generate(fields[:1], gls[:1], nside, rng=g.rng.Generator(1), form="fast")))
+    torch.cuda.synchronize()
+    out["setup_s"] = time.perf_counter() - a  # plan, seeds, FFT tables, autotuning
+    plan = _lib.get_plan(nside, lmax)
+    out["plm_table"] = plan.has_plm_table
+    out["plan_gb"] = plan.bytes / 1e9
+    ngal = 5.0 * npix / g.points.ARCMIN2_SPHERE
+    kappa = torch.zeros(npix, dtype=torch.float64, device="cuda")
+    same, stream = [], torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    t_counts = 0.0
+    for t, m in enumerate(g.generate(fields, gls, nside, rng=g.rng.Generator(42), form="fast")):
+        kappa.add_(m, alpha=1.0 / nshell)
+        if t < 2:
+            c0 = torch.cuda.Event(enable_timing=True)
+            c1 = torch.cuda.Event(enable_timing=True)
+            c0.record(stream)
+            n32 = g.points.counts_from_delta(ngal, m, rng=g.rng.Generator(7 + t))
+            c1.record(stream)
+            n64 = g.points.counts_from_delta(ngal, m.double(), rng=g.rng.Generator(7 + t))
+            torch.cuda.synchronize()
+            t_counts += c0.elapsed_time(c1)
+            same.append(bool(torch.equal(n32, n64)))
+            del n32, n64
+        del m
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) - t_counts
+    out["fast"] = {"ms": ms, "shell_maps_per_s": nshell / (ms / 1e3), "pixels_per_s": nshell * npix / (ms / 1e3),
+                   "note": "includes the FP64 counts of two shells' float64 copies"}
+    out["counts"] = {"bit_exact_f32_vs_f64_delta": all(same), "pixels_per_s": npix / (t_counts / 2 / 1e3),
+                     "mean_per_pixel": 5.0}
+    a = time.perf_counter()
+    (gamma,) = g.from_convergence(kappa, lmax=lmax, shear=True)
+    torch.cuda.synchronize()
+    out["shear"] = {"s": time.perf_counter() - a, "form": "plain FP64 (map2alm iter 3 + spin-2 synthesis)",
+                    "lmax": lmax, "discretized": True, "finite": bool(torch.isfinite(gamma).all())}
+    del gamma, kappa
+    _lib.clear_plans()
+    torch.cuda.empty_cache()
+    return out
+
+
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled during the timed region."""
 
@@ -398,10 +468,14 @@ def run_ours(args, rank: int, world: int) -> dict | None:
     peak_tf, peak_note = tf32_peak_tflops(peaks)
     achieved = flops / (leg_ms / max(leg_n, 1) / 1e3) / 1e12 if leg_ms > 0 else None
     # DRAM bytes of one full-size k_leg_tc launch (40 maps, nside 2048, lmax
-    # 4096) from ncu: dram__bytes_read.sum 17.68e9 + dram__bytes_write.sum
-    # 10.71e9, one-pass capture of the second launch of
-    # `bench.py --steps 1 --warmup 1 --plain-steps 0 --e2e-steps 0 ...`
-    traffic = 17.684237568e9 + 10.706691328e9 if (nshell, nside, lmax) == (40, 2048, 4096) else None
+    # 4096, P_lm table path), scaled from the ncu capture of the same launch
+    # at nside 512 / lmax 1024 (bench.py --ncu-case leg: 2.052 GB read, 0.644
+    # GB written) by the table size (138.0 / 2.20 GB) for the reads and by
+    # the Legendre sums' size (10.74 / 0.671 GB) for the writes
+    # (profiles/leg_tc_plm_40maps_nside512.md)
+    table = g.healpix.get_plan(nside, lmax).has_plm_table
+    traffic = (2.052e9 * 138.0 / 2.20 + 0.644e9 * 10.74 / 0.671) if table and (nshell, nside, lmax) == (
+        40, 2048, 4096) else None
     roofline = {"bound": "tensor", "kernel": "k_leg_tc", "achieved": achieved, "peak": peak_tf,
                 "unit": "TFLOP/s", "frac": (achieved / peak_tf) if achieved else None,
                 "traffic": traffic, "traffic_unit": "bytes per launch", "peak_note": peak_note, "passes": PASSES,
@@ -410,6 +484,10 @@ def run_ours(args, rank: int, world: int) -> dict | None:
     # the same figure against the measured bf16 GEMM rate halved (the
     # tensor pipe's tf32 rate is half its bf16 rate)
     bf_half = peaks.get("bf16_tflops", 1900.0) / 2.0
+    if traffic:  # the same launch against the measured copy bandwidth
+        gbs = traffic / (leg_ms / max(leg_n, 1) / 1e3) / 1e9
+        roofline["hbm"] = {"achieved": gbs, "peak": peaks.get("hbm_gbs", 6800.0), "unit": "GB/s",
+                           "frac": gbs / peaks.get("hbm_gbs", 6800.0), "traffic_note": "scaled from nside 512"}
     roofline["vs_bf16_half"] = {"peak": bf_half, "frac": (achieved / bf_half) if achieved else None,
                                 "issued_frac": (PASSES * achieved / bf_half) if achieved else None,
                                 "note": "of measured" if "fallback" not in peaks else "of fallback"}
@@ -436,6 +514,7 @@ def run_ours(args, rank: int, world: int) -> dict | None:
                  "shell_variances": [float(v) for v in shell_variances],
                  "speedup": (nshell / plain_s) and value / (nshell / plain_s)}
         del pm, fm
+        torch.cuda.empty_cache()  # the FP64 form's buffers: room for the host-output workspace
 
     # galaxy counts and positions on the benchmark's fast maps (n = 5 per
     # pixel on average): Poisson counts of 4 shells, positions of one
@@ -475,17 +554,26 @@ def run_ours(args, rank: int, world: int) -> dict | None:
         del maps
         torch.cuda.synchronize()
         a = time.perf_counter()
+        calls = []
         for _ in range(args.e2e_steps):
+            c = time.perf_counter()
             maps = list(g.generate(fields, gls_np, nside, rng=g.rng.Generator(42), form="fast"))
             del maps
+            calls.append((time.perf_counter() - c) * 1e3)
         torch.cuda.synchronize()
         e_s = (time.perf_counter() - a) / args.e2e_steps
-        e2e = {"value": nshell / e_s, "unit": UNIT, "ms_per_step": e_s * 1e3,
+        e2e = {"value": nshell / e_s, "unit": UNIT, "ms_per_step": e_s * 1e3, "ms_per_call": calls,
                "h2d_bytes_per_step": int(sum(c.nbytes for c in gls_np)),
                "d2h_bytes_per_step": d2h}
 
     serving = run_serving(args) if (args.serving > 0 or args.serving_plain > 0) else None
     cfg2 = run_cfg2() if args.cfg2 else None
+    cfg5 = None
+    if args.cfg5:
+        try:
+            cfg5 = run_cfg5()
+        except Exception as exc:  # noqa: BLE001 - recorded, the headline stands
+            cfg5 = {"error": f"{type(exc).__name__}: {exc}"}
     cpu = cpu_baseline(args) if args.cpu_baseline else None
     res = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -497,7 +585,7 @@ def run_ours(args, rank: int, world: int) -> dict | None:
         "pixels_per_sec": value * npix, "e2e": e2e, "plain_fp64": plain, "roofline": roofline, "points": points,
         "kernel_ms_per_step": {k: v[0] for k, v in kt.items()},
         "kernel_launches_per_step": {k: v[1] for k, v in kt.items()}, "gpu_launches": launches,
-        "clocks": clk.summary(), "cpu_baseline": cpu, "serving": serving, "cfg2": cfg2,
+        "clocks": clk.summary(), "cpu_baseline": cpu, "serving": serving, "cfg2": cfg2, "cfg5": cfg5,
     }
     return res
 
@@ -550,10 +638,27 @@ def ncu_case(which: str) -> None:
     lognormal shells of the serving spectra at nside 1024, lmax 2048 (the
     Legendre sums, 0.54 GB, exceed L2); profilers capture the first call.
     "alm": the correlated alm of the benchmark's 40 shells at lmax 4096 in the
-    fast form (2.7 GB written, no transform), twice."""
+    fast form (2.7 GB written, no transform), twice.  "leg": two fast
+    syntheses of 40 maps at nside 512, lmax 1024 (the contraction's P_lm
+    table 2.2 GB and its Legendre sums 0.67 GB exceed L2; about 4 GB on the
+    device)."""
     import torch
 
     import glass_gb300 as g
+
+    if which == "leg":
+        from glass_gb300 import healpix as hp
+
+        lmax = 1024
+        rng = np.random.default_rng(5)
+        n = (lmax + 1) * (lmax + 2) // 2
+        alm = torch.as_tensor(rng.standard_normal((40, n)) + 1j * rng.standard_normal((40, n)),
+                              dtype=torch.complex64, device="cuda")
+        for _ in range(2):
+            maps = hp.synth(alm, 512, lmax, form="fast")
+            torch.cuda.synchronize()
+        print("ncu case done", float(maps.abs().max()))
+        return
 
     if which == "alm":
         from glass_gb300 import fields
@@ -592,9 +697,11 @@ def main() -> None:
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--no-cfg2", dest="cfg2", action="store_false",
                     help="skip the config-2 record (10 shells, nside 512)")
+    ap.add_argument("--no-cfg5", dest="cfg5", action="store_false",
+                    help="skip the config-5 record (60 shells, nside 4096, streamed)")
     ap.add_argument("--no-points", dest="points", action="store_false",
                     help="skip the galaxy counts / positions aside")
-    ap.add_argument("--ncu-case", nargs="?", const="sht", choices=["sht", "alm"],
+    ap.add_argument("--ncu-case", nargs="?", const="sht", choices=["sht", "alm", "leg"],
                     help="run a small profiling case and exit")
     ap.add_argument("--peaks", action="store_true", help="measure the TF32 / FP32 / FP64 peak rates and exit")
     args = ap.parse_args()

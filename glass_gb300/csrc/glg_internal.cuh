@@ -121,6 +121,7 @@ struct glg_plan {
     float2 *chirp;           // exp(i pi k^2 / n), k < n, per Bluestein length
     int blu_Mmax;
     float2 *twM;             // [blu_Mmax / 2 + 1] exp(2 pi i t / blu_Mmax)
+    float2 *twMp;            // the same, padded (twMp[glg_zi(t)]), when blu_Mmax > 16384 (class 3)
 };
 
 // Radix passes of an FP32 ring FFT of length n (DIF order: 16s, then one 8,
@@ -177,9 +178,12 @@ int glg_launch_leg_syn(const glg_plan *P, const double2 *alm, int nmaps, double2
                        cudaStream_t st);
 int glg_launch_leg_syn_spin(const glg_plan *P, const double2 *elm, const double2 *blm, int spin,
                             double2 *F, cudaStream_t st);
+// FP64 ring FFTs; gbuf: glg_ring64_gbuf_bytes(P) bytes of device memory for
+// rings too long for shared memory (nside > 2048), else unused (may be null).
+size_t glg_ring64_gbuf_bytes(const glg_plan *P);
 int glg_launch_ring_syn(const glg_plan *P, const double2 *F, int nmaps, double *maps,
-                        const glg_epilogue *epi, cudaStream_t st);
-int glg_launch_ring_ana(const glg_plan *P, const double *maps, int nmaps, double2 *G,
+                        const glg_epilogue *epi, void *gbuf, cudaStream_t st);
+int glg_launch_ring_ana(const glg_plan *P, const double *maps, int nmaps, double2 *G, void *gbuf,
                         cudaStream_t st);
 int glg_launch_leg_ana(const glg_plan *P, const double2 *G, int nmaps, double2 *alm, int accumulate,
                        cudaStream_t st);
@@ -190,7 +194,12 @@ struct glg_refine_list {
     int *hdr;
     int cap;
     int4 *items;
+    float2 *gz;  // nside > 2048: the global transform buffers of Bluestein class 3
 };
+// Class-3 buffers: GLG_RING_GSLOTS slices of glg_zsize(Mmax) complex values.
+#define GLG_RING_GSLOTS 304
+// Bytes of the class-3 buffers for a plan of this nside (0 when nside <= 2048).
+size_t glg_ring_gz_bytes(int nside);
 int glg_launch_ring_syn_f32(const glg_plan *P, const float2 *F, float2 *Ft, int nmaps, float *maps,
                             const glg_epilogue *epi, const glg_refine_list *rl, cudaStream_t st);
 // FP64 recomputation of the listed pixels (no launch when no map of the call
@@ -201,7 +210,7 @@ int glg_launch_refine(const glg_plan *P, const float2 *Ft, int nmaps, float *map
 // One size bucket of the FP32 ring FFTs from transposed sums Ft, with
 // `threads` per block (0: the bucket's own), no epilogue (autotuning).
 int glg_launch_ring_bucket_f32(const glg_plan *P, int bucket, int threads, const float2 *Ft, int nmaps,
-                               float *maps, cudaStream_t st);
+                               float *maps, float2 *gz, cudaStream_t st);
 size_t glg_leg_tc_pack_bytes(const glg_plan *P, int nmaps);
 // Ring tiles (128 ring pairs each) of one tensor-core contraction launch, the
 // unit counter it draws from (slot in the status block) and whether the B

@@ -60,7 +60,6 @@ namespace {
 
 constexpr int CH = 3;             // groups per chunk = producer warp sets
 constexpr int NSEED = 16;         // slots of the seed / coefficient ring (groups)
-constexpr int NPLM = 6;           // slots of the P_lm tile ring (groups), table path
 constexpr int NU = 8;             // slots of the unit ring
 constexpr int NCONSUMERS = 19;    // warps that read the unit ring (all but the seed streamer)
 constexpr int TMEM_COLS = 512;
@@ -149,11 +148,22 @@ __device__ __forceinline__ int unit_m(int64_t mi, int lmax) {
 // B chunk slots in shared memory: as many as fit beside the accumulators and
 // the seed ring (up to 6), so the alm of a chunk are requested several chunks
 // before the MMAs that read them.
+// Recurrence path: as many B chunk slots as fit beside the accumulators and
+// the seed ring (up to 6).  Table path: 2 B chunk slots for wide N (their
+// tiles mostly come from L2, where the ring tiles of one m share them) and
+// the room left to P_lm tile slots, up to 12 (8 KB each): the tiles come
+// from HBM, and the copies in flight per SM bound the bandwidth.
 template <int N, bool T>
 constexpr int nbc_slots() {
-    constexpr int ring = T ? NPLM * GLG_PLM_TILE_BYTES : NSEED * 1280;
-    constexpr int room = (226 * 1024 - 512 * (2 * N + 4) - ring - 1024) / (CH * 128 * N);
+    if constexpr (T) return N <= 32 ? 4 : 2;
+    constexpr int room = (226 * 1024 - 512 * (2 * N + 4) - NSEED * 1280 - 1024) / (CH * 128 * N);
     return room > 6 ? 6 : room;
+}
+template <int N>
+constexpr int plm_slots() {
+    constexpr int room = (226 * 1024 - 512 * (2 * N + 4) - nbc_slots<N, true>() * CH * 128 * N - 1024) /
+                         GLG_PLM_TILE_BYTES;
+    return room > 12 ? 12 : room;
 }
 
 struct SeedSlot {
@@ -170,7 +180,8 @@ template <int N, bool T>
 struct Smem {
     static constexpr uint32_t BBYTES = 128 * N;  // one group: 4 tiles of N x 8 tf32
     static constexpr int NBC = nbc_slots<N, T>();
-    static constexpr int NS = T ? NPLM : NSEED;  // group slots of the lambda source
+    static constexpr int NS = T ? plm_slots<N>() : NSEED;  // group slots of the lambda source
+    static_assert(!T || NS >= 2 * CH, "P_lm slots for two chunks");
     static_assert(NBC >= 2, "at least two B chunk slots");
     struct BSlot {
         unsigned char b[CH * BBYTES];

@@ -14,6 +14,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "glg_internal.cuh"
@@ -231,7 +232,7 @@ extern "C" void glg_plan_destroy(glg_plan *P) {
                     P->fft_nst, P->tw_ofs,  P->tw,      P->cth32,  P->tw32,   P->coef32,
                     P->goff,  P->seeds,     P->lstart,  P->tfirst, P->bucket_pairs, P->chirp_ofs,
                     P->chirp, P->pos_ofs, P->pos16,   P->blu_ofs, P->blu_M,  P->blu_H,  P->twM,
-                    P->plm};
+                    P->plm,   P->twMp};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     delete[] P->bucket_pairs_host;
@@ -458,6 +459,7 @@ __global__ void k_plan_tfirst(int lmax, int npairs, int ntiles, const int *__res
 // H = DFT_M(h), h_t = e^{-i pi t^2 / n} for |t| < n (indices mod M), stored
 // in the DIF output order of M.
 size_t glg_ring32_smem(int kind, int n_or_M, int threads, bool fold) {
+    if (kind == 3) return 2 * (size_t)threads * sizeof(float2);  // the buffer is in global memory
     const size_t zs = (size_t)glg_zsize(n_or_M);
     size_t slots = zs + 2 * (size_t)threads + glg_zi(n_or_M / 2) + 1;
     if (kind != 1 && fold) slots += zs;
@@ -492,9 +494,11 @@ static int build_fft32_tables(glg_plan *P, cudaStream_t st) {
         for (int k = 0; k < 4 * i; ++k) pos16[pos_ofs[i] + k] = (uint16_t)dif_pos_host(r, ns, 4 * i, k);
     }
     std::vector<float2> H((size_t)(nblu > 0 ? nblu : 1)), chirp((size_t)(nchirp > 0 ? nchirp : 1));
-    for (int i = 1; i <= nside; ++i) {
+    // chirps and chirp spectra of every Bluestein length, ring lengths dealt
+    // out to the host's threads (each writes its own table ranges)
+    auto chirp_tables = [&](int i) {
         const int M = blu_M[i];
-        if (!M) continue;
+        if (!M) return;
         const int n = 4 * i;
         std::vector<std::complex<double>> h(M, 0.0);
         for (int t = 0; t < n; ++t) {
@@ -510,10 +514,27 @@ static int build_fft32_tables(glg_plan *P, cudaStream_t st) {
             const int q = dif_pos_host(mr, mns, M, k);
             H[blu_ofs[i] + q] = make_float2((float)h[k].real(), (float)h[k].imag());
         }
+    };
+    {
+        const unsigned hw = std::thread::hardware_concurrency();
+        const int nth = nside < 256 ? 1 : (int)(hw > 0 ? (hw < 32 ? hw : 32) : 4);
+        std::atomic<int> next{1};
+        std::vector<std::thread> pool;
+        for (int t = 1; t < nth; ++t)
+            pool.emplace_back([&] {
+                for (int i = next++; i <= nside; i = next++) chirp_tables(i);
+            });
+        for (int i = next++; i <= nside; i = next++) chirp_tables(i);
+        for (auto &th : pool) th.join();
     }
     std::vector<float2> twM(Mmax / 2 + 1);
     for (int t = 0; t <= Mmax / 2; ++t)
         twM[t] = make_float2((float)cos(2.0 * M_PI * t / Mmax), (float)sin(2.0 * M_PI * t / Mmax));
+    std::vector<float2> twMp;  // padded copy for class 3 (read from global memory)
+    if (Mmax > 16384) {
+        twMp.assign((size_t)glg_zsize(Mmax / 2 + 1), make_float2(0.f, 0.f));
+        for (int t = 0; t <= Mmax / 2; ++t) twMp[glg_zi(t)] = twM[t];
+    }
 
     // buckets: Bluestein rings by M, mixed-radix rings by (next power of two
     // of n, power-of-two n or not, whether m folds onto the ring); largest
@@ -530,8 +551,8 @@ static int build_fft32_tables(glg_plan *P, cudaStream_t st) {
     for (int p = 0; p < P->npairs; ++p) {
         const int i = p + 1 < nside ? p + 1 : nside;
         const int n = 4 * i;
-        if (blu_M[i]) {
-            groups[{1, blu_M[i], 0}].push_back(p);
+        if (blu_M[i]) {  // class 3 when the transform buffer exceeds shared memory
+            groups[{blu_M[i] > 16384 ? 3 : 1, blu_M[i], 0}].push_back(p);
         } else {
             int nb = 1;
             while (nb < n) nb <<= 1;
@@ -562,6 +583,7 @@ static int build_fft32_tables(glg_plan *P, cudaStream_t st) {
         (rc = dalloc(P, &P->pos_ofs, pos_ofs.size())) || (rc = dalloc(P, &P->pos16, pos16.size())) ||
         (rc = dalloc(P, &P->blu_ofs, blu_ofs.size())) || (rc = dalloc(P, &P->blu_M, blu_M.size())) ||
         (rc = dalloc(P, &P->blu_H, H.size())) || (rc = dalloc(P, &P->twM, twM.size())) ||
+        (!twMp.empty() && (rc = dalloc(P, &P->twMp, twMp.size()))) ||
         (rc = dalloc(P, &P->chirp_ofs, chirp_ofs.size())) || (rc = dalloc(P, &P->chirp, chirp.size())))
         return rc;
     cudaError_t e = cudaSuccess;
@@ -578,6 +600,7 @@ static int build_fft32_tables(glg_plan *P, cudaStream_t st) {
     up(P->blu_M, blu_M.data(), sizeof(int) * blu_M.size());
     up(P->blu_H, H.data(), sizeof(float2) * H.size());
     up(P->twM, twM.data(), sizeof(float2) * twM.size());
+    if (!twMp.empty()) up(P->twMp, twMp.data(), sizeof(float2) * twMp.size());
     up(P->chirp_ofs, chirp_ofs.data(), sizeof(int64_t) * chirp_ofs.size());
     up(P->chirp, chirp.data(), sizeof(float2) * chirp.size());
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // host vectors go out of scope

@@ -196,23 +196,29 @@ struct FLayout {
     int64_t map, ring, m;
 };
 
-// grid (npairs, nmaps): F -> maps [nmaps][npix]
-template <typename R>
+// grid (npairs, nmaps): F -> maps [nmaps][npix].  GB: rings too long for
+// shared memory (nside > 2048 in FP64): a persistent grid over the items
+// (ring pair, map), each block's ring buffer a slice of gbuf (gstride
+// complex values per block; the slices of the blocks in flight stay in L2).
+template <typename R, bool GB>
 __global__ void __launch_bounds__(FFT_THREADS)
 k_ring_syn(const int nrings, const int mmax, const int *__restrict__ nph, const int *__restrict__ half,
            const int64_t *__restrict__ startN, const int64_t *__restrict__ startS,
            const int *__restrict__ fft_radix, const int *__restrict__ fft_nst,
            const int64_t *__restrict__ tw_ofs, const V2<R> *__restrict__ tw,
            const V2<R> *__restrict__ F, const FLayout fl, R *__restrict__ maps, const int64_t npix,
-           const int map0, const EpiArgs epi) {
+           const int map0, const EpiArgs epi, cplx<R> *gbuf, const int64_t gstride, const int nitems,
+           const int cnt) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int p = blockIdx.x;
-    const int map = map0 + blockIdx.y;
+    __shared__ int radix_s[GLG_MAX_FFT_STAGES];
+    for (int it = GB ? blockIdx.x : 0; it < (GB ? nitems : 1); it += (GB ? gridDim.x : 1)) {
+    const int p = GB ? it / cnt : blockIdx.x;
+    const int slot = GB ? it % cnt : blockIdx.y;
+    const int map = map0 + slot;
     const int n = nph[p];
     const int i4 = n / 4;
-    cplx<R> *Z = reinterpret_cast<cplx<R> *>(smem_raw);
+    cplx<R> *Z = GB ? gbuf + (int64_t)blockIdx.x * gstride : reinterpret_cast<cplx<R> *>(smem_raw);
     cplx<R> *scratch = Z + n;
-    __shared__ int radix_s[GLG_MAX_FFT_STAGES];
     if (threadIdx.x < GLG_MAX_FFT_STAGES)
         radix_s[threadIdx.x] = fft_radix[i4 * GLG_MAX_FFT_STAGES + threadIdx.x];
     RingCtx<R> c;
@@ -250,7 +256,6 @@ k_ring_syn(const int nrings, const int mmax, const int *__restrict__ nph, const 
     }
     __syncthreads();
     fft_dif<R>(Z, scratch, c);
-    const int slot = blockIdx.y;
     const double var = epi.var[slot], lam = epi.lam[slot];
     const int ekind = epi.kind[slot];
     R *mp = maps + (int64_t)map * npix;
@@ -259,24 +264,29 @@ k_ring_syn(const int nrings, const int mmax, const int *__restrict__ nph, const 
         mp[startN[p] + j] = apply_epi(v.x, ekind, var, lam);
         if (!equator) mp[startS[p] + j] = apply_epi(v.y, ekind, var, lam);
     }
+    __syncthreads();  // the buffer and the radix table are reused by the block's next item
+    }
 }
 
 // grid (npairs, nmaps): maps -> G [nmaps][nrings][mmax+1],
 // G_m = (4 pi / npix) e^{-i m phi0} sum_j f_j e^{-2 pi i m j / n}.
+template <bool GB>
 __global__ void __launch_bounds__(FFT_THREADS)
 k_ring_ana(const int nrings, const int mmax, const int *__restrict__ nph, const int *__restrict__ half,
            const int64_t *__restrict__ startN, const int64_t *__restrict__ startS,
            const int *__restrict__ fft_radix, const int *__restrict__ fft_nst,
            const int64_t *__restrict__ tw_ofs, const double2 *__restrict__ tw,
-           const double *__restrict__ maps, const int64_t npix, double2 *__restrict__ G) {
+           const double *__restrict__ maps, const int64_t npix, double2 *__restrict__ G,
+           cplx<double> *gbuf, const int64_t gstride, const int nitems, const int nmaps) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int p = blockIdx.x;
-    const int map = blockIdx.y;
+    __shared__ int radix_s[GLG_MAX_FFT_STAGES];
+    for (int it = GB ? blockIdx.x : 0; it < (GB ? nitems : 1); it += (GB ? gridDim.x : 1)) {
+    const int p = GB ? it / nmaps : blockIdx.x;
+    const int map = GB ? it % nmaps : blockIdx.y;
     const int n = nph[p];
     const int i4 = n / 4;
-    cplx<double> *Z = reinterpret_cast<cplx<double> *>(smem_raw);
+    cplx<double> *Z = GB ? gbuf + (int64_t)blockIdx.x * gstride : reinterpret_cast<cplx<double> *>(smem_raw);
     cplx<double> *scratch = Z + n;
-    __shared__ int radix_s[GLG_MAX_FFT_STAGES];
     if (threadIdx.x < GLG_MAX_FFT_STAGES)
         radix_s[threadIdx.x] = fft_radix[i4 * GLG_MAX_FFT_STAGES + threadIdx.x];
     RingCtx<double> c;
@@ -313,6 +323,8 @@ k_ring_ana(const int nrings, const int mmax, const int *__restrict__ nph, const 
         GN[m] = make_double2(w * sn.x, w * sn.y);
         if (!equator) GS[m] = make_double2(w * ss.x, w * ss.y);
     }
+    __syncthreads();  // the buffer and the radix table are reused by the block's next item
+    }
 }
 
 template <typename R>
@@ -321,15 +333,19 @@ size_t ring_smem_bytes(int nmax) {
     return sizeof(cplx<R>) * ((size_t)nmax + (size_t)nmax / 4 + 1);
 }
 
+constexpr int GB_SLOTS = 304;  // blocks of the persistent global-buffer grid
+
 template <typename R>
 int launch_ring_syn(const glg_plan *P, const V2<R> *tw, const V2<R> *F, FLayout fl, int nmaps,
-                    R *maps, const glg_epilogue *epi, cudaStream_t st) {
+                    R *maps, const glg_epilogue *epi, void *gbuf, cudaStream_t st) {
     const size_t smem = ring_smem_bytes<R>(4 * P->nside);
-    if (smem > 227 * 1024) {
-        glg_set_error("ring FFT: nside too large for the shared-memory FFT of this precision");
+    const bool gb = smem > 227 * 1024;
+    if (gb && !gbuf) {
+        glg_set_error("ring FFT: rings too long for shared memory and no global ring buffers given");
         return GLG_ERR_UNSUPPORTED;
     }
-    cudaFuncSetAttribute(k_ring_syn<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const int64_t gstride = (int64_t)(smem / sizeof(cplx<R>));
+    if (!gb) cudaFuncSetAttribute(k_ring_syn<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     for (int m0 = 0; m0 < nmaps; m0 += 8) {
         const int cnt = nmaps - m0 < 8 ? nmaps - m0 : 8;
         EpiArgs ea;
@@ -338,11 +354,18 @@ int launch_ring_syn(const glg_plan *P, const V2<R> *tw, const V2<R> *F, FLayout 
             ea.var[k] = (epi && epi->var && k < cnt) ? epi->var[m0 + k] : 0.0;
             ea.lam[k] = (epi && epi->lamda && k < cnt) ? epi->lamda[m0 + k] : 1.0;
         }
-        dim3 grid(P->npairs, cnt);
         GLG_LAUNCH_SCOPE("k_ring_syn", st);
-        k_ring_syn<R><<<grid, FFT_THREADS, smem, st>>>(P->nrings, P->mmax, P->nph, P->half, P->startN,
-                                                       P->startS, P->fft_radix, P->fft_nst, P->tw_ofs,
-                                                       tw, F, fl, maps, P->npix, m0, ea);
+        if (gb) {
+            const int nitems = P->npairs * cnt;
+            k_ring_syn<R, true><<<nitems < GB_SLOTS ? nitems : GB_SLOTS, FFT_THREADS, 0, st>>>(
+                P->nrings, P->mmax, P->nph, P->half, P->startN, P->startS, P->fft_radix, P->fft_nst, P->tw_ofs,
+                tw, F, fl, maps, P->npix, m0, ea, (cplx<R> *)gbuf, gstride, nitems, cnt);
+        } else {
+            dim3 grid(P->npairs, cnt);
+            k_ring_syn<R, false><<<grid, FFT_THREADS, smem, st>>>(
+                P->nrings, P->mmax, P->nph, P->half, P->startN, P->startS, P->fft_radix, P->fft_nst, P->tw_ofs,
+                tw, F, fl, maps, P->npix, m0, ea, nullptr, 0, 0, cnt);
+        }
         GLG_CHECK_LAUNCH("k_ring_syn");
     }
     return GLG_OK;
@@ -350,26 +373,39 @@ int launch_ring_syn(const glg_plan *P, const V2<R> *tw, const V2<R> *F, FLayout 
 
 }  // namespace
 
+size_t glg_ring64_gbuf_bytes(const glg_plan *P) {
+    const size_t smem = ring_smem_bytes<double>(4 * P->nside);
+    return smem > 227 * 1024 ? (size_t)GB_SLOTS * smem : 0;
+}
+
 int glg_launch_ring_syn(const glg_plan *P, const double2 *F, int nmaps, double *maps,
-                        const glg_epilogue *epi, cudaStream_t st) {
+                        const glg_epilogue *epi, void *gbuf, cudaStream_t st) {
     const FLayout fl{(int64_t)P->nrings * (P->mmax + 1), (int64_t)(P->mmax + 1), 1};
-    return launch_ring_syn<double>(P, P->tw, F, fl, nmaps, maps, epi, st);
+    return launch_ring_syn<double>(P, P->tw, F, fl, nmaps, maps, epi, gbuf, st);
 }
 
 
-int glg_launch_ring_ana(const glg_plan *P, const double *maps, int nmaps, double2 *G,
+int glg_launch_ring_ana(const glg_plan *P, const double *maps, int nmaps, double2 *G, void *gbuf,
                         cudaStream_t st) {
     const size_t smem = ring_smem_bytes<double>(4 * P->nside);
-    if (smem > 227 * 1024) {
-        glg_set_error("ring FFT: nside too large for the FP64 shared-memory FFT");
+    const bool gb = smem > 227 * 1024;
+    if (gb && !gbuf) {
+        glg_set_error("ring FFT: rings too long for shared memory and no global ring buffers given");
         return GLG_ERR_UNSUPPORTED;
     }
-    cudaFuncSetAttribute(k_ring_ana, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    dim3 grid(P->npairs, nmaps);
     GLG_LAUNCH_SCOPE("k_ring_ana", st);
-    k_ring_ana<<<grid, FFT_THREADS, smem, st>>>(P->nrings, P->mmax, P->nph, P->half, P->startN,
-                                               P->startS, P->fft_radix, P->fft_nst, P->tw_ofs,
-                                               P->tw, maps, P->npix, G);
+    if (gb) {
+        const int nitems = P->npairs * nmaps;
+        k_ring_ana<true><<<nitems < GB_SLOTS ? nitems : GB_SLOTS, FFT_THREADS, 0, st>>>(
+            P->nrings, P->mmax, P->nph, P->half, P->startN, P->startS, P->fft_radix, P->fft_nst, P->tw_ofs, P->tw,
+            maps, P->npix, G, (cplx<double> *)gbuf, (int64_t)(smem / sizeof(cplx<double>)), nitems, nmaps);
+    } else {
+        cudaFuncSetAttribute(k_ring_ana<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        dim3 grid(P->npairs, nmaps);
+        k_ring_ana<false><<<grid, FFT_THREADS, smem, st>>>(P->nrings, P->mmax, P->nph, P->half, P->startN,
+                                                          P->startS, P->fft_radix, P->fft_nst, P->tw_ofs,
+                                                          P->tw, maps, P->npix, G, nullptr, 0, 0, nmaps);
+    }
     GLG_CHECK_LAUNCH("k_ring_ana");
     return GLG_OK;
 }

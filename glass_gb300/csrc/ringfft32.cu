@@ -383,6 +383,8 @@ struct RingArgs {
     const int *blu_M;
     const float2 *blu_H, *chirp, *twM;
     int Mmax;
+    const float2 *twMp;  // padded twiddles of Mmax (class 3)
+    float2 *gz;          // global transform buffers of class 3, glg_zsize(Mmax) per block
     const float2 *Ft;  // [map][ring][m]
     float *maps;
     int64_t npix;
@@ -564,19 +566,13 @@ __global__ void __launch_bounds__(POW2 ? TMAX_POW2 : TMAX) k_ring32(const RingAr
     }
 }
 
-// Class 1: Bluestein.  smem: Z[M] (the south fold scratch sits at n..2n-1) |
-// X[2T] | wh[zi(M/2) + 1].
-__global__ void __launch_bounds__(TMAX_POW2) k_ring32_blu(const RingArgs a, const Epi32 e) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int map = blockIdx.x % a.nmaps;
-    const int p = a.pairs[blockIdx.x / a.nmaps];
+// Bluestein transform of ring pair p, map `map`, in buffer Z (shared or
+// global memory) with the padded twiddle table wh of its length M and the
+// partial-sum scratch X (2 x blockDim).  Ends with the stores.
+__device__ __forceinline__ void blu_ring(const RingArgs &a, const Epi32 &e, int map, int p, c32 *Z, c32 *X,
+                                         const c32 *wh) {
     const int n = a.nph[p], i4 = n / 4, T = blockDim.x;
     const int M = a.blu_M[i4];
-    c32 *Z = reinterpret_cast<c32 *>(smem_raw);
-    c32 *X = Z + glg_zsize(M);
-    c32 *wh = X + 2 * T;
-    const int stride = a.Mmax / M;
-    for (int t = threadIdx.x; t <= M / 2; t += T) wh[zi(t)] = ldg(a.twM + (int64_t)t * stride);
     const float2 *w2n = a.tw32 + a.tw_ofs[i4];
     const float2 *chirp = a.chirp + a.chirp_ofs[i4];  // e^{i pi k^2 / n}
     const int rn = p, rs = a.nrings - 1 - p;
@@ -622,6 +618,37 @@ __global__ void __launch_bounds__(TMAX_POW2) k_ring32_blu(const RingArgs a, cons
             *reinterpret_cast<float4 *>(mp + sS + 4 * q) =
                 make_float4(epi(v0.y, kind, hv, lam), epi(v1.y, kind, hv, lam), epi(v2.y, kind, hv, lam),
                             epi(v3.y, kind, hv, lam));
+    }
+}
+
+// Class 1: Bluestein.  smem: Z[M] (the south fold scratch sits at n..2n-1) |
+// X[2T] | wh[zi(M/2) + 1].
+__global__ void __launch_bounds__(TMAX_POW2) k_ring32_blu(const RingArgs a, const Epi32 e) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int map = blockIdx.x % a.nmaps;
+    const int p = a.pairs[blockIdx.x / a.nmaps];
+    const int M = a.blu_M[a.nph[p] / 4], T = blockDim.x;
+    c32 *Z = reinterpret_cast<c32 *>(smem_raw);
+    c32 *X = Z + glg_zsize(M);
+    c32 *wh = X + 2 * T;
+    const int stride = a.Mmax / M;
+    for (int t = threadIdx.x; t <= M / 2; t += T) wh[zi(t)] = ldg(a.twM + (int64_t)t * stride);
+    blu_ring(a, e, map, p, Z, X, wh);
+}
+
+// Class 3: Bluestein lengths too large for shared memory (M = 32768, the
+// polar rings of nside 4096 with a large prime factor): the same transform
+// with Z in a global slice per block of a persistent grid (the slices of
+// the blocks in flight, 2 per SM x 275 KB, stay in L2) and the padded
+// twiddles of M = Mmax from a global table; only X is in shared memory.
+__global__ void __launch_bounds__(TMAX_POW2) k_ring32_blug(const RingArgs a, const Epi32 e, int nitems) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    c32 *X = reinterpret_cast<c32 *>(smem_raw);
+    c32 *Z = reinterpret_cast<c32 *>(a.gz) + (int64_t)blockIdx.x * glg_zsize(a.Mmax);
+    const c32 *wh = reinterpret_cast<const c32 *>(a.twMp);
+    for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+        blu_ring(a, e, item % a.nmaps, a.pairs[item / a.nmaps], Z, X, wh);
+        __syncthreads();  // the buffer is reused by the block's next item
     }
 }
 
@@ -721,6 +748,8 @@ static void ring_args(const glg_plan *P, const float2 *Ft, int nmaps, float *map
     a.chirp = P->chirp;
     a.twM = P->twM;
     a.Mmax = P->blu_Mmax;
+    a.twMp = P->twMp;
+    a.gz = nullptr;
     a.Ft = Ft;
     a.maps = maps;
     a.npix = P->npix;
@@ -734,7 +763,17 @@ static int launch_bucket(const glg_plan *P, const glg_ring_bucket &B, int thread
     a.pairs = P->bucket_pairs + B.first + lo;
     const size_t smem = glg_ring32_smem(B.kind, B.size, threads, B.fold != 0);
     const unsigned grid = (unsigned)count * (unsigned)a.nmaps;
-    if (B.kind == 1) {
+    if (B.kind == 3) {
+        if (!a.gz || B.size != P->blu_Mmax) {
+            glg_set_error("fast ring FFT: no global transform buffers for the largest Bluestein length");
+            return GLG_ERR_UNSUPPORTED;
+        }
+        const unsigned g3 = grid < GLG_RING_GSLOTS ? grid : GLG_RING_GSLOTS;
+        cudaFuncSetAttribute(k_ring32_blug, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        GLG_LAUNCH_SCOPE("k_ring32_blug", st);
+        k_ring32_blug<<<g3, threads, smem, st>>>(a, e, (int)grid);
+        GLG_CHECK_LAUNCH("k_ring32_blug");
+    } else if (B.kind == 1) {
         cudaFuncSetAttribute(k_ring32_blu, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         GLG_LAUNCH_SCOPE("k_ring32_blu", st);
         k_ring32_blu<<<grid, threads, smem, st>>>(a, e);
@@ -828,7 +867,7 @@ int glg_launch_ring_syn_f32_range(const glg_plan *P, const float2 *F, float2 *Ft
     const int nm = P->mmax + 1, nr = P->nrings;
     for (int b = 0; b < P->nbuckets; ++b)
         if (P->buckets[b].smem > 227 * 1024) {
-            glg_set_error("fast ring FFT: ring length too large for shared memory (nside <= 2048)");
+            glg_set_error("fast ring FFT: ring length too large for shared memory (nside <= 4096)");
             return GLG_ERR_UNSUPPORTED;
         }
     // north rings p0 .. p1-1 and their south partners nr-p1 .. nr-1-p0 (the
@@ -849,6 +888,7 @@ int glg_launch_ring_syn_f32_range(const glg_plan *P, const float2 *F, float2 *Ft
     e.rcount = rl ? rl->hdr : nullptr;
     e.rcap = rl ? rl->cap : 0;
     e.ritems = rl ? rl->items : nullptr;
+    a.gz = rl ? rl->gz : nullptr;
     const bool whole = p0 == 0 && p1 == P->npairs;
     for (int b = 0; b < P->nbuckets; ++b) {
         const glg_ring_bucket &B = P->buckets[b];
@@ -864,8 +904,15 @@ int glg_launch_ring_syn_f32_range(const glg_plan *P, const float2 *F, float2 *Ft
     return GLG_OK;
 }
 
+size_t glg_ring_gz_bytes(int nside) {
+    if (nside <= 2048) return 0;
+    int M = 1;
+    while (M < 8 * nside - 1) M <<= 1;
+    return sizeof(float2) * (size_t)GLG_RING_GSLOTS * glg_zsize(M);
+}
+
 int glg_launch_ring_bucket_f32(const glg_plan *P, int bucket, int threads, const float2 *Ft, int nmaps,
-                               float *maps, cudaStream_t st) {
+                               float *maps, float2 *gz, cudaStream_t st) {
     const glg_ring_bucket &B = P->buckets[bucket];
     if (glg_ring32_smem(B.kind, B.size, threads, B.fold != 0) > 227 * 1024) {
         glg_set_error("fast ring FFT: block size does not fit shared memory");
@@ -873,6 +920,7 @@ int glg_launch_ring_bucket_f32(const glg_plan *P, int bucket, int threads, const
     }
     RingArgs a;
     ring_args(P, Ft, nmaps, maps, a);
+    a.gz = gz;
     Epi32 e;
     for (int k = 0; k < EPI_MAX; ++k) {
         e.kind[k] = GLG_EPI_NONE;

@@ -16,6 +16,17 @@ __global__ void k_residual(const double *__restrict__ f, double *__restrict__ r,
 size_t ring_coef_bytes(const glg_plan *P, int nmaps) {
     return sizeof(double2) * (size_t)nmaps * P->nrings * (P->mmax + 1);
 }
+size_t up256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+// Plain-form workspaces end with the FP64 ring FFTs' global ring buffers
+// (nside > 2048 only; none below).
+void *ring_gbuf(const glg_plan *P, void *ws, size_t before) {
+    return glg_ring64_gbuf_bytes(P) ? (char *)ws + up256(before) : nullptr;
+}
+size_t with_gbuf(const glg_plan *P, size_t before) {
+    const size_t g = glg_ring64_gbuf_bytes(P);
+    return g ? up256(before) + g : before;
+}
 
 }  // namespace
 
@@ -38,7 +49,6 @@ struct FastWs {
     glg_refine_list rl;
     char *end;
 };
-size_t up256(size_t b) { return (b + 255) & ~(size_t)255; }
 // Offsets from the workspace's start (256-byte aligned blocks: the lists'
 // int4 items and the staged maps' float4 stores need 16-byte alignment).
 FastWs fast_ws(const glg_plan *P, int nmaps, void *ws) {
@@ -58,6 +68,9 @@ FastWs fast_ws(const glg_plan *P, int nmaps, void *ws) {
     c += 256;
     w.rl.items = (int4 *)c;
     c += up256(sizeof(int4) * (size_t)w.rl.cap);
+    const size_t gzb = glg_ring_gz_bytes(P->nside);
+    w.rl.gz = gzb ? (float2 *)c : nullptr;
+    c += up256(gzb);
     w.end = c;
     return w;
 }
@@ -70,7 +83,7 @@ size_t fast_ws_bytes(const glg_plan *P, int nmaps) {
 extern "C" size_t glg_alm2map_workspace(const glg_plan *P, int nmaps, int form) {
     if (!P || nmaps <= 0) return 0;
     if (form == GLG_FORM_FAST) return fast_ws_bytes(P, nmaps);
-    return ring_coef_bytes(P, nmaps);
+    return with_gbuf(P, ring_coef_bytes(P, nmaps));
 }
 
 extern "C" int glg_alm2map(const glg_plan *P, const void *alm, int nmaps, int form, void *maps,
@@ -101,7 +114,7 @@ extern "C" int glg_alm2map(const glg_plan *P, const void *alm, int nmaps, int fo
     double2 *F = (double2 *)ws;
     int rc = glg_launch_leg_syn(P, (const double2 *)alm, nmaps, F, st);
     if (rc) return rc;
-    return glg_launch_ring_syn(P, F, nmaps, (double *)maps, epi, st);
+    return glg_launch_ring_syn(P, F, nmaps, (double *)maps, epi, ring_gbuf(P, ws, ring_coef_bytes(P, nmaps)), st);
 }
 
 extern "C" size_t glg_alm2map_host_workspace(const glg_plan *P, int nmaps) {
@@ -267,7 +280,7 @@ extern "C" int glg_workspace_status(const void *ws, void *stream) {
 }
 
 extern "C" size_t glg_alm2map_spin_workspace(const glg_plan *P) {
-    return P ? ring_coef_bytes(P, 2) : 0;
+    return P ? with_gbuf(P, ring_coef_bytes(P, 2)) : 0;
 }
 
 extern "C" int glg_alm2map_spin(const glg_plan *P, const void *elm, const void *blm, int spin,
@@ -280,14 +293,15 @@ extern "C" int glg_alm2map_spin(const glg_plan *P, const void *elm, const void *
     double2 *F = (double2 *)ws;
     int rc = glg_launch_leg_syn_spin(P, (const double2 *)elm, (const double2 *)blm, spin, F, st);
     if (rc) return rc;
-    rc = glg_launch_ring_syn(P, F, 1, (double *)q, nullptr, st);
+    void *gb = ring_gbuf(P, ws, ring_coef_bytes(P, 2));
+    rc = glg_launch_ring_syn(P, F, 1, (double *)q, nullptr, gb, st);
     if (rc) return rc;
-    return glg_launch_ring_syn(P, F + (size_t)P->nrings * (P->mmax + 1), 1, (double *)u, nullptr, st);
+    return glg_launch_ring_syn(P, F + (size_t)P->nrings * (P->mmax + 1), 1, (double *)u, nullptr, gb, st);
 }
 
 extern "C" size_t glg_map2alm_workspace(const glg_plan *P, int nmaps) {
     if (!P || nmaps <= 0) return 0;
-    return ring_coef_bytes(P, nmaps) + sizeof(double) * (size_t)nmaps * P->npix;
+    return with_gbuf(P, ring_coef_bytes(P, nmaps) + sizeof(double) * (size_t)nmaps * P->npix);
 }
 
 extern "C" int glg_map2alm(const glg_plan *P, const void *maps, int nmaps, int niter, void *alm,
@@ -302,19 +316,20 @@ extern "C" int glg_map2alm(const glg_plan *P, const void *maps, int nmaps, int n
     double *tmp = (double *)((char *)ws + ring_coef_bytes(P, nmaps));
     const double *f = (const double *)maps;
     double2 *a = (double2 *)alm;
-    int rc = glg_launch_ring_ana(P, f, nmaps, G, st);
+    void *gb = ring_gbuf(P, ws, ring_coef_bytes(P, nmaps) + sizeof(double) * (size_t)nmaps * P->npix);
+    int rc = glg_launch_ring_ana(P, f, nmaps, G, gb, st);
     if (rc) return rc;
     if ((rc = glg_launch_leg_ana(P, G, nmaps, a, 0, st))) return rc;
     const int64_t n = (int64_t)nmaps * P->npix;
     for (int it = 0; it < niter; ++it) {
         if ((rc = glg_launch_leg_syn(P, a, nmaps, G, st))) return rc;
-        if ((rc = glg_launch_ring_syn(P, G, nmaps, tmp, nullptr, st))) return rc;
+        if ((rc = glg_launch_ring_syn(P, G, nmaps, tmp, nullptr, gb, st))) return rc;
         {
             GLG_LAUNCH_SCOPE("k_residual", st);
             k_residual<<<1216, 256, 0, st>>>(f, tmp, n);
             GLG_CHECK_LAUNCH("k_residual");
         }
-        if ((rc = glg_launch_ring_ana(P, tmp, nmaps, G, st))) return rc;
+        if ((rc = glg_launch_ring_ana(P, tmp, nmaps, G, gb, st))) return rc;
         if ((rc = glg_launch_leg_ana(P, G, nmaps, a, 1, st))) return rc;
     }
     return GLG_OK;
@@ -333,6 +348,7 @@ extern "C" int glg_autotune_fast(glg_plan *P, int nmaps, void *maps, void *ws, s
     if (rc) return rc;
     const size_t fbytes = sizeof(float2) * (size_t)nmaps * P->nrings * (P->mmax + 1);
     float2 *Ft = fast_ws(P, nmaps, ws).Ft;
+    float2 *gz = fast_ws(P, nmaps, ws).rl.gz;
     cudaError_t e = cudaMemsetAsync(Ft, 0, fbytes, st);
     if (e != cudaSuccess) return glg_cuda_status(e, "glg_autotune_fast");
     cudaEvent_t a, b;
@@ -347,9 +363,10 @@ extern "C" int glg_autotune_fast(glg_plan *P, int nmaps, void *maps, void *ws, s
             if (glg_ring32_smem(P->buckets[k].kind, P->buckets[k].size, threads, P->buckets[k].fold != 0) >
                 227 * 1024)
                 continue;
-            if ((rc = glg_launch_ring_bucket_f32(P, k, threads, Ft, nmaps, (float *)maps, st))) break;
+            if ((rc = glg_launch_ring_bucket_f32(P, k, threads, Ft, nmaps, (float *)maps, gz, st))) break;
             cudaEventRecord(a, st);
-            for (int r = 0; r < 2 && !rc; ++r) rc = glg_launch_ring_bucket_f32(P, k, threads, Ft, nmaps, (float *)maps, st);
+            for (int r = 0; r < 2 && !rc; ++r)
+                rc = glg_launch_ring_bucket_f32(P, k, threads, Ft, nmaps, (float *)maps, gz, st);
             cudaEventRecord(b, st);
             if (rc) break;
             e = cudaEventSynchronize(b);

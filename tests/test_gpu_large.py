@@ -147,3 +147,44 @@ def test_accuracy_report(g):
         assert abs(r["rms_rel"] - rel_rms(fast[s], plain[s])) < 1e-12
         assert r["rms_rel"] < FAST_RMS and r["max_rel"] < 2e-5
         assert abs(r["max_abs"] - np.max(np.abs(fast[s].astype(np.float64) - plain[s]))) < 1e-12
+
+
+def test_cfg5_size_fast_vs_plain_and_counts(g):
+    """Config-5 sizes, nside 4096 / lmax 8192, at two shells: the fast form
+    (lambda from the FP32 recurrence -- the P_lm table would take 1.1 TB --
+    and Bluestein rings of M = 32768 in global memory) within 1e-6 RMS of the
+    FP64 form on Gaussian fields; Poisson galaxy counts (n = 5 per pixel)
+    bit-exact from the same delta values given as float32 or float64, i.e.
+    whichever form produced them."""
+    import torch
+
+    from glass_gb300 import _lib
+
+    _lib.clear_plans()
+    torch.cuda.empty_cache()
+    try:
+        nside, lmax = 4096, 8192
+        gls = _spectra_cfg3([0.02, 0.005], lmax)
+        fields = [g.grf.Normal(), g.grf.Normal()]
+        gls_d = [torch.as_tensor(c, device="cuda") for c in gls]
+        fast = list(g.generate(fields, gls_d, nside, rng=g.rng.Generator(3), form="fast"))
+        plan = _lib.get_plan(nside, lmax)
+        assert not plan.has_plm_table
+        kinds = [b["kind"] for b in g.healpix.buckets(nside, lmax)]
+        assert 3 in kinds  # rings whose Bluestein buffer lives in global memory
+        plain = list(g.generate(fields, gls_d, nside, rng=g.rng.Generator(3), form="plain"))
+        for s in range(2):
+            d = fast[s].double() - plain[s]
+            assert float(torch.sqrt(torch.mean(d * d)) / torch.sqrt(torch.mean(plain[s] ** 2))) < FAST_RMS
+        del plain, d
+        ngal = 5.0 * 12 * nside * nside / g.points.ARCMIN2_SPHERE
+        delta = fast[1]
+        c32 = g.points.counts_from_delta(ngal, delta, rng=g.rng.Generator(7))
+        c64 = g.points.counts_from_delta(ngal, delta.double(), rng=g.rng.Generator(7))
+        assert torch.equal(torch.as_tensor(c32), torch.as_tensor(c64))
+        # mean count = 5 <max(1 + delta, 0)> (the expected count is clipped at 0)
+        want = 5.0 * float(torch.clamp(1.0 + delta.double(), min=0.0).mean())
+        assert abs(float(torch.as_tensor(c32).double().mean()) / want - 1.0) < 1e-3
+    finally:
+        _lib.clear_plans()
+        torch.cuda.empty_cache()

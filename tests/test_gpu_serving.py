@@ -69,6 +69,9 @@ def test_admission_within_measured_budget(cuda_lib):
     while srv.queue or srv.active:
         srv.step()
         assert srv.used <= srv.budget
+        for r in srv.finished:  # the client takes finished maps to the host
+            r.maps = [m.cpu() for m in r.maps]
+        srv.finished.clear()
     torch.cuda.synchronize()
     assert all(r.finished is not None for r in reqs)
     # two requests fit the budget with the plan's estimated bytes; once the
