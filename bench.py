@@ -190,13 +190,34 @@ def run_cfg2(steps: int = 3) -> dict:
     out["fast_error_per_shell"] = rep
     out["fast_rel_rms_max"] = max(r["rms_rel"] for r in rep)
     kappa = torch.stack(maps).double().mean(dim=0)  # summed convergence (mean of the shells)
-    g.from_convergence(kappa, shear=True)  # warm-up (plans, pixel windows)
-    torch.cuda.synchronize()
-    a = time.perf_counter()
-    (gamma,) = g.from_convergence(kappa, shear=True)
-    torch.cuda.synchronize()
-    out["shear"] = {"ms": (time.perf_counter() - a) * 1e3, "form": "plain FP64 (map2alm iter 3 + spin-2 synthesis)",
-                    "discretized": True, "lmax": 3 * nside - 1, "finite": bool(torch.isfinite(gamma).all())}
+    shear = {"discretized": True, "lmax": 3 * nside - 1,
+             "note": "analysis of kappa (map2alm, 3 iterations) in FP64 in both forms; the form is the synthesis'"}
+    gam = {}
+    for form in ("plain", "fast"):
+        g.from_convergence(kappa, shear=True, form=form)  # warm-up (plans, spin tables, pixel windows)
+        torch.cuda.synchronize()
+        a = time.perf_counter()
+        (gam[form],) = g.from_convergence(kappa, shear=True, form=form)
+        torch.cuda.synchronize()
+        shear[form] = {"ms": (time.perf_counter() - a) * 1e3}
+    # the spin-2 synthesis alone (the shear's alm from one analysis), both forms
+    lmx = 3 * nside - 1
+    alm = g.healpix.analysis(kappa.reshape(1, -1), lmx, 3)[0]
+    zero = torch.zeros_like(alm)
+    for form in ("plain", "fast"):
+        g.healpix.alm2map_spin([alm, zero], nside, 2, lmx, form=form)
+        torch.cuda.synchronize()
+        a = time.perf_counter()
+        g.healpix.alm2map_spin([alm, zero], nside, 2, lmx, form=form)
+        torch.cuda.synchronize()
+        shear[form]["spin2_synthesis_ms"] = (time.perf_counter() - a) * 1e3
+    d = gam["fast"].to(torch.complex128) - gam["plain"]
+    shear["fast_vs_plain"] = {
+        "rms_rel": float(torch.sqrt(torch.mean(d.abs() ** 2)) / torch.sqrt(torch.mean(gam["plain"].abs() ** 2))),
+        "max_rel": float(d.abs().max() / gam["plain"].abs().max()),
+        "max_abs": float(d.abs().max())}
+    shear["finite"] = bool(torch.isfinite(gam["fast"]).all())
+    out["shear"] = shear
     return out
 
 
@@ -260,10 +281,16 @@ def run_cfg5(nshell: int = 60, nside: int = 4096, lmax: int = 8192) -> dict:
     out["counts"] = {"bit_exact_f32_vs_f64_delta": all(same), "pixels_per_s": npix / (t_counts / 2 / 1e3),
                      "mean_per_pixel": 5.0}
     a = time.perf_counter()
+    _lib.timing_enable(True)
+    _lib.timing_reset()
     (gamma,) = g.from_convergence(kappa, lmax=lmax, shear=True)
     torch.cuda.synchronize()
+    names = ("k_leg_ana", "k_leg_syn", "k_leg_syn_spin", "k_ring_ana", "k_ring_syn", "k_residual", "k_almxfl")
+    kms = {k: _lib.kernel_time(k)[0] for k in names}
+    _lib.timing_enable(False)
     out["shear"] = {"s": time.perf_counter() - a, "form": "plain FP64 (map2alm iter 3 + spin-2 synthesis)",
-                    "lmax": lmax, "discretized": True, "finite": bool(torch.isfinite(gamma).all())}
+                    "lmax": lmax, "discretized": True, "finite": bool(torch.isfinite(gamma).all()),
+                    "kernel_ms": kms}
     del gamma, kappa
     _lib.clear_plans()
     torch.cuda.empty_cache()

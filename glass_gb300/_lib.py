@@ -88,6 +88,8 @@ _SIGNATURES = {
     "glg_peak_fma": ([c_i, c_i, c_i, c_p, c_p], c_i),
     "glg_alm2map_spin_workspace": ([c_p], c_sz),
     "glg_alm2map_spin": ([c_p, c_p, c_p, c_i, c_p, c_p, c_p, c_sz, c_p], c_i),
+    "glg_alm2map_spin_fast_workspace": ([c_p, c_i, c_i], c_sz),
+    "glg_alm2map_spin_fast": ([c_p, c_p, c_p, c_i, c_i, c_p, c_p, c_sz, c_p], c_i),
     "glg_map2alm_workspace": ([c_p, c_i], c_sz),
     "glg_map2alm": ([c_p, c_p, c_i, c_i, c_p, c_p, c_sz, c_p], c_i),
     "glg_timing_enable": ([c_i], c_i),
@@ -272,6 +274,15 @@ def to_device(x, dtype: torch.dtype, device: torch.device | None = None) -> torc
     else:
         t = torch.as_tensor(np.asarray(x), dtype=dtype).to(device, non_blocking=False)
     return t.contiguous()
+
+
+def default_form() -> str:
+    """The transform form when a call names none: ``GLASS_GB300_FORM``
+    ("plain", the FP64 drop-in, by default; or "fast")."""
+    f = os.environ.get("GLASS_GB300_FORM", "plain").lower()
+    if f not in ("plain", "fast"):
+        raise ValueError(f"GLASS_GB300_FORM must be 'plain' or 'fast', not {f!r}")
+    return f
 
 
 def is_numpy_like(x) -> bool:

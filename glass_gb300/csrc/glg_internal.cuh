@@ -101,6 +101,13 @@ struct glg_plan {
     // beyond lmax and beyond the last ring pair.  nullptr: recurrence path.
     float4 *plm;
     size_t plm_bytes;
+    // Spin tables of the fast spin-s synthesis (s = 1, 2; index s - 1), built
+    // on first use by glg_plan_prepare_spin: the same tile layout holding
+    // lambda^+_l / d_l and lambda^-_l / d_l, and per (m, ring tile) the first
+    // group where either reaches 2^-40 on some ring of the tile.
+    float4 *plm_spin[2][2];  // [s - 1][+ / -]
+    int *tfirst_spin[2];
+    size_t spin_bytes;
 
     // FP32 ring FFTs of the fast form.  Class 0: ring lengths whose prime
     // factors are all <= 13 (mixed-radix DIF, output order from pos16).
@@ -157,6 +164,9 @@ size_t glg_ring32_smem(int kind, int n_or_M, int threads, bool fold);
 #define GLG_GROUP 16
 
 int glg_plan_prepare_fast(glg_plan *P, cudaStream_t st);
+// The spin-s tables of the fast spin synthesis (after glg_plan_prepare_fast);
+// GLG_ERR_UNSUPPORTED when they do not fit the table budget and free memory.
+int glg_plan_prepare_spin(glg_plan *P, int spin, cudaStream_t st);
 
 // Bytes of one group's P_lm tile (128 ring pairs x 16 l, FP32).
 #define GLG_PLM_TILE_BYTES (128 * GLG_GROUP * 4)
@@ -221,7 +231,14 @@ struct glg_tile_run {
 };
 int glg_launch_leg_tc(const glg_plan *P, const float2 *alm, int nmaps, float *bpack, float2 *F,
                       int *err, const glg_tile_run &run, cudaStream_t st);
-// Ring FFTs of the ring pairs [p0, p1) only (transpose included).
+// The same with the B columns of maps nsplit .. nmaps-1 taken from alm2
+// (map nsplit + k is alm2 row k) and the lambda tiles and first groups of a
+// spin table instead of the plan's P_lm table (table/tfirst null: the plan's).
+int glg_launch_leg_tc_ex(const glg_plan *P, const float2 *alm, const float2 *alm2, int nsplit, int nmaps,
+                         float *bpack, float2 *F, int *err, const glg_tile_run &run, const float4 *table,
+                         const int *tfirst, cudaStream_t st);
+// Ring FFTs of the ring pairs [p0, p1) only (transpose included; F null:
+// Ft already holds the sums [map][ring][m]).
 int glg_launch_ring_syn_f32_range(const glg_plan *P, const float2 *F, float2 *Ft, int nmaps, float *maps,
                                   const glg_epilogue *epi, int p0, int p1, const glg_refine_list *rl,
                                   cudaStream_t st);

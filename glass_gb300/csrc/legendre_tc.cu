@@ -636,7 +636,8 @@ template <int N>
 __global__ void __launch_bounds__(256) k_pack_b(int mmax, int lmax, int nmaps, int64_t nalm, int64_t ngroups,
                                                 const int64_t *__restrict__ mofs,
                                                 const int64_t *__restrict__ goff, const float4 *__restrict__ coef32,
-                                                const float2 *__restrict__ alm, float *__restrict__ bpack) {
+                                                const float2 *__restrict__ alm, const float2 *__restrict__ alm2,
+                                                int nsplit, float *__restrict__ bpack) {
     const int64_t idx = blockIdx.x * 256LL + threadIdx.x;
     if (idx >= ngroups * 2 * N) return;
     const int64_t gg = idx / (2 * N);
@@ -654,14 +655,15 @@ __global__ void __launch_bounds__(256) k_pack_b(int mmax, int lmax, int nmaps, i
     const int map = ng * 4 + mi;
     float4 rh, rl, ih, il;
     float *r4 = &rh.x, *i4 = &ih.x, *rl4 = &rl.x, *il4 = &il.x;
-    const int64_t base = (int64_t)map * nalm + mofs[m];
+    const float2 *src = map < nsplit ? alm + (int64_t)map * nalm : alm2 + (int64_t)(map - nsplit) * nalm;
+    const int64_t base = mofs[m];
 #pragma unroll
     for (int kk = 0; kk < 4; ++kk) {
         const int l = m + g * GLG_GROUP + par + 8 * j + 2 * kk;
         float2 z = make_float2(0.f, 0.f);
         float d = 0.f;
         if (l <= lmax && map < nmaps) {
-            z = alm[base + (l - m)];
+            z = src[base + (l - m)];
             d = coef32[mofs[m] + (l - m)].z;
         }
         if (m == 0) z.y = 0.f;  // imaginary part of a_l0 is ignored
@@ -684,13 +686,15 @@ __global__ void __launch_bounds__(256) k_pack_b(int mmax, int lmax, int nmaps, i
 }
 
 template <int N>
-int launch_tc(const glg_plan *P, const float2 *alm, int nmaps, float *bpack, float2 *F, int *err,
-              const glg_tile_run &run, cudaStream_t st) {
+int launch_tc(const glg_plan *P, const float2 *alm, const float2 *alm2, int nsplit, int nmaps, float *bpack,
+              float2 *F, int *err, const glg_tile_run &run, const float4 *table, const int *tfirst,
+              cudaStream_t st) {
     if (run.pack) {
         const int64_t items = P->ngroups * 2 * N;
         GLG_LAUNCH_SCOPE("k_pack_b", st);
         k_pack_b<N><<<(unsigned)((items + 255) / 256), 256, 0, st>>>(P->mmax, P->lmax, nmaps, P->nalm, P->ngroups,
-                                                                     P->mofs, P->goff, P->coef32, alm, bpack);
+                                                                     P->mofs, P->goff, P->coef32, alm, alm2,
+                                                                     nsplit, bpack);
         GLG_CHECK_LAUNCH("k_pack_b");
     }
     LegTcArgs a;
@@ -714,7 +718,7 @@ int launch_tc(const glg_plan *P, const float2 *alm, int nmaps, float *bpack, flo
     a.seeds = P->seeds;
     a.seed_stride = P->seed_stride;
     a.lstart = P->lstart;
-    a.tfirst = P->tfirst;
+    a.tfirst = tfirst ? tfirst : P->tfirst;
     a.bpack = reinterpret_cast<const unsigned char *>(bpack);
     a.F = F;
     a.err = err;
@@ -722,7 +726,7 @@ int launch_tc(const glg_plan *P, const float2 *alm, int nmaps, float *bpack, flo
     a.ucount = reinterpret_cast<unsigned long long *>(reinterpret_cast<char *>(err) + 64) + run.slot;
     a.wait_limit = g_test_wait_limit ? g_test_wait_limit : WAIT_LIMIT;
     a.stall = g_test_stall;
-    a.plm = P->plm;
+    a.plm = table ? table : P->plm;
     int nsm = 0, dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -736,7 +740,7 @@ int launch_tc(const glg_plan *P, const float2 *alm, int nmaps, float *bpack, flo
         GLG_LAUNCH_SCOPE("k_leg_tc", st);
         kern<<<(unsigned)grid, THREADS, smem, st>>>(a);
     };
-    if (P->plm) go(k_leg_tc<N, true>, sizeof(Smem<N, true>));
+    if (a.plm) go(k_leg_tc<N, true>, sizeof(Smem<N, true>));
     else go(k_leg_tc<N, false>, sizeof(Smem<N, false>));
     GLG_CHECK_LAUNCH("k_leg_tc");
     return GLG_OK;
@@ -757,15 +761,27 @@ size_t glg_leg_tc_pack_bytes(const glg_plan *P, int nmaps) {
 
 int glg_launch_leg_tc(const glg_plan *P, const float2 *alm, int nmaps, float *bpack, float2 *F,
                       int *err, const glg_tile_run &run, cudaStream_t st) {
+    return glg_launch_leg_tc_ex(P, alm, nullptr, nmaps, nmaps, bpack, F, err, run, nullptr, nullptr, st);
+}
+
+int glg_launch_leg_tc_ex(const glg_plan *P, const float2 *alm, const float2 *alm2, int nsplit, int nmaps,
+                         float *bpack, float2 *F, int *err, const glg_tile_run &run, const float4 *table,
+                         const int *tfirst, cudaStream_t st) {
     const int N = ((2 * nmaps + 15) / 16) * 16;
+    if ((table == nullptr) != (tfirst == nullptr)) {
+        glg_set_error("fast Legendre contraction: a spin table needs its first-group table");
+        return GLG_ERR_INVALID;
+    }
+#define GLG_TC(n) launch_tc<n>(P, alm, alm2, nsplit, nmaps, bpack, F, err, run, table, tfirst, st)
     switch (N) {
-        case 16: return launch_tc<16>(P, alm, nmaps, bpack, F, err, run, st);
-        case 32: return launch_tc<32>(P, alm, nmaps, bpack, F, err, run, st);
-        case 48: return launch_tc<48>(P, alm, nmaps, bpack, F, err, run, st);
-        case 64: return launch_tc<64>(P, alm, nmaps, bpack, F, err, run, st);
-        case 80: return launch_tc<80>(P, alm, nmaps, bpack, F, err, run, st);
+        case 16: return GLG_TC(16);
+        case 32: return GLG_TC(32);
+        case 48: return GLG_TC(48);
+        case 64: return GLG_TC(64);
+        case 80: return GLG_TC(80);
         default:
             glg_set_error("fast Legendre contraction: at most 40 maps per launch");
             return GLG_ERR_UNSUPPORTED;
     }
 }
+#undef GLG_TC

@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <atomic>
+#include <cstdio>
 #include <math.h>
 
 #include <algorithm>
@@ -232,7 +233,8 @@ extern "C" void glg_plan_destroy(glg_plan *P) {
                     P->fft_nst, P->tw_ofs,  P->tw,      P->cth32,  P->tw32,   P->coef32,
                     P->goff,  P->seeds,     P->lstart,  P->tfirst, P->bucket_pairs, P->chirp_ofs,
                     P->chirp, P->pos_ofs, P->pos16,   P->blu_ofs, P->blu_M,  P->blu_H,  P->twM,
-                    P->plm,   P->twMp};
+                    P->plm,   P->twMp, P->plm_spin[0][0], P->plm_spin[0][1], P->plm_spin[1][0],
+                    P->plm_spin[1][1], P->tfirst_spin[0], P->tfirst_spin[1]};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     delete[] P->bucket_pairs_host;
@@ -400,6 +402,93 @@ __global__ void k_plan_plm(int lmax, int npairs, int ntiles, const double *__res
             plm[(gt * 4 + (t % GLG_GROUP) / 4) * 128 + p % 128] = q4;
         }
     }
+}
+
+// Spin-s tables (s = 1, 2) of the fast spin synthesis: the same tiles as
+// k_plan_plm holding lambda^+_l / d_l (tab_p) and lambda^-_l / d_l (tab_m),
+// with lambda^+- from lambda_l and lambda_{l-1} of the FP64 extended-range
+// recurrence (the formulas of the FP64 spin synthesis, evaluated in FP64 and
+// rounded once):
+//   dlam = (l x lam_l - sqrt((2l+1)/(2l-1) (l^2 - m^2)) lam_{l-1}) / sin,
+//   s = 1: lambda^+ = -dlam / N, lambda^- = m lam / (sin N),  N = sqrt(l(l+1));
+//   s = 2: lambda^+ = (-2 cot dlam + (2 m^2 / sin^2 - l(l+1)) lam) / N,
+//          lambda^- = (2 m / sin)(cot lam - dlam) / N,        N = sqrt((l-1)l(l+1)(l+2)).
+// One block of 128 threads per (ring tile, m); the block also writes the
+// tile's first group where |lambda^+| or |lambda^-| reaches 2^-40 (the
+// number of groups when none does).
+__global__ void k_plan_plm_spin(int lmax, int npairs, int ntiles, int spin, const double *__restrict__ cth,
+                                const double *__restrict__ sth, const int64_t *__restrict__ mofs,
+                                const double2 *__restrict__ coef, const double *__restrict__ lmm,
+                                const int *__restrict__ lmm_scale, const int64_t *__restrict__ goff,
+                                const float4 *__restrict__ coef32, float4 *__restrict__ tab_p,
+                                float4 *__restrict__ tab_m, int *__restrict__ tfirst) {
+    const int m = blockIdx.y;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;  // < ntiles * 128
+    const bool live = p < npairs;
+    const int pp = live ? p : npairs - 1;
+    const double x = cth[pp], isn = 1.0 / sth[pp], cot = x * isn, fm = m;
+    double l0 = 0.0, l1 = lmm[(int64_t)m * npairs + pp];
+    int sc = lmm_scale[(int64_t)m * npairs + pp];
+    const int64_t base = mofs[m];
+    const int G = (lmax - m + GLG_GROUP) / GLG_GROUP;
+    int first = G;
+    float4 qp = make_float4(0.f, 0.f, 0.f, 0.f), qm = qp;
+    float *vp = &qp.x, *vm = &qm.x;
+    for (int t = 0; t < G * GLG_GROUP; ++t) {
+        const int l = m + t;
+        float a = 0.f, b = 0.f;
+        if (l <= lmax) {
+            if (l > m) {
+                double nl;
+                if (l == m + 1) {
+                    nl = sqrt(2.0 * m + 3.0) * x * l1;
+                } else {
+                    const double2 ab = coef[base + t];
+                    nl = ab.x * (x * l1) - ab.y * l0;
+                }
+                l0 = l1;
+                l1 = nl;
+                if (sc < 0 && fabs(nl) > GLG_TWO_P400) {
+                    l0 *= GLG_TWO_M800;
+                    l1 *= GLG_TWO_M800;
+                    sc += 1;
+                }
+            }
+            if (live && sc == 0 && l >= spin) {
+                const double fl = l, lam = l1, lprev = l > m ? l0 : 0.0;
+                const double dlam =
+                    (fl * x * lam - sqrt((2.0 * fl + 1.0) / (2.0 * fl - 1.0) * (fl * fl - fm * fm)) * lprev) * isn;
+                double lp, lmv;
+                if (spin == 1) {
+                    const double nrm = 1.0 / sqrt(fl * (fl + 1.0));
+                    lp = -dlam * nrm;
+                    lmv = fm * lam * isn * nrm;
+                } else {
+                    const double nrm = 1.0 / sqrt((fl - 1.0) * fl * (fl + 1.0) * (fl + 2.0));
+                    lp = (-2.0 * cot * dlam + (2.0 * fm * fm * isn * isn - fl * (fl + 1.0)) * lam) * nrm;
+                    lmv = (2.0 * fm * isn) * (cot * lam - dlam) * nrm;
+                }
+                if (first == G && fmax(fabs(lp), fabs(lmv)) >= 0x1p-40) first = t / GLG_GROUP;
+                const double d = (double)coef32[base + t].z;
+                a = (float)(lp / d);
+                b = (float)(lmv / d);
+            }
+        }
+        vp[t & 3] = a;
+        vm[t & 3] = b;
+        if ((t & 3) == 3) {
+            const int64_t gt = (goff[m] + t / GLG_GROUP) * ntiles + p / 128;
+            const int64_t ix = (gt * 4 + (t % GLG_GROUP) / 4) * 128 + p % 128;
+            tab_p[ix] = qp;
+            tab_m[ix] = qm;
+        }
+    }
+    __shared__ int fmin_s;
+    if (threadIdx.x == 0) fmin_s = G;
+    __syncthreads();
+    atomicMin(&fmin_s, first);
+    __syncthreads();
+    if (threadIdx.x == 0) tfirst[(int64_t)m * ntiles + blockIdx.x] = fmin_s;
 }
 
 // Output position of frequency k after in-place DIF passes with `radix`.
@@ -668,6 +757,43 @@ int glg_plan_prepare_fast(glg_plan *P, cudaStream_t st) {
     if (e != cudaSuccess) return glg_cuda_status(e, "glg_plan_prepare_fast");
     if ((rc = build_fft32_tables(P, st))) return rc;
     P->fast_ready = true;
+    return GLG_OK;
+}
+
+int glg_plan_prepare_spin(glg_plan *P, int spin, cudaStream_t st) {
+    static std::mutex mu;
+    std::lock_guard<std::mutex> lk(mu);
+    GLG_REQUIRE(spin == 1 || spin == 2, "fast spin synthesis: spin must be 1 or 2");
+    GLG_REQUIRE(P->fast_ready, "fast spin synthesis: fast tables not prepared");
+    const int k = spin - 1;
+    if (P->plm_spin[k][0]) return GLG_OK;
+    const int np = P->npairs, lmax = P->lmax, ntiles = (np + 127) / 128;
+    const size_t tbytes = (size_t)GLG_PLM_TILE_BYTES * (size_t)P->ngroups * ntiles;
+    const size_t used = P->plm_bytes + P->spin_bytes;
+    size_t free_b = 0, total_b = 0;
+    if (used + 2 * tbytes > g_plm_budget.load() || cudaMemGetInfo(&free_b, &total_b) != cudaSuccess ||
+        2 * tbytes + ((size_t)4 << 30) > free_b) {
+        cudaGetLastError();
+        char msg[200];
+        snprintf(msg, sizeof msg,
+                 "fast spin synthesis: its lambda+- tables (2 x %.2f GB) do not fit the table budget or the "
+                 "free device memory; use the FP64 form", (double)tbytes / 1e9);
+        glg_set_error(msg);
+        return GLG_ERR_UNSUPPORTED;
+    }
+    int rc;
+    if ((rc = dalloc(P, &P->plm_spin[k][0], tbytes / sizeof(float4))) ||
+        (rc = dalloc(P, &P->plm_spin[k][1], tbytes / sizeof(float4))) ||
+        (rc = dalloc(P, &P->tfirst_spin[k], (size_t)(lmax + 1) * ntiles)))
+        return rc;
+    P->spin_bytes += 2 * tbytes;
+    k_plan_plm_spin<<<dim3(ntiles, lmax + 1), 128, 0, st>>>(lmax, np, ntiles, spin, P->cth, P->sth, P->mofs,
+                                                           P->coef, P->lmm, P->lmm_scale, P->goff, P->coef32,
+                                                           P->plm_spin[k][0], P->plm_spin[k][1],
+                                                           P->tfirst_spin[k]);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return glg_cuda_status(e, "glg_plan_prepare_spin");
     return GLG_OK;
 }
 

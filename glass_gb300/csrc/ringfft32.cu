@@ -872,9 +872,11 @@ int glg_launch_ring_syn_f32_range(const glg_plan *P, const float2 *F, float2 *Ft
         }
     // north rings p0 .. p1-1 and their south partners nr-p1 .. nr-1-p0 (the
     // equator ring, pair npairs-1, is its own partner)
-    int rc = launch_transpose(F, Ft, nm, nr, p0, p1, nmaps, st);
-    if (!rc) rc = launch_transpose(F, Ft, nm, nr, nr - p1 > p1 ? nr - p1 : p1, nr - p0, nmaps, st);
-    if (rc) return rc;
+    if (F) {
+        int rc = launch_transpose(F, Ft, nm, nr, p0, p1, nmaps, st);
+        if (!rc) rc = launch_transpose(F, Ft, nm, nr, nr - p1 > p1 ? nr - p1 : p1, nr - p0, nmaps, st);
+        if (rc) return rc;
+    }
     RingArgs a;
     ring_args(P, Ft, nmaps, maps, a);
     Epi32 e;

@@ -221,10 +221,7 @@ def _glass_to_healpix_alm(alm):
 
 
 def _default_form() -> str:
-    f = os.environ.get("GLASS_GB300_FORM", "plain").lower()
-    if f not in ("plain", "fast"):
-        raise ValueError(f"GLASS_GB300_FORM must be 'plain' or 'fast', not {f!r}")
-    return f
+    return _lib.default_form()
 
 
 class _FieldBatcher:

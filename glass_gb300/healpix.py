@@ -339,10 +339,51 @@ def _spin_synth(elm: torch.Tensor, blm: torch.Tensor | None, nside: int, spin: i
     return q, u
 
 
-def alm2map_spin(alms: Sequence, nside: int, spin: int, lmax: int):
-    """Spin-weighted maps [Q, U] from [E, B] alm (glass/healpix.py:81-108)."""
+def _spin_synth_fast(elm: torch.Tensor, blm: torch.Tensor | None, nside: int, spin: int, lmax: int):
+    """Fast-form spin synthesis of nf fields: E (and B) alm [nf, nalm] (or
+    [nalm]) -> float32 Q, U maps [nf, npix] (or [npix]).  The spin tables
+    are built with the plan on first use (NotImplementedError when they do
+    not fit the P_lm table budget)."""
+    plan = get_plan(nside, lmax, elm.device)
+    single = elm.ndim == 1
+    e = elm.reshape(-1, plan.nalm).to(torch.complex64).contiguous()
+    b = None if blm is None else blm.reshape(-1, plan.nalm).to(torch.complex64).contiguous()
+    nf = e.shape[0]
+    stream = c_p(stream_ptr(e.device))
+    if not getattr(plan, "tuned", False):
+        n = min(2 * nf, FAST_MAX_MAPS)
+        tws = torch.empty(int(lib().glg_alm2map_workspace(plan.handle, n, _lib.FORM_FAST)), dtype=torch.uint8,
+                          device=e.device)
+        autotune(plan, n, torch.empty((n, plan.npix), dtype=torch.float32, device=e.device), tws)
+        del tws
+    step = min(nf, 20)
+    ws_bytes = int(lib().glg_alm2map_spin_fast_workspace(plan.handle, step, int(b is not None)))
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device=e.device)
+    q = torch.empty((nf, plan.npix), dtype=torch.float32, device=e.device)
+    u = torch.empty_like(q)
+    for f0 in range(0, nf, step):
+        cnt = min(step, nf - f0)
+        qu = torch.empty((2, cnt, plan.npix), dtype=torch.float32, device=e.device)
+        check(lib().glg_alm2map_spin_fast(plan.handle, c_p(ptr(e[f0:f0 + cnt])),
+                                          c_p(ptr(b[f0:f0 + cnt])) if b is not None else None, cnt, int(spin),
+                                          c_p(ptr(qu)), c_p(ptr(ws)), ws_bytes, stream), "glg_alm2map_spin_fast")
+        check(lib().glg_workspace_status(c_p(ptr(ws)), stream), "glg_alm2map_spin_fast")
+        q[f0:f0 + cnt] = qu[0]
+        u[f0:f0 + cnt] = qu[1]
+    return (q[0], u[0]) if single else (q, u)
+
+
+def alm2map_spin(alms: Sequence, nside: int, spin: int, lmax: int, *, form: str | None = None):
+    """Spin-weighted maps [Q, U] from [E, B] alm (glass/healpix.py:81-108).
+
+    ``form="plain"`` (the default unless ``GLASS_GB300_FORM`` says otherwise):
+    FP64, float64 maps.  ``form="fast"``: split-precision TF32 contraction
+    and FP32 ring FFTs, float32 maps."""
     if len(alms) != 2:
         raise ValueError("alm2map_spin needs exactly two alm arrays")
+    form = _lib.default_form() if form is None else form
+    if form not in ("plain", "fast"):
+        raise ValueError(f"form must be 'plain' or 'fast', not {form!r}")
     numpy_out = all(_lib.is_numpy_like(a) for a in alms)
     e = _as_device_alm(alms[0])
     b = _as_device_alm(alms[1])
@@ -351,7 +392,10 @@ def alm2map_spin(alms: Sequence, nside: int, spin: int, lmax: int):
     b = _resize_alm(b, lmax_in, lmax)
     if not bool(torch.any(b != 0)):
         b = None
-    q, u = _spin_synth(e, b, nside, int(spin), int(lmax))
+    if form == "fast":
+        q, u = _spin_synth_fast(e, b, nside, int(spin), int(lmax))
+    else:
+        q, u = _spin_synth(e, b, nside, int(spin), int(lmax))
     return [_finish(q, numpy_out), _finish(u, numpy_out)]
 
 

@@ -21,15 +21,25 @@ def _ell(lmax: int, like) -> np.ndarray:
 
 
 def from_convergence(kappa, lmax: int | None = None, *, potential: bool = False,
-                     deflection: bool = False, shear: bool = False, discretized: bool = True):
+                     deflection: bool = False, shear: bool = False, discretized: bool = True,
+                     form: str | None = None):
     """Potential, deflection and/or shear from a convergence map (glass/lensing.py:185-371).
 
     ``discretized=True`` (the default) scales the shear's harmonic kernel by
     the ratio of the spin-2 and spin-0 pixel windows pw2 / pw0
     (glass/lensing.py:360-362), computed on the GPU by ``healpix.pixwin``.
+    ``form="plain"`` (default unless ``GLASS_GB300_FORM`` says otherwise):
+    FP64 throughout.  ``form="fast"``: the analysis of kappa and the harmonic
+    kernels stay FP64; the syntheses of the potential, deflection and shear
+    run in the fast form (split-precision TF32 contractions, FP32 ring FFTs)
+    and return float32 / complex64 maps.
     """
     if not (potential or deflection or shear):
         return ()
+    form = _lib.default_form() if form is None else form
+    if form not in ("plain", "fast"):
+        raise ValueError(f"form must be 'plain' or 'fast', not {form!r}")
+    fast = form == "fast"
     numpy_out = _lib.is_numpy_like(kappa)
     k = _lib.to_device(kappa, torch.float64)
     nside = hp.get_nside(k)
@@ -47,15 +57,17 @@ def from_convergence(kappa, lmax: int | None = None, *, potential: bool = False,
     fl[1:] = -2.0 / (ell[1:] * (ell[1:] + 1))
     alm = hp.almxfl(alm, torch.as_tensor(fl, device=alm.device))
     if potential:
-        psi = hp.synth(alm.reshape(1, -1), nside, lmax)[0]
+        psi = hp.synth(alm.reshape(1, -1), nside, lmax, form="fast")[0] if fast else \
+            hp.synth(alm.reshape(1, -1), nside, lmax)[0]
         results += (out(psi),)
     if not (deflection or shear):
         return results
     # potential -> deflection: sqrt(l (l+1))
     fl = np.sqrt(ell * (ell + 1))
     alm = hp.almxfl(alm, torch.as_tensor(fl, device=alm.device))
+    spin_synth = hp._spin_synth_fast if fast else hp._spin_synth
     if deflection:
-        q, u = hp._spin_synth(alm, None, nside, 1, lmax)
+        q, u = spin_synth(alm, None, nside, 1, lmax)
         results += (out(torch.complex(q, u)),)
     if not shear:
         return results
@@ -67,7 +79,7 @@ def from_convergence(kappa, lmax: int | None = None, *, potential: bool = False,
         pw0, pw2 = hp.pixwin_device(nside, lmax, alm.device)
         flt = flt * (pw2 / pw0)
     alm = hp.almxfl(alm, flt)
-    q, u = hp._spin_synth(alm, None, nside, 2, lmax)
+    q, u = spin_synth(alm, None, nside, 2, lmax)
     results += (out(torch.complex(q, u)),)
     return results
 

@@ -296,6 +296,21 @@ int glg_alm2map_spin(const glg_plan *plan, const void *elm, const void *blm, int
                      void *u, void *workspace, size_t workspace_bytes, void *stream);
 
 /*
+ * Fast form of the spin-s synthesis (s = 1, 2) of the same convention, for
+ * nfields fields at once (glass/healpix.py:81-108 as called at
+ * glass/lensing.py:343, :366): two split-precision TF32 contractions on the
+ * tensor cores (lambda^+ and lambda^-, from FP32 tables of the FP64
+ * recurrence kept with the plan; GLG_ERR_UNSUPPORTED when they do not fit the
+ * P_lm table budget or the free device memory) and FP32 ring FFTs.
+ * elm: complex64 [nfields][nalm]; blm: complex64 [nfields][nalm] or NULL
+ * (zero B-modes); qu: float32 [2][nfields][npix] (the Q maps, then the U
+ * maps).  nfields <= 20.  Check glg_workspace_status afterwards.
+ */
+size_t glg_alm2map_spin_fast_workspace(const glg_plan *plan, int nfields, int with_b);
+int glg_alm2map_spin_fast(const glg_plan *plan, const void *elm, const void *blm, int nfields, int spin,
+                          void *qu, void *workspace, size_t workspace_bytes, void *stream);
+
+/*
  * Spin-0 analysis, glass/healpix.py:232-276 (healpy.map2alm with pol=False,
  * as called at glass/lensing.py:306), uniform pixel weights 4 pi / npix and
  * `niter` Jacobi refinements (healpy's default iter = 3).  maps: float64
