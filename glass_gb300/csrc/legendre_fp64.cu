@@ -126,6 +126,7 @@ k_leg_syn(const int npairs, const int nrings, const int lmax, const int64_t nalm
 //          N lm = (2 m / sin)(cot lam - dlam);              N = sqrt((l-1)l(l+1)(l+2))
 //   dlam = (l x lam - sqrt((2l+1)/(2l-1) (l^2-m^2)) lam_{l-1}) / sin.
 // Mirror ring: lp(pi-t) = (-1)^(l+m+s) lp(t), lm(pi-t) = -(-1)^(l+m+s) lm(t).
+template <bool HASB>
 __global__ void __launch_bounds__(LEG_THREADS)
 k_leg_syn_spin(const int npairs, const int nrings, const int lmax, const int spin,
                const double *__restrict__ cth, const double *__restrict__ sth,
@@ -136,7 +137,12 @@ k_leg_syn_spin(const int npairs, const int nrings, const int lmax, const int spi
     const int m = blockIdx.y;
     const int p = blockIdx.x * LEG_THREADS + threadIdx.x;
     const bool active = p < npairs;
-    __shared__ double2 e_s[LEG_CHUNK], b_s[LEG_CHUNK], c_s[LEG_CHUNK];
+    // per l of the chunk: alm, recurrence coefficients, and the l-only
+    // factors of lambda^+- (sqrt((2l+1)/(2l-1) (l^2-m^2)), 1/N, l(l+1)),
+    // computed once per block instead of per ring (FP64 sqrt and division
+    // are slow)
+    __shared__ double2 e_s[LEG_CHUNK], b_s[HASB ? LEG_CHUNK : 1], c_s[LEG_CHUNK];
+    __shared__ double f_s[LEG_CHUNK], n_s[LEG_CHUNK], ll_s[LEG_CHUNK];
     const int pp = active ? p : npairs - 1;
     const double x = cth[pp], sn = sth[pp];
     const double isn = 1.0 / sn, cot = x * isn;
@@ -152,14 +158,21 @@ k_leg_syn_spin(const int npairs, const int nrings, const int lmax, const int spi
             for (int c = 0; c < 2; ++c) acc[a][b][c] = make_double2(0.0, 0.0);
     const int64_t base = mofs[m];
     const double fm = m;
+    const double m2i2 = 2.0 * fm * fm * isn * isn, m2i = 2.0 * fm * isn, mi = fm * isn;
     double lam_prev = 0.0;
     for (int l0 = m; l0 <= lmax; l0 += LEG_CHUNK) {
         const int cnt = min(LEG_CHUNK, lmax + 1 - l0);
         __syncthreads();
         for (int t = threadIdx.x; t < cnt; t += LEG_THREADS) {
             e_s[t] = elm[base + (l0 - m) + t];
-            b_s[t] = blm ? blm[base + (l0 - m) + t] : make_double2(0.0, 0.0);
+            if constexpr (HASB) b_s[t] = blm[base + (l0 - m) + t];
             c_s[t] = coef[base + (l0 - m) + t];
+            const double fl = l0 + t;
+            f_s[t] = fl >= 1.0 ? sqrt((2.0 * fl + 1.0) / (2.0 * fl - 1.0) * (fl * fl - fm * fm)) : 0.0;
+            n_s[t] = fl < spin ? 0.0
+                     : spin == 1 ? 1.0 / sqrt(fl * (fl + 1.0))
+                                 : 1.0 / sqrt((fl - 1.0) * fl * (fl + 1.0) * (fl + 2.0));
+            ll_s[t] = fl * (fl + 1.0);
         }
         __syncthreads();
         for (int j = 0; j < cnt; ++j) {
@@ -171,25 +184,25 @@ k_leg_syn_spin(const int npairs, const int nrings, const int lmax, const int spi
                 lam = rec_step(r, l, m, x, c_s[j]);
             }
             if (l >= spin && l >= 1) {
-                const double fl = l;
-                const double dlam =
-                    (fl * x * lam - sqrt((2.0 * fl + 1.0) / (2.0 * fl - 1.0) * (fl * fl - fm * fm)) * lam_prev) * isn;
+                const double dlam = ((double)l * x * lam - f_s[j] * lam_prev) * isn;
+                const double nrm = n_s[j];
                 double lp, lmv;
                 if (spin == 1) {
-                    const double nrm = 1.0 / sqrt(fl * (fl + 1.0));
                     lp = -dlam * nrm;
-                    lmv = fm * lam * isn * nrm;
+                    lmv = mi * lam * nrm;
                 } else {
-                    const double nrm = 1.0 / sqrt((fl - 1.0) * fl * (fl + 1.0) * (fl + 2.0));
-                    lp = (-2.0 * cot * dlam + (2.0 * fm * fm * isn * isn - fl * (fl + 1.0)) * lam) * nrm;
-                    lmv = (2.0 * fm * isn) * (cot * lam - dlam) * nrm;
+                    lp = (-2.0 * cot * dlam + (m2i2 - ll_s[j]) * lam) * nrm;
+                    lmv = m2i * (cot * lam - dlam) * nrm;
                 }
                 const int par = (l - m) & 1;
-                const double2 e = e_s[j], b = b_s[j];
+                const double2 e = e_s[j];
                 acc[par][0][0].x += lp * e.x;  acc[par][0][0].y += lp * e.y;
                 acc[par][1][0].x += lmv * e.x; acc[par][1][0].y += lmv * e.y;
-                acc[par][0][1].x += lp * b.x;  acc[par][0][1].y += lp * b.y;
-                acc[par][1][1].x += lmv * b.x; acc[par][1][1].y += lmv * b.y;
+                if constexpr (HASB) {
+                    const double2 b = b_s[j];
+                    acc[par][0][1].x += lp * b.x;  acc[par][0][1].y += lp * b.y;
+                    acc[par][1][1].x += lmv * b.x; acc[par][1][1].y += lmv * b.y;
+                }
             }
             lam_prev = lam;
         }
@@ -263,18 +276,38 @@ k_leg_ana(const int npairs, const int nrings, const int lmax, const int64_t nalm
             __syncthreads();
             for (int t = threadIdx.x; t < cnt; t += ANA_THREADS) c_s[t] = coef[base + (l0 - m) + t];
             __syncthreads();
-            for (int j = 0; j < cnt; ++j) {
-                const int l = l0 + j;
-                double lam = (l == m) ? (r.sc == 0 ? r.l1 : 0.0) : rec_step(r, l, m, x, c_s[j]);
-                if (!active) lam = 0.0;
-                const double2 g = ((l - m) & 1) ? gO : gE;
-                double vr = lam * g.x, vi = lam * g.y;
+            // 16 l at a time: every lane forms its ring pair's 16 products,
+            // then one butterfly reduction across the warp sums all 16 (each
+            // step keeps half of the values and trades the other half with
+            // the partner lane): 16 shuffles per 16 l and per component,
+            // instead of 5 per l.  Lane 2k ends with the sum of l0 + j0 + k.
+            for (int j0 = 0; j0 < cnt; j0 += 16) {
+                double vr[16], vi[16];
 #pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
-                    vr += __shfl_down_sync(0xffffffffu, vr, o);
-                    vi += __shfl_down_sync(0xffffffffu, vi, o);
+                for (int i = 0; i < 16; ++i) {
+                    const int j = j0 + i, l = l0 + j;
+                    double lam = 0.0;
+                    if (j < cnt) lam = (l == m) ? (r.sc == 0 ? r.l1 : 0.0) : rec_step(r, l, m, x, c_s[j]);
+                    if (!active) lam = 0.0;
+                    const double2 g = (i & 1) ? gO : gE;  // l0 - m and j0 are even
+                    vr[i] = lam * g.x;
+                    vi[i] = lam * g.y;
                 }
-                if (lane == 0) part[warp][j] = make_double2(vr, vi);
+#pragma unroll
+                for (int h = 8; h >= 1; h >>= 1) {  // lane bit 4, 3, 2, 1
+                    const bool up = lane & (2 * h);
+#pragma unroll
+                    for (int i = 0; i < h; ++i) {
+                        const double kr = up ? vr[i + h] : vr[i], ki = up ? vi[i + h] : vi[i];
+                        const double sr = up ? vr[i] : vr[i + h], si = up ? vi[i] : vi[i + h];
+                        vr[i] = kr + __shfl_xor_sync(0xffffffffu, sr, 2 * h);
+                        vi[i] = ki + __shfl_xor_sync(0xffffffffu, si, 2 * h);
+                    }
+                }
+                const double tr = vr[0] + __shfl_xor_sync(0xffffffffu, vr[0], 1);
+                const double ti = vi[0] + __shfl_xor_sync(0xffffffffu, vi[0], 1);
+                const int k = lane >> 1;
+                if (!(lane & 1) && j0 + k < cnt) part[warp][j0 + k] = make_double2(tr, ti);
             }
             __syncthreads();
             for (int t = threadIdx.x; t < cnt; t += ANA_THREADS) {
@@ -336,9 +369,12 @@ int glg_launch_leg_syn_spin(const glg_plan *P, const double2 *elm, const double2
                             double2 *F, cudaStream_t st) {
     dim3 grid((P->npairs + LEG_THREADS - 1) / LEG_THREADS, P->mmax + 1);
     GLG_LAUNCH_SCOPE("k_leg_syn_spin", st);
-    k_leg_syn_spin<<<grid, LEG_THREADS, 0, st>>>(P->npairs, P->nrings, P->lmax, spin, P->cth,
-                                                 P->sth, P->mofs, P->coef, P->lmm, P->lmm_scale,
-                                                 elm, blm, F);
+    if (blm)
+        k_leg_syn_spin<true><<<grid, LEG_THREADS, 0, st>>>(P->npairs, P->nrings, P->lmax, spin, P->cth, P->sth,
+                                                           P->mofs, P->coef, P->lmm, P->lmm_scale, elm, blm, F);
+    else
+        k_leg_syn_spin<false><<<grid, LEG_THREADS, 0, st>>>(P->npairs, P->nrings, P->lmax, spin, P->cth, P->sth,
+                                                            P->mofs, P->coef, P->lmm, P->lmm_scale, elm, blm, F);
     GLG_CHECK_LAUNCH("k_leg_syn_spin");
     return GLG_OK;
 }

@@ -330,6 +330,69 @@ __device__ void fft_dif_adjoint(c32 *Z, const c32 *wh, int n) {
     for (int s = ns - 1; s >= 0; --s) pass_any<DIR, true, POW2>(Z, wh, n, r[s], Ls[s]);
 }
 
+// Power-of-two transforms of a compile-time length N: the same passes (16s,
+// then one 8, 4 or 2) with every index, shift and mask a constant.
+template <int R, int DIR, bool ADJ, bool ZV, int N, int L>
+__device__ __forceinline__ void pass_ct(c32 *Z, const c32 *wh, int nv) {
+    constexpr int msub = L / R, nbf = N / R, tsc = N / L;
+    constexpr bool by_blk = tsc >= 32;
+    constexpr int lg_tsc = __builtin_ctz(tsc), lg_msub = __builtin_ctz(msub);
+    for (int bf = threadIdx.x; bf < nbf; bf += blockDim.x) {
+        const int blk = by_blk ? bf & (tsc - 1) : bf >> lg_msub;
+        const int j1 = by_blk ? bf >> lg_tsc : bf & (msub - 1);
+        const int base = blk * L + j1;
+        const int ts = tsc * j1;
+        c32 v[R];
+        if constexpr (!ADJ) {
+#pragma unroll
+            for (int j = 0; j < R; ++j) {
+                if constexpr (ZV) v[j] = base + msub * j < nv ? Z[zi(base + msub * j)] : c32{0.f, 0.f};
+                else v[j] = Z[zi(base + msub * j)];
+            }
+            dft<R, DIR>(v, wh, N);
+            Z[zi(base)] = v[0];
+#pragma unroll
+            for (int k = 1; k < R; ++k) Z[zi(base + msub * k)] = cmul(v[k], tw<DIR>(wh, N, ts * k));
+        } else {
+            v[0] = Z[zi(base)];
+#pragma unroll
+            for (int k = 1; k < R; ++k) v[k] = cmul(Z[zi(base + msub * k)], tw<-DIR>(wh, N, ts * k));
+            dft<R, -DIR>(v, wh, N);
+#pragma unroll
+            for (int j = 0; j < R; ++j) Z[zi(base + msub * j)] = v[j];
+        }
+    }
+    __syncthreads();
+}
+
+template <int L>
+struct RadixOf {
+    static constexpr int value = L % 16 == 0 ? 16 : L;
+};
+
+// DIF passes from sub-length L down; the first pass reads zeros at and
+// beyond nv when ZV; SKIP2: a last radix-2 pass is left to the caller.
+template <int DIR, int N, int L, bool ZV, bool SKIP2>
+__device__ __forceinline__ void dif_ct(c32 *Z, const c32 *wh, int nv) {
+    if constexpr (L > 1) {
+        constexpr int R = RadixOf<L>::value;
+        if constexpr (!(SKIP2 && L == 2 && R == 2 && N > 2)) {
+            pass_ct<R, DIR, false, ZV, N, L>(Z, wh, nv);
+            dif_ct<DIR, N, L / R, false, SKIP2>(Z, wh, nv);
+        }
+    }
+}
+
+// The adjoint of dif_ct<DIR, N, L>: its passes in reverse order.
+template <int DIR, int N, int L>
+__device__ __forceinline__ void adj_ct(c32 *Z, const c32 *wh) {
+    if constexpr (L > 1) {
+        constexpr int R = RadixOf<L>::value;
+        adj_ct<DIR, N, L / R>(Z, wh);
+        pass_ct<R, DIR, true, false, N, L>(Z, wh, 0);
+    }
+}
+
 // ------------------------------------------------------------- epilogue
 
 __device__ __forceinline__ float epi(float v, int kind, float hv, float lam) {
@@ -502,7 +565,8 @@ __device__ void fold(const float2 *FN, const float2 *FS, bool equator, int n, in
 // Class 0 (any n) and class 2 (power-of-two equatorial n, POW2: radices
 // 16/8/4/2 only):
 // mixed-radix DIF.  smem: Z | SS (n <= mmax) | X[2T] | wh[zi(n/2) + 1].
-template <bool POW2>
+// LOGN > 0 (class 2 only): the ring length is 2^LOGN, a compile-time constant.
+template <bool POW2, int LOGN = 0>
 __global__ void __launch_bounds__(POW2 ? TMAX_POW2 : TMAX) k_ring32(const RingArgs a, const Epi32 e) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int map = blockIdx.x % a.nmaps;
@@ -523,10 +587,18 @@ __global__ void __launch_bounds__(POW2 ? TMAX_POW2 : TMAX) k_ring32(const RingAr
     fold(FN, FS, equator, n, a.mmax, a.half[p], w2n, nullptr, Z, SS, 0, X);
     // a last DIF pass of radix 2 (L = 2: no twiddles) is folded into the
     // output gather: frequency at storage slot s is Z[s & ~1] +- Z[s | 1]
-    int rr[GLG_MAX_FFT_STAGES];
-    const int nst = glg_fft32_radices(n, rr);
-    const bool last2 = POW2 && nst > 1 && rr[nst - 1] == 2;
-    fft_dif<1, POW2>(Z, wh, n, -1, last2);
+    bool last2;
+    if constexpr (LOGN > 0) {
+        constexpr int N = 1 << LOGN;
+        // the passes are 16s then one 8/4/2: the last is radix 2 when log2(N) % 4 == 1
+        last2 = LOGN > 1 && LOGN % 4 == 1;
+        dif_ct<1, N, N, false, true>(Z, wh, 0);
+    } else {
+        int rr[GLG_MAX_FFT_STAGES];
+        const int nst = glg_fft32_radices(n, rr);
+        last2 = POW2 && nst > 1 && rr[nst - 1] == 2;
+        fft_dif<1, POW2>(Z, wh, n, -1, last2);
+    }
     const uint16_t *pos = a.pos16 + a.pos_ofs[i4];
     float *mp = a.maps + (int64_t)map * a.npix;
     const int64_t sN = a.startN[p], sS = a.startS[p];
@@ -569,6 +641,7 @@ __global__ void __launch_bounds__(POW2 ? TMAX_POW2 : TMAX) k_ring32(const RingAr
 // Bluestein transform of ring pair p, map `map`, in buffer Z (shared or
 // global memory) with the padded twiddle table wh of its length M and the
 // partial-sum scratch X (2 x blockDim).  Ends with the stores.
+template <int LOGM = 0>
 __device__ __forceinline__ void blu_ring(const RingArgs &a, const Epi32 &e, int map, int p, c32 *Z, c32 *X,
                                          const c32 *wh) {
     const int n = a.nph[p], i4 = n / 4, T = blockDim.x;
@@ -580,12 +653,18 @@ __device__ __forceinline__ void blu_ring(const RingArgs &a, const Epi32 &e, int 
     const float2 *FN = a.Ft + ((int64_t)map * a.nrings + rn) * (a.mmax + 1);
     const float2 *FS = a.Ft + ((int64_t)map * a.nrings + rs) * (a.mmax + 1);
     fold(FN, FS, equator, n, a.mmax, a.half[p], w2n, chirp, Z, Z, n, X);
-    fft_dif<-1, true>(Z, wh, M, n);  // the padding beyond n is zero: not written, not read
+    if constexpr (LOGM > 0)  // the padding beyond n is zero: not written, not read
+        dif_ct<-1, (1 << LOGM), (1 << LOGM), true, false>(Z, wh, n);
+    else
+        fft_dif<-1, true>(Z, wh, M, n);
     const float2 *H = a.blu_H + a.blu_ofs[i4];
 #pragma unroll 8
     for (int k = threadIdx.x; k < M; k += T) Z[zi(k)] = cmul(Z[zi(k)], ldg(H + k));  // 8 loads in flight
     __syncthreads();
-    fft_dif_adjoint<-1, true>(Z, wh, M);
+    if constexpr (LOGM > 0)
+        adj_ct<-1, (1 << LOGM), (1 << LOGM)>(Z, wh);
+    else
+        fft_dif_adjoint<-1, true>(Z, wh, M);
     float *mp = a.maps + (int64_t)map * a.npix;
     const int64_t sN = a.startN[p], sS = a.startS[p];
     const int kind = e.kind[map];
@@ -623,6 +702,7 @@ __device__ __forceinline__ void blu_ring(const RingArgs &a, const Epi32 &e, int 
 
 // Class 1: Bluestein.  smem: Z[M] (the south fold scratch sits at n..2n-1) |
 // X[2T] | wh[zi(M/2) + 1].
+template <int LOGM>
 __global__ void __launch_bounds__(TMAX_POW2) k_ring32_blu(const RingArgs a, const Epi32 e) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int map = blockIdx.x % a.nmaps;
@@ -633,7 +713,7 @@ __global__ void __launch_bounds__(TMAX_POW2) k_ring32_blu(const RingArgs a, cons
     c32 *wh = X + 2 * T;
     const int stride = a.Mmax / M;
     for (int t = threadIdx.x; t <= M / 2; t += T) wh[zi(t)] = ldg(a.twM + (int64_t)t * stride);
-    blu_ring(a, e, map, p, Z, X, wh);
+    blu_ring<LOGM>(a, e, map, p, Z, X, wh);
 }
 
 // Class 3: Bluestein lengths too large for shared memory (M = 32768, the
@@ -647,7 +727,7 @@ __global__ void __launch_bounds__(TMAX_POW2) k_ring32_blug(const RingArgs a, con
     c32 *Z = reinterpret_cast<c32 *>(a.gz) + (int64_t)blockIdx.x * glg_zsize(a.Mmax);
     const c32 *wh = reinterpret_cast<const c32 *>(a.twMp);
     for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
-        blu_ring(a, e, item % a.nmaps, a.pairs[item / a.nmaps], Z, X, wh);
+        blu_ring<0>(a, e, item % a.nmaps, a.pairs[item / a.nmaps], Z, X, wh);
         __syncthreads();  // the buffer is reused by the block's next item
     }
 }
@@ -755,6 +835,17 @@ static void ring_args(const glg_plan *P, const float2 *Ft, int nmaps, float *map
     a.npix = P->npix;
 }
 
+typedef void (*RingKernel)(const RingArgs, const Epi32);
+// Bluestein kernels by log2 M (3 .. 14) and equatorial kernels by log2 n (2 .. 14).
+static const RingKernel kBlu[15] = {nullptr,           nullptr,           nullptr,           k_ring32_blu<3>,
+                                    k_ring32_blu<4>,   k_ring32_blu<5>,   k_ring32_blu<6>,   k_ring32_blu<7>,
+                                    k_ring32_blu<8>,   k_ring32_blu<9>,   k_ring32_blu<10>,  k_ring32_blu<11>,
+                                    k_ring32_blu<12>,  k_ring32_blu<13>,  k_ring32_blu<14>};
+static const RingKernel kEq[15] = {nullptr,            nullptr,            k_ring32<true, 2>,  k_ring32<true, 3>,
+                                   k_ring32<true, 4>,  k_ring32<true, 5>,  k_ring32<true, 6>,  k_ring32<true, 7>,
+                                   k_ring32<true, 8>,  k_ring32<true, 9>,  k_ring32<true, 10>, k_ring32<true, 11>,
+                                   k_ring32<true, 12>, k_ring32<true, 13>, k_ring32<true, 14>};
+
 // Pairs lo .. lo+count-1 of bucket B (the whole bucket by default).
 static int launch_bucket(const glg_plan *P, const glg_ring_bucket &B, int threads, RingArgs a, const Epi32 &e,
                          cudaStream_t st, int lo = 0, int count = -1) {
@@ -774,14 +865,22 @@ static int launch_bucket(const glg_plan *P, const glg_ring_bucket &B, int thread
         k_ring32_blug<<<g3, threads, smem, st>>>(a, e, (int)grid);
         GLG_CHECK_LAUNCH("k_ring32_blug");
     } else if (B.kind == 1) {
-        cudaFuncSetAttribute(k_ring32_blu, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        const int lg = __builtin_ctz((unsigned)B.size);
+        if (B.size != (1 << lg) || lg < 3 || lg > 14) {
+            glg_set_error("fast ring FFT: Bluestein length outside 2^3 .. 2^14");
+            return GLG_ERR_UNSUPPORTED;
+        }
+        const RingKernel kern = kBlu[lg];
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         GLG_LAUNCH_SCOPE("k_ring32_blu", st);
-        k_ring32_blu<<<grid, threads, smem, st>>>(a, e);
+        kern<<<grid, threads, smem, st>>>(a, e);
         GLG_CHECK_LAUNCH("k_ring32_blu");
     } else if (B.kind == 2) {
-        cudaFuncSetAttribute(k_ring32<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        const int lg = __builtin_ctz((unsigned)B.size);
+        const RingKernel kern = (B.size == (1 << lg) && lg >= 2 && lg <= 14) ? kEq[lg] : k_ring32<true, 0>;
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         GLG_LAUNCH_SCOPE("k_ring32", st);
-        k_ring32<true><<<grid, threads, smem, st>>>(a, e);
+        kern<<<grid, threads, smem, st>>>(a, e);
         GLG_CHECK_LAUNCH("k_ring32");
     } else {
         cudaFuncSetAttribute(k_ring32<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
