@@ -129,6 +129,11 @@ struct glg_plan {
     int blu_Mmax;
     float2 *twM;             // [blu_Mmax / 2 + 1] exp(2 pi i t / blu_Mmax)
     float2 *twMp;            // the same, padded (twMp[glg_zi(t)]), when blu_Mmax > 16384 (class 3)
+    // padded half twiddle tables e^{2 pi i t / L}, t <= L / 2, at twp[twp_ofs[log2 L] + glg_zi(t)]
+    // for L = 2^3 .. the largest power-of-two transform of the plan (each 16-byte aligned,
+    // copied whole into shared memory by the staged kernels)
+    float2 *twp;
+    int64_t twp_ofs[16];
 };
 
 // Radix passes of an FP32 ring FFT of length n (DIF order: 16s, then one 8,
@@ -205,6 +210,7 @@ struct glg_refine_list {
     int cap;
     int4 *items;
     float2 *gz;  // nside > 2048: the global transform buffers of Bluestein class 3
+    int *err;    // the call's status word (a staged copy's bounded wait that ran out), or null
 };
 // Class-3 buffers: GLG_RING_GSLOTS slices of glg_zsize(Mmax) complex values.
 #define GLG_RING_GSLOTS 304

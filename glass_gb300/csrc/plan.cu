@@ -233,7 +233,7 @@ extern "C" void glg_plan_destroy(glg_plan *P) {
                     P->fft_nst, P->tw_ofs,  P->tw,      P->cth32,  P->tw32,   P->coef32,
                     P->goff,  P->seeds,     P->lstart,  P->tfirst, P->bucket_pairs, P->chirp_ofs,
                     P->chirp, P->pos_ofs, P->pos16,   P->blu_ofs, P->blu_M,  P->blu_H,  P->twM,
-                    P->plm,   P->twMp, P->plm_spin[0][0], P->plm_spin[0][1], P->plm_spin[1][0],
+                    P->plm,   P->twMp, P->twp, P->plm_spin[0][0], P->plm_spin[0][1], P->plm_spin[1][0],
                     P->plm_spin[1][1], P->tfirst_spin[0], P->tfirst_spin[1]};
     for (void *q : ptrs)
         if (q) cudaFree(q);
@@ -619,6 +619,18 @@ static int build_fft32_tables(glg_plan *P, cudaStream_t st) {
     std::vector<float2> twM(Mmax / 2 + 1);
     for (int t = 0; t <= Mmax / 2; ++t)
         twM[t] = make_float2((float)cos(2.0 * M_PI * t / Mmax), (float)sin(2.0 * M_PI * t / Mmax));
+    // padded half tables of every power of two up to the largest transform
+    int lgmax = 3;
+    while ((1 << lgmax) < Mmax || (1 << lgmax) < 4 * nside) ++lgmax;
+    std::vector<float2> twp;
+    for (int lg = 0; lg < 16; ++lg) P->twp_ofs[lg] = -1;
+    for (int lg = 3; lg <= lgmax && lg < 16; ++lg) {
+        const int L = 1 << lg;
+        P->twp_ofs[lg] = (int64_t)twp.size();
+        twp.resize(twp.size() + ((glg_zsize(L / 2 + 1) + 1) & ~1) + 2, make_float2(0.f, 0.f));  // 16-byte sizes, slack
+        for (int t = 0; t <= L / 2; ++t)
+            twp[P->twp_ofs[lg] + glg_zi(t)] = make_float2((float)cos(2.0 * M_PI * t / L), (float)sin(2.0 * M_PI * t / L));
+    }
     std::vector<float2> twMp;  // padded copy for class 3 (read from global memory)
     if (Mmax > 16384) {
         twMp.assign((size_t)glg_zsize(Mmax / 2 + 1), make_float2(0.f, 0.f));
@@ -672,7 +684,7 @@ static int build_fft32_tables(glg_plan *P, cudaStream_t st) {
         (rc = dalloc(P, &P->pos_ofs, pos_ofs.size())) || (rc = dalloc(P, &P->pos16, pos16.size())) ||
         (rc = dalloc(P, &P->blu_ofs, blu_ofs.size())) || (rc = dalloc(P, &P->blu_M, blu_M.size())) ||
         (rc = dalloc(P, &P->blu_H, H.size())) || (rc = dalloc(P, &P->twM, twM.size())) ||
-        (!twMp.empty() && (rc = dalloc(P, &P->twMp, twMp.size()))) ||
+        (!twMp.empty() && (rc = dalloc(P, &P->twMp, twMp.size()))) || (rc = dalloc(P, &P->twp, twp.size())) ||
         (rc = dalloc(P, &P->chirp_ofs, chirp_ofs.size())) || (rc = dalloc(P, &P->chirp, chirp.size())))
         return rc;
     cudaError_t e = cudaSuccess;
@@ -690,6 +702,7 @@ static int build_fft32_tables(glg_plan *P, cudaStream_t st) {
     up(P->blu_H, H.data(), sizeof(float2) * H.size());
     up(P->twM, twM.data(), sizeof(float2) * twM.size());
     if (!twMp.empty()) up(P->twMp, twMp.data(), sizeof(float2) * twMp.size());
+    up(P->twp, twp.data(), sizeof(float2) * twp.size());
     up(P->chirp_ofs, chirp_ofs.data(), sizeof(int64_t) * chirp_ofs.size());
     up(P->chirp, chirp.data(), sizeof(float2) * chirp.size());
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // host vectors go out of scope

@@ -38,6 +38,7 @@
 #include <algorithm>
 
 #include "glg_internal.cuh"
+#include "tc_ptx.cuh"
 
 namespace {
 
@@ -451,6 +452,9 @@ struct RingArgs {
     const float2 *Ft;  // [map][ring][m]
     float *maps;
     int64_t npix;
+    const float2 *twp;   // padded half twiddle tables by log2 length (staged kernels)
+    int64_t twp_ofs[16];
+    int *err;            // status word for a staged copy that never arrived (or null)
 };
 
 __device__ __forceinline__ c32 pack(c32 bn, c32 bs) { return {bn.x - bs.y, bn.y + bs.x}; }
@@ -609,6 +613,138 @@ __global__ void __launch_bounds__(POW2 ? TMAX_POW2 : TMAX) k_ring32(const RingAr
     // which the CPU-GPU link takes better when the maps are host memory
 #pragma unroll 2
     for (int q = threadIdx.x; q < (n >> 2); q += T) {
+        const ushort4 ps = *reinterpret_cast<const ushort4 *>(pos + 4 * q);
+        auto at = [&](int sl) -> c32 {
+            if (!last2) return Z[zi(sl)];
+            const c32 u0 = Z[zi(sl & ~1)], u1 = Z[zi(sl | 1)];
+            return (sl & 1) ? csub(u0, u1) : cadd(u0, u1);
+        };
+        const c32 v0 = at(ps.x), v1 = at(ps.y), v2 = at(ps.z), v3 = at(ps.w);
+        if (kind == GLG_EPI_LOGNORMAL) {
+            refine_note(e, map, v0.x, rn, 4 * q);
+            refine_note(e, map, v1.x, rn, 4 * q + 1);
+            refine_note(e, map, v2.x, rn, 4 * q + 2);
+            refine_note(e, map, v3.x, rn, 4 * q + 3);
+            if (!equator) {
+                refine_note(e, map, v0.y, rs, 4 * q);
+                refine_note(e, map, v1.y, rs, 4 * q + 1);
+                refine_note(e, map, v2.y, rs, 4 * q + 2);
+                refine_note(e, map, v3.y, rs, 4 * q + 3);
+            }
+        }
+        *reinterpret_cast<float4 *>(mp + sN + 4 * q) =
+            make_float4(epi(v0.x, kind, hv, lam), epi(v1.x, kind, hv, lam), epi(v2.x, kind, hv, lam),
+                        epi(v3.x, kind, hv, lam));
+        if (!equator)
+            *reinterpret_cast<float4 *>(mp + sS + 4 * q) =
+                make_float4(epi(v0.y, kind, hv, lam), epi(v1.y, kind, hv, lam), epi(v2.y, kind, hv, lam),
+                            epi(v3.y, kind, hv, lam));
+    }
+}
+
+template <int CNT>
+struct ZSize {  // glg_zsize(CNT) as a constant
+    static constexpr int value = (CNT - 1) + ((CNT - 1) >> 4) + ((CNT - 1) >> 8) + 1;
+};
+constexpr uint32_t STAGE_WAIT_LIMIT = 1u << 24;  // polls of a staged copy (its data is plain HBM reads)
+
+// Class 2 (power-of-two equatorial rings, n = 2^LOGN > mmax) with staged
+// inputs: one thread bulk-copies the ring pair's two rows of Legendre sums
+// (mmax + 1 values each, from the 16-byte boundary at or below each row
+// start) into the raw bytes of the transform buffer and the padded half
+// twiddle table of n into its own slot, all on one mbarrier; the threads
+// then form the folded sequence in registers from shared memory (every
+// staged value is read before the first write) and run the compile-time DIF
+// passes.  T threads, n / 2 + 1 residue pairs in ceil((n/2+1)/T) per thread.
+// smem: Z[zsize(n)] | wh[zsize(n/2+1)], 16-byte aligned.
+template <int LOGN, int T>
+__global__ void __launch_bounds__(T, T <= 512 ? 2 : 1) k_ring32eq(const RingArgs a, const Epi32 e) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int N = 1 << LOGN, NZ = ZSize<N>::value, NW = ZSize<N / 2 + 1>::value;
+    constexpr int NI = (N / 2 + 1 + T - 1) / T;
+    constexpr uint32_t BW = (uint32_t)(((NW * 8) + 15) & ~15);
+    __shared__ __align__(8) uint64_t bar;
+    const int map = blockIdx.x % a.nmaps;
+    const int p = a.pairs[blockIdx.x / a.nmaps];
+    const int rn = p, rs = a.nrings - 1 - p;
+    const bool equator = rn == rs;
+    const int mm = a.mmax + 1;
+    c32 *Z = reinterpret_cast<c32 *>(smem_raw);
+    c32 *wh = Z + ((NZ + 1) & ~1);
+    const float2 *FN = a.Ft + ((int64_t)map * a.nrings + rn) * mm;
+    const float2 *FS = a.Ft + ((int64_t)map * a.nrings + rs) * mm;
+    const int oN = (int)((reinterpret_cast<uintptr_t>(FN) >> 3) & 1);
+    const int oS = (int)((reinterpret_cast<uintptr_t>(FS) >> 3) & 1);
+    const uint32_t bN = (uint32_t)(((oN + mm) * 8 + 15) & ~15);
+    const uint32_t bS = equator ? 0u : (uint32_t)(((oS + mm) * 8 + 15) & ~15);
+    const float2 *stN = reinterpret_cast<const float2 *>(smem_raw) + oN;
+    const float2 *stS = reinterpret_cast<const float2 *>(smem_raw + bN) + oS;
+    if (threadIdx.x == 0) {
+        glg_tc::mbar_init(&bar, 1);
+        glg_tc::fence_barrier_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        glg_tc::mbar_arrive_expect_tx(&bar, bN + bS + BW);
+        glg_tc::bulk_g2s(smem_raw, FN - oN, bN, &bar);
+        if (!equator) glg_tc::bulk_g2s(smem_raw + bN, FS - oS, bS, &bar);
+        glg_tc::bulk_g2s(wh, a.twp + a.twp_ofs[LOGN], BW, &bar);
+    }
+    if (!glg_tc::mbar_wait(&bar, 0, STAGE_WAIT_LIMIT)) {
+        if (threadIdx.x == 0 && a.err) atomicExch(a.err, GLG_ERR_TIMEOUT);
+        glg_tc::mbar_wait(&bar, 0, STAGE_WAIT_LIMIT);  // the copies in flight land before the block exits
+        return;
+    }
+    // residue pairs (k, n - k): Z_k and Z_{n-k} from F_k and F_{n-k} (one term each, n > mmax)
+    const float2 *w2n = a.tw32 + a.tw_ofs[N / 4];  // e^{i pi t / n}
+    const bool h = a.half[p] != 0;
+    const c32 one = {1.f, 0.f}, zero = {0.f, 0.f};
+    c32 z1[NI], z2[NI];
+#pragma unroll
+    for (int i = 0; i < NI; ++i) {
+        const int k = threadIdx.x + i * T;
+        z1[i] = z2[i] = zero;
+        if (k <= N / 2) {
+            const int k2 = k ? N - k : 0;
+            const float ck = k ? 1.f : 0.5f;
+            c32 fn = zero, fs = zero, gn = zero, gs = zero;
+            if (k < mm) {
+                fn = {stN[k].x, stN[k].y};
+                if (!equator) fs = {stS[k].x, stS[k].y};
+            }
+            if (k2 < mm) {
+                gn = {stN[k2].x, stN[k2].y};
+                if (!equator) gs = {stS[k2].x, stS[k2].y};
+            }
+            const c32 wk = h ? ldg(w2n + k) : one, wk2 = h ? ldg(w2n + k2) : one;
+            const c32 an = cscale(fn, ck), as = cscale(fs, ck), bn = cscale(gn, ck), bs = cscale(gs, ck);
+            const c32 BN = cadd(cmul(wk, an), cconj(cmul(wk2, bn)));
+            const c32 BS = cadd(cmul(wk, as), cconj(cmul(wk2, bs)));
+            z1[i] = pack(BN, BS);
+            if (k2 != k)
+                z2[i] = pack(cadd(cmul(wk2, gn), cconj(cmul(wk, fn))), cadd(cmul(wk2, gs), cconj(cmul(wk, fs))));
+        }
+    }
+    __syncthreads();  // every staged value is in registers
+#pragma unroll
+    for (int i = 0; i < NI; ++i) {
+        const int k = threadIdx.x + i * T;
+        if (k <= N / 2) {
+            Z[zi(k)] = z1[i];
+            if (k && k != N / 2) Z[zi(N - k)] = z2[i];
+        }
+    }
+    __syncthreads();
+    constexpr bool last2 = LOGN > 1 && LOGN % 4 == 1;
+    dif_ct<1, N, N, false, true>(Z, wh, 0);
+    const int i4 = N / 4;
+    const uint16_t *pos = a.pos16 + a.pos_ofs[i4];
+    float *mp = a.maps + (int64_t)map * a.npix;
+    const int64_t sN = a.startN[p], sS = a.startS[p];
+    const int kind = e.kind[map];
+    const float hv = e.hvar[map], lam = e.lam[map];
+#pragma unroll 2
+    for (int q = threadIdx.x; q < N / 4; q += T) {
         const ushort4 ps = *reinterpret_cast<const ushort4 *>(pos + 4 * q);
         auto at = [&](int sl) -> c32 {
             if (!last2) return Z[zi(sl)];
@@ -833,6 +969,9 @@ static void ring_args(const glg_plan *P, const float2 *Ft, int nmaps, float *map
     a.Ft = Ft;
     a.maps = maps;
     a.npix = P->npix;
+    a.twp = P->twp;
+    for (int k = 0; k < 16; ++k) a.twp_ofs[k] = P->twp_ofs[k];
+    a.err = nullptr;
 }
 
 typedef void (*RingKernel)(const RingArgs, const Epi32);
@@ -845,6 +984,22 @@ static const RingKernel kEq[15] = {nullptr,            nullptr,            k_rin
                                    k_ring32<true, 4>,  k_ring32<true, 5>,  k_ring32<true, 6>,  k_ring32<true, 7>,
                                    k_ring32<true, 8>,  k_ring32<true, 9>,  k_ring32<true, 10>, k_ring32<true, 11>,
                                    k_ring32<true, 12>, k_ring32<true, 13>, k_ring32<true, 14>};
+
+// Staged equatorial kernels by log2 n (10 .. 14): 512 threads, 1024 at 2^14.
+static const RingKernel kEqStaged[15] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                                         nullptr, nullptr, k_ring32eq<10, 512>, k_ring32eq<11, 512>,
+                                         k_ring32eq<12, 512>, k_ring32eq<13, 512>, k_ring32eq<14, 1024>};
+static size_t eq_staged_smem(int n) {
+    return sizeof(float2) * (size_t)(((glg_zsize(n) + 1) & ~1) + ((glg_zsize(n / 2 + 1) + 1) & ~1) + 2);
+}
+// The staged kernel takes a power-of-two bucket of 2^10 .. 2^14 when n > mmax
+// and the two staged rows fit the transform buffer.
+static bool staged_eq_ok(const glg_plan *P, const glg_ring_bucket &B) {
+    const int n = B.size, lg = __builtin_ctz((unsigned)n);
+    if (n != (1 << lg) || lg < 10 || lg > 14 || n <= P->mmax || !P->twp || P->twp_ofs[lg] < 0) return false;
+    const size_t rows = 2 * (((size_t)(P->mmax + 2) * 8 + 15) & ~(size_t)15);
+    return rows <= sizeof(float2) * (size_t)glg_zsize(n) && eq_staged_smem(n) <= 227 * 1024;
+}
 
 // Pairs lo .. lo+count-1 of bucket B (the whole bucket by default).
 static int launch_bucket(const glg_plan *P, const glg_ring_bucket &B, int threads, RingArgs a, const Epi32 &e,
@@ -875,6 +1030,15 @@ static int launch_bucket(const glg_plan *P, const glg_ring_bucket &B, int thread
         GLG_LAUNCH_SCOPE("k_ring32_blu", st);
         kern<<<grid, threads, smem, st>>>(a, e);
         GLG_CHECK_LAUNCH("k_ring32_blu");
+    } else if (B.kind == 2 && staged_eq_ok(P, B)) {
+        const int lg = __builtin_ctz((unsigned)B.size);
+        const int T = lg >= 14 ? 1024 : 512;
+        const RingKernel kern = kEqStaged[lg];
+        const size_t sm = eq_staged_smem(B.size);
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        GLG_LAUNCH_SCOPE("k_ring32", st);
+        kern<<<grid, T, sm, st>>>(a, e);
+        GLG_CHECK_LAUNCH("k_ring32");
     } else if (B.kind == 2) {
         const int lg = __builtin_ctz((unsigned)B.size);
         const RingKernel kern = (B.size == (1 << lg) && lg >= 2 && lg <= 14) ? kEq[lg] : k_ring32<true, 0>;
@@ -990,6 +1154,7 @@ int glg_launch_ring_syn_f32_range(const glg_plan *P, const float2 *F, float2 *Ft
     e.rcap = rl ? rl->cap : 0;
     e.ritems = rl ? rl->items : nullptr;
     a.gz = rl ? rl->gz : nullptr;
+    a.err = rl ? rl->err : nullptr;
     const bool whole = p0 == 0 && p1 == P->npairs;
     for (int b = 0; b < P->nbuckets; ++b) {
         const glg_ring_bucket &B = P->buckets[b];

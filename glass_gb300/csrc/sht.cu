@@ -70,6 +70,7 @@ FastWs fast_ws(const glg_plan *P, int nmaps, void *ws) {
     c += up256(sizeof(int4) * (size_t)w.rl.cap);
     const size_t gzb = glg_ring_gz_bytes(P->nside);
     w.rl.gz = gzb ? (float2 *)c : nullptr;
+    w.rl.err = w.err;
     c += up256(gzb);
     w.end = c;
     return w;

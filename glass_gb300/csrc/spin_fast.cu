@@ -90,6 +90,7 @@ SpinWs spin_ws(const glg_plan *P, int nf, bool hasb, void *ws) {
     const size_t gzb = glg_ring_gz_bytes(P->nside);
     w.gz = gzb ? (float2 *)c : nullptr;
     c += up256(gzb);
+    c += 256;  // slack: the staged ring FFTs copy whole 16-byte words around each row of Ft
     w.end = c;
     return w;
 }
@@ -137,7 +138,7 @@ extern "C" int glg_alm2map_spin_fast(const glg_plan *P, const void *elm, const v
                                                      (spin & 1) ? -1.f : 1.f);
         GLG_CHECK_LAUNCH("k_spin_combine");
     }
-    glg_refine_list rl{nullptr, 0, nullptr, w.gz};
+    glg_refine_list rl{nullptr, 0, nullptr, w.gz, w.err};
     return glg_launch_ring_syn_f32_range(P, nullptr, w.Ft, 2 * nfields, (float *)qu, nullptr, 0, P->npairs, &rl,
                                          st);
 }
