@@ -779,7 +779,7 @@ __global__ void __launch_bounds__(T, T <= 512 ? 2 : 1) k_ring32eq(const RingArgs
 // partial-sum scratch X (2 x blockDim).  Ends with the stores.
 template <int LOGM = 0>
 __device__ __forceinline__ void blu_ring(const RingArgs &a, const Epi32 &e, int map, int p, c32 *Z, c32 *X,
-                                         const c32 *wh) {
+                                         const c32 *wh, bool folded = false) {
     const int n = a.nph[p], i4 = n / 4, T = blockDim.x;
     const int M = a.blu_M[i4];
     const float2 *w2n = a.tw32 + a.tw_ofs[i4];
@@ -788,7 +788,7 @@ __device__ __forceinline__ void blu_ring(const RingArgs &a, const Epi32 &e, int 
     const bool equator = rn == rs;
     const float2 *FN = a.Ft + ((int64_t)map * a.nrings + rn) * (a.mmax + 1);
     const float2 *FS = a.Ft + ((int64_t)map * a.nrings + rs) * (a.mmax + 1);
-    fold(FN, FS, equator, n, a.mmax, a.half[p], w2n, chirp, Z, Z, n, X);
+    if (!folded) fold(FN, FS, equator, n, a.mmax, a.half[p], w2n, chirp, Z, Z, n, X);
     if constexpr (LOGM > 0)  // the padding beyond n is zero: not written, not read
         dif_ct<-1, (1 << LOGM), (1 << LOGM), true, false>(Z, wh, n);
     else
@@ -834,6 +834,145 @@ __device__ __forceinline__ void blu_ring(const RingArgs &a, const Epi32 &e, int 
                 make_float4(epi(v0.y, kind, hv, lam), epi(v1.y, kind, hv, lam), epi(v2.y, kind, hv, lam),
                             epi(v3.y, kind, hv, lam));
     }
+}
+
+// The Bluestein fold of blu_ring (chirp included) from rows staged in
+// shared memory (stN, stS: element m of the north / south row; they occupy
+// the raw bytes of Z): every staged value is read into registers before Z
+// is written.  n >= blockDim.x.  NI, NK: register slots of the one-term
+// residue pairs (n > mmax) and of the signed multi-term fold (n <= mmax).
+template <int NI, int NK>
+__device__ __forceinline__ void fold_staged(const float2 *stN, const float2 *stS, bool equator, int n, int mmax,
+                                            int h, const float2 *w2n, const float2 *chirp, c32 *Z) {
+    const int T = blockDim.x, t = threadIdx.x;
+    const c32 one = {1.f, 0.f}, zero = {0.f, 0.f};
+    auto ld = [](const float2 *q, int m) -> c32 { return {q[m].x, q[m].y}; };
+    if (n > mmax) {  // at most one term per residue: pairs (k, n - k) from the same two values
+        c32 z1[NI], z2[NI];
+#pragma unroll
+        for (int i = 0; i < NI; ++i) {
+            const int k = t + i * T;
+            z1[i] = z2[i] = zero;
+            if (k <= (n >> 1)) {
+                const int k2 = k ? n - k : 0;
+                const float ck = k ? 1.f : 0.5f;
+                c32 fn = zero, fs = zero, gn = zero, gs = zero;
+                if (k <= mmax) {
+                    fn = ld(stN, k);
+                    if (!equator) fs = ld(stS, k);
+                }
+                if (k2 <= mmax) {
+                    gn = ld(stN, k2);
+                    if (!equator) gs = ld(stS, k2);
+                }
+                const c32 wk = h ? ldg(w2n + k) : one, wk2 = h ? ldg(w2n + k2) : one;
+                const c32 an = cscale(fn, ck), as = cscale(fs, ck), bn = cscale(gn, ck), bs = cscale(gs, ck);
+                const c32 BN = cadd(cmul(wk, an), cconj(cmul(wk2, bn)));
+                const c32 BS = cadd(cmul(wk, as), cconj(cmul(wk2, bs)));
+                z1[i] = cmul(pack(BN, BS), ldg(chirp + k));
+                if (k2 != k)
+                    z2[i] = cmul(pack(cadd(cmul(wk2, gn), cconj(cmul(wk, fn))), cadd(cmul(wk2, gs), cconj(cmul(wk, fs)))),
+                                 ldg(chirp + k2));
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < NI; ++i) {
+            const int k = t + i * T;
+            if (k <= (n >> 1)) {
+                Z[zi(k)] = z1[i];
+                if (k && 2 * k != n) Z[zi(n - k)] = z2[i];
+            }
+        }
+        __syncthreads();
+        return;
+    }
+    // signed fold S_k, one thread per residue (the order of fold's sums)
+    const float sgn = h ? -1.f : 1.f;
+    c32 sn[NK], ss[NK];
+#pragma unroll
+    for (int i = 0; i < NK; ++i) {
+        const int k = t + i * T;
+        sn[i] = ss[i] = zero;
+        if (k < n) {
+            float s = 1.f;
+            for (int m = k; m <= mmax; m += n, s *= sgn) {
+                const float c = m ? s : 0.5f * s;
+                const c32 fn = ld(stN, m), fs = ld(equator ? stN : stS, m);
+                sn[i] = {fmaf(c, fn.x, sn[i].x), fmaf(c, fn.y, sn[i].y)};
+                ss[i] = {fmaf(c, fs.x, ss[i].x), fmaf(c, fs.y, ss[i].y)};
+            }
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < NK; ++i) {
+        const int k = t + i * T;
+        if (k < n) {
+            Z[zi(k)] = sn[i];
+            Z[zi(n + k)] = ss[i];
+        }
+    }
+    __syncthreads();
+    // combine the residue pair (k, n - k), as fold does
+    for (int k = t; k <= (n >> 1); k += T) {
+        const int k2 = k ? n - k : 0;
+        const c32 an = Z[zi(k)], bn = Z[zi(k2)];
+        c32 as = Z[zi(n + k)], bs = Z[zi(n + k2)];
+        if (equator) as = bs = zero;
+        const c32 wk = h ? ldg(w2n + k) : one, wk2 = h ? ldg(w2n + k2) : one;
+        const c32 pa = cmul(wk, an), pb = cmul(wk2, bn), qa = cmul(wk, as), qb = cmul(wk2, bs);
+        const c32 z = cmul(pack(cadd(pa, cconj(pb)), cadd(qa, cconj(qb))), ldg(chirp + k));
+        Z[zi(k)] = z;
+        if (k2 != k) Z[zi(k2)] = cmul(pack(cadd(pb, cconj(pa)), cadd(qb, cconj(qa))), ldg(chirp + k2));
+    }
+    __syncthreads();
+}
+
+// Class 1 for M = 2^13, 2^14 with staged inputs (as k_ring32eq): the ring
+// pair's rows of Legendre sums and the padded half twiddle table of M
+// bulk-copied into shared memory on one mbarrier, then the fold from shared
+// memory and blu_ring's transforms.  smem: Z[zsize(M)] | wh[zsize(M/2+1)].
+template <int LOGM, int T>
+__global__ void __launch_bounds__(T, T <= 512 ? 2 : 1) k_ring32_blus(const RingArgs a, const Epi32 e) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int M = 1 << LOGM, NZ = ZSize<M>::value, NW = ZSize<M / 2 + 1>::value;
+    constexpr int NI = (M / 4 + 1 + T - 1) / T, NK = (M / 2 + T - 1) / T;
+    constexpr uint32_t BW = (uint32_t)(((NW * 8) + 15) & ~15);
+    __shared__ __align__(8) uint64_t bar;
+    const int map = blockIdx.x % a.nmaps;
+    const int p = a.pairs[blockIdx.x / a.nmaps];
+    const int rn = p, rs = a.nrings - 1 - p;
+    const bool equator = rn == rs;
+    const int mm = a.mmax + 1, n = a.nph[p], i4 = n / 4;
+    c32 *Z = reinterpret_cast<c32 *>(smem_raw);
+    c32 *wh = Z + ((NZ + 1) & ~1);
+    const float2 *FN = a.Ft + ((int64_t)map * a.nrings + rn) * mm;
+    const float2 *FS = a.Ft + ((int64_t)map * a.nrings + rs) * mm;
+    const int oN = (int)((reinterpret_cast<uintptr_t>(FN) >> 3) & 1);
+    const int oS = (int)((reinterpret_cast<uintptr_t>(FS) >> 3) & 1);
+    const uint32_t bN = (uint32_t)(((oN + mm) * 8 + 15) & ~15);
+    const uint32_t bS = equator ? 0u : (uint32_t)(((oS + mm) * 8 + 15) & ~15);
+    if (threadIdx.x == 0) {
+        glg_tc::mbar_init(&bar, 1);
+        glg_tc::fence_barrier_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        glg_tc::mbar_arrive_expect_tx(&bar, bN + bS + BW);
+        glg_tc::bulk_g2s(smem_raw, FN - oN, bN, &bar);
+        if (!equator) glg_tc::bulk_g2s(smem_raw + bN, FS - oS, bS, &bar);
+        glg_tc::bulk_g2s(wh, a.twp + a.twp_ofs[LOGM], BW, &bar);
+    }
+    if (!glg_tc::mbar_wait(&bar, 0, STAGE_WAIT_LIMIT)) {
+        if (threadIdx.x == 0 && a.err) atomicExch(a.err, GLG_ERR_TIMEOUT);
+        glg_tc::mbar_wait(&bar, 0, STAGE_WAIT_LIMIT);  // the copies in flight land before the block exits
+        return;
+    }
+    fold_staged<NI, NK>(reinterpret_cast<const float2 *>(smem_raw) + oN,
+                        reinterpret_cast<const float2 *>(smem_raw + bN) + oS, equator, n, a.mmax, a.half[p],
+                        a.tw32 + a.tw_ofs[i4], a.chirp + a.chirp_ofs[i4], Z);
+    blu_ring<LOGM>(a, e, map, p, Z, nullptr, wh, true);
 }
 
 // Class 1: Bluestein.  smem: Z[M] (the south fold scratch sits at n..2n-1) |
@@ -1001,6 +1140,23 @@ static bool staged_eq_ok(const glg_plan *P, const glg_ring_bucket &B) {
     return rows <= sizeof(float2) * (size_t)glg_zsize(n) && eq_staged_smem(n) <= 227 * 1024;
 }
 
+// The staged Bluestein kernels take M = 2^13 (512 threads) and 2^14 (1024)
+// when the two staged rows fit the transform buffer and every ring of the
+// bucket has at least as many pixels as the block has threads.
+static bool staged_blu_ok(const glg_plan *P, const glg_ring_bucket &B, int count) {
+    const int M = B.size;
+    if ((M != 8192 && M != 16384) || !P->twp || P->twp_ofs[M == 8192 ? 13 : 14] < 0 || count <= 0) return false;
+    const int T = M == 8192 ? 512 : 1024;
+    const int *bp = P->bucket_pairs_host + B.first;
+    for (int i = 0; i < B.count; ++i) {
+        const int p = bp[i];
+        const int ring = p + 1 < P->nside ? p + 1 : P->nside;  // north ring p + 1 has 4 min(p + 1, nside) pixels
+        if (4 * ring < T) return false;
+    }
+    const size_t rows = 2 * (((size_t)(P->mmax + 2) * 8 + 15) & ~(size_t)15);
+    return rows <= sizeof(float2) * (size_t)glg_zsize(M) && eq_staged_smem(M) <= 227 * 1024;
+}
+
 // Pairs lo .. lo+count-1 of bucket B (the whole bucket by default).
 static int launch_bucket(const glg_plan *P, const glg_ring_bucket &B, int threads, RingArgs a, const Epi32 &e,
                          cudaStream_t st, int lo = 0, int count = -1) {
@@ -1019,6 +1175,15 @@ static int launch_bucket(const glg_plan *P, const glg_ring_bucket &B, int thread
         GLG_LAUNCH_SCOPE("k_ring32_blug", st);
         k_ring32_blug<<<g3, threads, smem, st>>>(a, e, (int)grid);
         GLG_CHECK_LAUNCH("k_ring32_blug");
+    } else if (B.kind == 1 && staged_blu_ok(P, B, count)) {
+        const int lg = __builtin_ctz((unsigned)B.size);
+        const int T = lg >= 14 ? 1024 : 512;
+        const RingKernel kern = lg >= 14 ? k_ring32_blus<14, 1024> : k_ring32_blus<13, 512>;
+        const size_t sm = eq_staged_smem(B.size);
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        GLG_LAUNCH_SCOPE("k_ring32_blu", st);
+        kern<<<grid, T, sm, st>>>(a, e);
+        GLG_CHECK_LAUNCH("k_ring32_blu");
     } else if (B.kind == 1) {
         const int lg = __builtin_ctz((unsigned)B.size);
         if (B.size != (1 << lg) || lg < 3 || lg > 14) {
