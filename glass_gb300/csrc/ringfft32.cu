@@ -32,6 +32,7 @@
 // bucket, all maps of the call in one grid with the map index fastest, so the
 // blocks that share a ring's tables run together).
 #include <cuda_runtime.h>
+#include <type_traits>
 
 #include <math.h>
 
@@ -333,64 +334,152 @@ __device__ void fft_dif_adjoint(c32 *Z, const c32 *wh, int n) {
 
 // Power-of-two transforms of a compile-time length N: the same passes (16s,
 // then one 8, 4 or 2) with every index, shift and mask a constant.
-template <int R, int DIR, bool ADJ, bool ZV, int N, int L>
-__device__ __forceinline__ void pass_ct(c32 *Z, const c32 *wh, int nv) {
-    constexpr int msub = L / R, nbf = N / R, tsc = N / L;
-    constexpr bool by_blk = tsc >= 32;
-    constexpr int lg_tsc = __builtin_ctz(tsc), lg_msub = __builtin_ctz(msub);
-    for (int bf = threadIdx.x; bf < nbf; bf += blockDim.x) {
-        const int blk = by_blk ? bf & (tsc - 1) : bf >> lg_msub;
-        const int j1 = by_blk ? bf >> lg_tsc : bf & (msub - 1);
-        const int base = blk * L + j1;
-        const int ts = tsc * j1;
-        c32 v[R];
-        if constexpr (!ADJ) {
-#pragma unroll
-            for (int j = 0; j < R; ++j) {
-                if constexpr (ZV) v[j] = base + msub * j < nv ? Z[zi(base + msub * j)] : c32{0.f, 0.f};
-                else v[j] = Z[zi(base + msub * j)];
-            }
-            dft<R, DIR>(v, wh, N);
-            Z[zi(base)] = v[0];
-#pragma unroll
-            for (int k = 1; k < R; ++k) Z[zi(base + msub * k)] = cmul(v[k], tw<DIR>(wh, N, ts * k));
-        } else {
-            v[0] = Z[zi(base)];
-#pragma unroll
-            for (int k = 1; k < R; ++k) v[k] = cmul(Z[zi(base + msub * k)], tw<-DIR>(wh, N, ts * k));
-            dft<R, -DIR>(v, wh, N);
-#pragma unroll
-            for (int j = 0; j < R; ++j) Z[zi(base + msub * j)] = v[j];
-        }
-    }
-    __syncthreads();
-}
-
 template <int L>
 struct RadixOf {
     static constexpr int value = L % 16 == 0 ? 16 : L;
 };
 
+// Per-pass twiddle tables of a compile-time length N: for every DIF pass
+// below the first (sub-length L < N) with more than one butterfly column
+// (msub = L / R > 1), the R - 1 rows [k - 1][j1] of e^{2 pi i j1 k / L},
+// j1 < msub, so that a thread's twiddles sit at constant offsets from its
+// column and neighbouring threads read neighbouring words.  WTab<N, L>:
+// offset of pass L's rows, and the total size of the passes from L down.
+template <int N, int L>
+struct WTab {
+    static constexpr int R = L > 1 ? RadixOf<L>::value : 1;
+    static constexpr int own = (L < N && L > 1 && L / R > 1) ? (R - 1) * (L / R) : 0;
+    static constexpr int below = L > 1 ? WTab<N, L / R>::total : 0;
+    static constexpr int total = own + below;
+};
+template <int N>
+struct WTab<N, 1> {
+    static constexpr int R = 1, own = 0, below = 0, total = 0;
+};
+// offset of pass L's rows when the passes from N down are laid out in order
+template <int N, int L>
+struct WOfs {
+    static constexpr int value = WTab<N, N>::total - WTab<N, L>::total;
+};
+
+// Fill the per-pass tables from the padded half table wh (the same values
+// tw() gives, so the transforms are unchanged); ends with __syncthreads().
+template <int N, int L>
+__device__ __forceinline__ void wtab_fill_rec(c32 *wp, const c32 *wh) {
+    if constexpr (L > 1) {
+        constexpr int R = RadixOf<L>::value, msub = L / R, own = WTab<N, L>::own;
+        if constexpr (own > 0) {
+            c32 *w = wp + WOfs<N, L>::value;
+            for (int q = threadIdx.x; q < own; q += blockDim.x) {
+                const int k = q / msub + 1, j1 = q % msub;
+                w[q] = tw<1>(wh, N, (N / L) * j1 * k);
+            }
+        }
+        wtab_fill_rec<N, L / R>(wp, wh);
+    }
+}
+template <int N>
+__device__ __forceinline__ void wtab_fill(c32 *wp, const c32 *wh) {
+    wtab_fill_rec<N, N>(wp, wh);
+    __syncthreads();
+}
+
+template <int E>
+struct ZiC {  // glg_zi(E) as a constant
+    static constexpr int value = E + (E >> 4) + (E >> 8);
+};
+
+// cmul by w (DIR > 0) or by conj(w) (DIR < 0)
+template <int DIR>
+__device__ __forceinline__ c32 cmul_dir(c32 a, c32 w) {
+    return cmul(a, DIR > 0 ? w : cconj(w));
+}
+
+// Host copy of WTab<N, N>::total (entries of the per-pass tables of N).
+static int wtab_total_host(int N) {
+    int tot = 0;
+    for (int L = N; L > 1;) {
+        const int R = L % 16 == 0 ? 16 : L, msub = L / R;
+        if (L < N && msub > 1) tot += (R - 1) * msub;
+        L /= R;
+    }
+    return tot;
+}
+
+// One DIF pass (or its adjoint) of radix R, sub-length L, length N.  wp:
+// the per-pass tables of wtab_fill (null: twiddles from wh).  For msub >=
+// 16 the padded offsets of a butterfly's elements are constants from its
+// first (the column j1 < msub adds no carry into bits 4 and 8); for msub
+// == 1 every twiddle is 1.
+template <int R, int DIR, bool ADJ, bool ZV, int N, int L>
+__device__ __forceinline__ void pass_ct(c32 *Z, const c32 *wh, const c32 *wp, int nv) {
+    constexpr int msub = L / R, nbf = N / R, tsc = N / L;
+    constexpr bool by_blk = tsc >= 32;
+    constexpr int lg_tsc = __builtin_ctz(tsc), lg_msub = __builtin_ctz(msub);
+    constexpr bool cidx = msub >= 16;
+    constexpr bool unit = msub == 1;
+    const bool table = wp != nullptr && L < N && !unit;
+    const c32 *wl = table ? wp + WOfs<N, L>::value : nullptr;
+    for (int bf = threadIdx.x; bf < nbf; bf += blockDim.x) {
+        const int blk = by_blk ? bf & (tsc - 1) : bf >> lg_msub;
+        const int j1 = by_blk ? bf >> lg_tsc : bf & (msub - 1);
+        const int base = blk * L + j1;
+        const int ts = tsc * j1;
+        const int zb = zi(base);
+        c32 *zp = Z + zb;
+        // element j of the butterfly (j a constant once unrolled)
+        auto el = [&](int j) -> c32 & {
+            return cidx ? zp[msub * j + ((msub * j) >> 4) + ((msub * j) >> 8)] : Z[zi(base + msub * j)];
+        };
+        // a * e^{D 2 pi i ts k / N}
+        auto twm = [&](c32 a, int k, auto dtag) -> c32 {
+            constexpr int D = decltype(dtag)::value;
+            if (table) return cmul_dir<D>(a, wl[(k - 1) * msub + j1]);
+            return cmul(a, tw<D>(wh, N, ts * k));
+        };
+        c32 v[R];
+        if constexpr (!ADJ) {
+#pragma unroll
+            for (int j = 0; j < R; ++j) {
+                if constexpr (ZV) v[j] = base + msub * j < nv ? el(j) : c32{0.f, 0.f};
+                else v[j] = el(j);
+            }
+            dft<R, DIR>(v, wh, N);
+            el(0) = v[0];
+#pragma unroll
+            for (int k = 1; k < R; ++k) el(k) = unit ? v[k] : twm(v[k], k, std::integral_constant<int, DIR>{});
+        } else {
+            v[0] = el(0);
+#pragma unroll
+            for (int k = 1; k < R; ++k) v[k] = unit ? el(k) : twm(el(k), k, std::integral_constant<int, -DIR>{});
+            dft<R, -DIR>(v, wh, N);
+#pragma unroll
+            for (int j = 0; j < R; ++j) el(j) = v[j];
+        }
+    }
+    __syncthreads();
+}
+
 // DIF passes from sub-length L down; the first pass reads zeros at and
 // beyond nv when ZV; SKIP2: a last radix-2 pass is left to the caller.
 template <int DIR, int N, int L, bool ZV, bool SKIP2>
-__device__ __forceinline__ void dif_ct(c32 *Z, const c32 *wh, int nv) {
+__device__ __forceinline__ void dif_ct(c32 *Z, const c32 *wh, int nv, const c32 *wp = nullptr) {
     if constexpr (L > 1) {
         constexpr int R = RadixOf<L>::value;
         if constexpr (!(SKIP2 && L == 2 && R == 2 && N > 2)) {
-            pass_ct<R, DIR, false, ZV, N, L>(Z, wh, nv);
-            dif_ct<DIR, N, L / R, false, SKIP2>(Z, wh, nv);
+            pass_ct<R, DIR, false, ZV, N, L>(Z, wh, wp, nv);
+            dif_ct<DIR, N, L / R, false, SKIP2>(Z, wh, nv, wp);
         }
     }
 }
 
 // The adjoint of dif_ct<DIR, N, L>: its passes in reverse order.
 template <int DIR, int N, int L>
-__device__ __forceinline__ void adj_ct(c32 *Z, const c32 *wh) {
+__device__ __forceinline__ void adj_ct(c32 *Z, const c32 *wh, const c32 *wp = nullptr) {
     if constexpr (L > 1) {
         constexpr int R = RadixOf<L>::value;
-        adj_ct<DIR, N, L / R>(Z, wh);
-        pass_ct<R, DIR, true, false, N, L>(Z, wh, 0);
+        adj_ct<DIR, N, L / R>(Z, wh, wp);
+        pass_ct<R, DIR, true, false, N, L>(Z, wh, wp, 0);
     }
 }
 
@@ -671,6 +760,7 @@ __global__ void __launch_bounds__(T, T <= 512 ? 2 : 1) k_ring32eq(const RingArgs
     const int mm = a.mmax + 1;
     c32 *Z = reinterpret_cast<c32 *>(smem_raw);
     c32 *wh = Z + ((NZ + 1) & ~1);
+    c32 *wp = wh + ((NW + 1) & ~1);  // per-pass twiddle tables
     const float2 *FN = a.Ft + ((int64_t)map * a.nrings + rn) * mm;
     const float2 *FS = a.Ft + ((int64_t)map * a.nrings + rs) * mm;
     const int oN = (int)((reinterpret_cast<uintptr_t>(FN) >> 3) & 1);
@@ -695,6 +785,7 @@ __global__ void __launch_bounds__(T, T <= 512 ? 2 : 1) k_ring32eq(const RingArgs
         glg_tc::mbar_wait(&bar, 0, STAGE_WAIT_LIMIT);  // the copies in flight land before the block exits
         return;
     }
+    wtab_fill_rec<N, N>(wp, wh);  // the barrier before the transform's first pass publishes it
     // residue pairs (k, n - k): Z_k and Z_{n-k} from F_k and F_{n-k} (one term each, n > mmax)
     const float2 *w2n = a.tw32 + a.tw_ofs[N / 4];  // e^{i pi t / n}
     const bool h = a.half[p] != 0;
@@ -736,7 +827,7 @@ __global__ void __launch_bounds__(T, T <= 512 ? 2 : 1) k_ring32eq(const RingArgs
     }
     __syncthreads();
     constexpr bool last2 = LOGN > 1 && LOGN % 4 == 1;
-    dif_ct<1, N, N, false, true>(Z, wh, 0);
+    dif_ct<1, N, N, false, true>(Z, wh, 0, wp);
     const int i4 = N / 4;
     const uint16_t *pos = a.pos16 + a.pos_ofs[i4];
     float *mp = a.maps + (int64_t)map * a.npix;
@@ -779,7 +870,7 @@ __global__ void __launch_bounds__(T, T <= 512 ? 2 : 1) k_ring32eq(const RingArgs
 // partial-sum scratch X (2 x blockDim).  Ends with the stores.
 template <int LOGM = 0>
 __device__ __forceinline__ void blu_ring(const RingArgs &a, const Epi32 &e, int map, int p, c32 *Z, c32 *X,
-                                         const c32 *wh, bool folded = false) {
+                                         const c32 *wh, bool folded = false, const c32 *wp = nullptr) {
     const int n = a.nph[p], i4 = n / 4, T = blockDim.x;
     const int M = a.blu_M[i4];
     const float2 *w2n = a.tw32 + a.tw_ofs[i4];
@@ -790,7 +881,7 @@ __device__ __forceinline__ void blu_ring(const RingArgs &a, const Epi32 &e, int 
     const float2 *FS = a.Ft + ((int64_t)map * a.nrings + rs) * (a.mmax + 1);
     if (!folded) fold(FN, FS, equator, n, a.mmax, a.half[p], w2n, chirp, Z, Z, n, X);
     if constexpr (LOGM > 0)  // the padding beyond n is zero: not written, not read
-        dif_ct<-1, (1 << LOGM), (1 << LOGM), true, false>(Z, wh, n);
+        dif_ct<-1, (1 << LOGM), (1 << LOGM), true, false>(Z, wh, n, wp);
     else
         fft_dif<-1, true>(Z, wh, M, n);
     const float2 *H = a.blu_H + a.blu_ofs[i4];
@@ -798,7 +889,7 @@ __device__ __forceinline__ void blu_ring(const RingArgs &a, const Epi32 &e, int 
     for (int k = threadIdx.x; k < M; k += T) Z[zi(k)] = cmul(Z[zi(k)], ldg(H + k));  // 8 loads in flight
     __syncthreads();
     if constexpr (LOGM > 0)
-        adj_ct<-1, (1 << LOGM), (1 << LOGM)>(Z, wh);
+        adj_ct<-1, (1 << LOGM), (1 << LOGM)>(Z, wh, wp);
     else
         fft_dif_adjoint<-1, true>(Z, wh, M);
     float *mp = a.maps + (int64_t)map * a.npix;
@@ -947,6 +1038,7 @@ __global__ void __launch_bounds__(T, T <= 512 ? 2 : 1) k_ring32_blus(const RingA
     const int mm = a.mmax + 1, n = a.nph[p], i4 = n / 4;
     c32 *Z = reinterpret_cast<c32 *>(smem_raw);
     c32 *wh = Z + ((NZ + 1) & ~1);
+    c32 *wp = wh + ((NW + 1) & ~1);  // per-pass twiddle tables
     const float2 *FN = a.Ft + ((int64_t)map * a.nrings + rn) * mm;
     const float2 *FS = a.Ft + ((int64_t)map * a.nrings + rs) * mm;
     const int oN = (int)((reinterpret_cast<uintptr_t>(FN) >> 3) & 1);
@@ -969,10 +1061,11 @@ __global__ void __launch_bounds__(T, T <= 512 ? 2 : 1) k_ring32_blus(const RingA
         glg_tc::mbar_wait(&bar, 0, STAGE_WAIT_LIMIT);  // the copies in flight land before the block exits
         return;
     }
+    wtab_fill_rec<M, M>(wp, wh);  // published by the fold's barriers
     fold_staged<NI, NK>(reinterpret_cast<const float2 *>(smem_raw) + oN,
                         reinterpret_cast<const float2 *>(smem_raw + bN) + oS, equator, n, a.mmax, a.half[p],
                         a.tw32 + a.tw_ofs[i4], a.chirp + a.chirp_ofs[i4], Z);
-    blu_ring<LOGM>(a, e, map, p, Z, nullptr, wh, true);
+    blu_ring<LOGM>(a, e, map, p, Z, nullptr, wh, true, wp);
 }
 
 // Class 1: Bluestein.  smem: Z[M] (the south fold scratch sits at n..2n-1) |
@@ -1129,7 +1222,8 @@ static const RingKernel kEqStaged[15] = {nullptr, nullptr, nullptr, nullptr, nul
                                          nullptr, nullptr, k_ring32eq<10, 512>, k_ring32eq<11, 512>,
                                          k_ring32eq<12, 512>, k_ring32eq<13, 512>, k_ring32eq<14, 1024>};
 static size_t eq_staged_smem(int n) {
-    return sizeof(float2) * (size_t)(((glg_zsize(n) + 1) & ~1) + ((glg_zsize(n / 2 + 1) + 1) & ~1) + 2);
+    return sizeof(float2) *
+           (size_t)(((glg_zsize(n) + 1) & ~1) + ((glg_zsize(n / 2 + 1) + 1) & ~1) + wtab_total_host(n) + 2);
 }
 // The staged kernel takes a power-of-two bucket of 2^10 .. 2^14 when n > mmax
 // and the two staged rows fit the transform buffer.
