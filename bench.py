@@ -160,7 +160,8 @@ def run_cfg2(steps: int = 3) -> dict:
     shifts in [0.5, 2], from seed 0), device-resident.  Plain FP64 and fast
     forms timed with CUDA events (best of `steps`), the fast form's error per
     shell against the FP64 form (accuracy_report), and the spin-2 shear of
-    the summed convergence (from_convergence, discretized, FP64 form)."""
+    the summed convergence (from_convergence, discretized) with its
+    synthesis in both forms: times and the fast shear's error against FP64."""
     import torch
 
     import glass_gb300 as g

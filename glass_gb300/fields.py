@@ -354,10 +354,31 @@ def _generate_grf(gls, nside: int, *, ncorr=None, rng=None, form: str | None = N
             raise ValueError(b.bad_msg)
 
 
-def _pinned_maps(nmaps: int, npix: int) -> torch.Tensor:
-    """Pinned float32 [nmaps, npix] host buffer (recycled by torch's caching
-    host allocator) for the fast form's host-output synthesis."""
-    return torch.empty((nmaps, npix), dtype=torch.float32, pin_memory=True)
+# Page-locked output buffers of the host-output synthesis, kept for reuse.
+# Each is held as (tensor, numpy view of the whole buffer); the maps handed
+# to a caller are rows of that numpy view, so its reference count says
+# whether any map of an earlier call is still alive.  Pinning 8 GB anew
+# costs 0.3-0.6 s, more than a whole 40-shell step.
+_PINNED: list[tuple[torch.Tensor, np.ndarray]] = []
+_PINNED_KEEP = 2  # buffers of one shape kept when every one is in use
+
+
+def _pinned_maps(nmaps: int, npix: int) -> tuple[torch.Tensor, np.ndarray]:
+    """Pinned float32 [nmaps, npix] host buffer for the fast form's
+    host-output synthesis, and its numpy view (hand out its rows), reused
+    once the caller has dropped every map of an earlier call into it."""
+    for i in range(len(_PINNED)):
+        # references to the view: the pool entry and getrefcount's argument;
+        # any more are maps of an earlier call still alive
+        if _PINNED[i][1].shape == (nmaps, npix) and sys.getrefcount(_PINNED[i][1]) <= 2:
+            return _PINNED[i]
+    t = torch.empty((nmaps, npix), dtype=torch.float32, pin_memory=True)
+    entry = (t, t.numpy())
+    same = [i for i in range(len(_PINNED)) if _PINNED[i][1].shape == (nmaps, npix)]
+    if len(same) >= _PINNED_KEEP:
+        del _PINNED[same[0]]  # the oldest goes back to torch once its maps are dropped
+    _PINNED.append(entry)
+    return entry
 
 
 def _to_host(maps: torch.Tensor) -> list[np.ndarray]:
@@ -407,13 +428,14 @@ def _generate(fields, gls, nside, ncorr, rng, form):
             epi_kind = [_lib.EPI_LOGNORMAL if f else _lib.EPI_NONE for f in fused]
             epi = (epi_kind, [variances[t] for t in range(t0, t0 + cnt)],
                    [kinds[t][1] if fused[s] else 1.0 for s, t in enumerate(range(t0, t0 + cnt))])
-            host = _pinned_maps(cnt, 12 * b.nside * b.nside) if b.numpy_out and form == "fast" else None
-            if host is not None:
+            pinned = _pinned_maps(cnt, 12 * b.nside * b.nside) if b.numpy_out and form == "fast" else None
+            if pinned is not None:
                 # each run of ring tiles is copied to the pinned buffer while
                 # the next run computes: little copying is left after the last
-                b.maps(t0, cnt, epi=epi, out=host)
+                b.maps(t0, cnt, epi=epi, out=pinned[0])
                 torch.cuda.current_stream(b.device).synchronize()
-                maps = [h.numpy() for h in host]
+                maps = list(pinned[1])
+                del pinned
             else:
                 maps = b.maps(t0, cnt, epi=epi)
                 if b.numpy_out:

@@ -162,3 +162,37 @@ def test_fft_radix_constants_exact():
         h = np.float32(val)
         lval = float(np.float32(re.search(name + r"L = (-?[0-9.]+(?:e-?[0-9]+)?)f", src).group(1)))
         assert abs(float(h) + lval - val) < 1e-15
+
+
+def test_pinned_output_buffers_reused_only_when_dropped(monkeypatch):
+    """The host-output synthesis hands out rows of a pooled page-locked
+    buffer: a buffer is reused only once every map of the earlier call that
+    wrote into it has been dropped (pinning 8 GB anew costs more than a
+    step)."""
+    import torch
+
+    import glass_gb300.fields as f
+
+    real_empty = torch.empty
+
+    def empty(*a, **k):  # no page-locked memory without a GPU
+        k.pop("pin_memory", None)
+        return real_empty(*a, **k)
+
+    monkeypatch.setattr(f.torch, "empty", empty)
+    monkeypatch.setattr(f, "_PINNED", [])
+    e = f._pinned_maps(3, 5)
+    rows = list(e[1])
+    first = id(e[1])
+    del e
+    e = f._pinned_maps(3, 5)
+    assert id(e[1]) != first  # the first call's maps are alive
+    second = id(e[1])
+    del e
+    keep = rows[1]
+    del rows
+    e = f._pinned_maps(3, 5)
+    assert id(e[1]) == second  # the first buffer is still viewed by `keep`
+    del e, keep
+    e = f._pinned_maps(3, 5)
+    assert id(e[1]) in (first, second) and len(f._PINNED) == 2
