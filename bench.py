@@ -93,14 +93,13 @@ def _serving_requests(n: int, seed: int):
     return reqs
 
 
-def _serve(reqs, rate: float | None, form: str, batching: bool) -> dict:
+def _serve(reqs, rate: float | None, srv) -> dict:
     """Serve `reqs` arriving as a Poisson stream of `rate` requests/s (all at
-    once when rate is None); finished maps are dropped as they complete."""
+    once when rate is None) on server `srv`; finished maps are dropped as
+    they complete."""
     import torch
 
-    from glass_gb300 import serving
-
-    srv = serving.Server(hbm_budget=120 << 30, form=form, batching=batching)
+    form, batching = srv.form, srv.batching
     gaps = np.random.default_rng(7).exponential(1.0 / rate, len(reqs)) if rate else np.zeros(len(reqs))
     t0 = time.perf_counter() + 0.05
     arrivals = t0 + np.cumsum(gaps)
@@ -138,19 +137,26 @@ def _serve(reqs, rate: float | None, form: str, batching: bool) -> dict:
 
 
 def run_serving(args) -> dict:
-    """Serving workload: calibrate capacity on a closed batch, then serve a
-    Poisson arrival stream at 70% of it; the FP64 form without batching on a
-    smaller sample for comparison."""
+    """Serving workload on one long-running server: a closed warm-up batch
+    (plans, fast tables, captured launch graphs), a closed calibration batch
+    for the capacity, then a Poisson arrival stream at 70% of it; the FP64
+    form without batching on a smaller sample for comparison."""
+    from glass_gb300 import serving
+
     out = {}
     for form, batching, n, ncal in (("fast", True, args.serving, min(200, args.serving)),
                                     ("plain", False, args.serving_plain, min(20, args.serving_plain))):
         if n <= 0:
             continue
-        cal = _serve(_serving_requests(ncal, seed=91), None, form, batching)
+        srv = serving.Server(hbm_budget=120 << 30, form=form, batching=batching)
+        _serve(_serving_requests(ncal, seed=17), None, srv)  # warm-up
+        cal = _serve(_serving_requests(ncal, seed=91), None, srv)
         cap = cal["requests"] / cal["span_s"]
-        res = _serve(_serving_requests(n, seed=3), 0.7 * cap, form, batching)
+        res = _serve(_serving_requests(n, seed=3), 0.7 * cap, srv)
         res["capacity_req_per_s"] = cap
+        res["launch_graphs"] = bool(getattr(srv, "graphs", False))
         out[f"{form}{'_batched' if batching else '_unbatched'}"] = res
+        del srv
     return out
 
 

@@ -89,6 +89,9 @@ _SIGNATURES = {
     "glg_alm2map_spin_workspace": ([c_p], c_sz),
     "glg_alm2map_spin": ([c_p, c_p, c_p, c_i, c_p, c_p, c_p, c_sz, c_p], c_i),
     "glg_alm2map_spin_fast_workspace": ([c_p, c_i, c_i], c_sz),
+    "glg_epilogue_dev_bytes": ([], c_sz),
+    "glg_epilogue_dev_fill": ([c_p, c_i, c_p], c_i),
+    "glg_alm2map_fast_devepi": ([c_p, c_p, c_i, c_p, c_p, c_p, c_sz, c_p], c_i),
     "glg_alm2map_spin_fast": ([c_p, c_p, c_p, c_i, c_i, c_p, c_p, c_sz, c_p], c_i),
     "glg_map2alm_workspace": ([c_p, c_i], c_sz),
     "glg_map2alm": ([c_p, c_p, c_i, c_i, c_p, c_p, c_sz, c_p], c_i),

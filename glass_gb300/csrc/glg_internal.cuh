@@ -205,13 +205,26 @@ int glg_launch_leg_ana(const glg_plan *P, const double2 *G, int nmaps, double2 *
 // Tail refinement list of the fast form (in the fast workspace): hdr[0]
 // entries appended by the ring FFTs, hdr[1] entries already refined; items
 // (map, ring, pixel within the ring).
+// Device-resident epilogue of a graph-captured fast synthesis (the kernels
+// read it at run time instead of taking it as a launch argument, so one
+// captured graph serves every epilogue); filled on the host by
+// glg_epilogue_dev_fill and copied to the device before each replay.
+#define GLG_EPI_MAPS 40
+struct glg_epi_dev {
+    int kind[GLG_EPI_MAPS];
+    float hvar[GLG_EPI_MAPS], lam[GLG_EPI_MAPS], thr[GLG_EPI_MAPS];  // var / 2, shift, tail threshold
+    double hv64[GLG_EPI_MAPS], lam64[GLG_EPI_MAPS];                  // the same in FP64 (tail refinement)
+};
 struct glg_refine_list {
     int *hdr;
     int cap;
     int4 *items;
     float2 *gz;  // nside > 2048: the global transform buffers of Bluestein class 3
     int *err;    // the call's status word (a staged copy's bounded wait that ran out), or null
+    const glg_epi_dev *edev = nullptr;  // device epilogue (graph-captured calls), or null
 };
+// Fill a device-epilogue image in host memory from a host epilogue.
+void glg_epi_dev_fill(const glg_epilogue *epi, int nmaps, glg_epi_dev *out);
 // Class-3 buffers: GLG_RING_GSLOTS slices of glg_zsize(Mmax) complex values.
 #define GLG_RING_GSLOTS 304
 // Bytes of the class-3 buffers for a plan of this nside (0 when nside <= 2048).

@@ -516,8 +516,8 @@ struct Epi32 {
 constexpr double REFINE_KAPPA = 1000.0;
 constexpr double REFINE_MIN_VAR = 4.0;
 
-__device__ __forceinline__ void refine_note(const Epi32 &e, int map, float g, int ring, int k) {
-    if (g > e.thr[map]) {
+__device__ __forceinline__ void refine_note(const Epi32 &e, float thr, int map, float g, int ring, int k) {
+    if (g > thr) {
         const int slot = atomicAdd(e.rcount, 1);
         if (slot < e.rcap) e.ritems[slot] = make_int4(map, ring, k, 0);
     }
@@ -544,7 +544,18 @@ struct RingArgs {
     const float2 *twp;   // padded half twiddle tables by log2 length (staged kernels)
     int64_t twp_ofs[16];
     int *err;            // status word for a staged copy that never arrived (or null)
+    const glg_epi_dev *edev;  // epilogue in device memory (graph-captured calls), or null
 };
+
+// The epilogue of one map: from the device epilogue when the call has one.
+struct EpiMap {
+    int kind;
+    float hv, lam, thr;
+};
+__device__ __forceinline__ EpiMap epi_map(const RingArgs &a, const Epi32 &e, int map) {
+    if (a.edev) return {a.edev->kind[map], a.edev->hvar[map], a.edev->lam[map], a.edev->thr[map]};
+    return {e.kind[map], e.hvar[map], e.lam[map], e.thr[map]};
+}
 
 __device__ __forceinline__ c32 pack(c32 bn, c32 bs) { return {bn.x - bs.y, bn.y + bs.x}; }
 
@@ -695,8 +706,9 @@ __global__ void __launch_bounds__(POW2 ? TMAX_POW2 : TMAX) k_ring32(const RingAr
     const uint16_t *pos = a.pos16 + a.pos_ofs[i4];
     float *mp = a.maps + (int64_t)map * a.npix;
     const int64_t sN = a.startN[p], sS = a.startS[p];
-    const int kind = e.kind[map];
-    const float hv = e.hvar[map], lam = e.lam[map];
+    const EpiMap em = epi_map(a, e, map);
+    const int kind = em.kind;
+    const float hv = em.hv, lam = em.lam;
     // four consecutive pixels per thread, stored as one 16-byte vector (ring
     // starts and lengths are multiples of 4 pixels): fewer, larger stores,
     // which the CPU-GPU link takes better when the maps are host memory
@@ -710,15 +722,15 @@ __global__ void __launch_bounds__(POW2 ? TMAX_POW2 : TMAX) k_ring32(const RingAr
         };
         const c32 v0 = at(ps.x), v1 = at(ps.y), v2 = at(ps.z), v3 = at(ps.w);
         if (kind == GLG_EPI_LOGNORMAL) {
-            refine_note(e, map, v0.x, rn, 4 * q);
-            refine_note(e, map, v1.x, rn, 4 * q + 1);
-            refine_note(e, map, v2.x, rn, 4 * q + 2);
-            refine_note(e, map, v3.x, rn, 4 * q + 3);
+            refine_note(e, em.thr, map, v0.x, rn, 4 * q);
+            refine_note(e, em.thr, map, v1.x, rn, 4 * q + 1);
+            refine_note(e, em.thr, map, v2.x, rn, 4 * q + 2);
+            refine_note(e, em.thr, map, v3.x, rn, 4 * q + 3);
             if (!equator) {
-                refine_note(e, map, v0.y, rs, 4 * q);
-                refine_note(e, map, v1.y, rs, 4 * q + 1);
-                refine_note(e, map, v2.y, rs, 4 * q + 2);
-                refine_note(e, map, v3.y, rs, 4 * q + 3);
+                refine_note(e, em.thr, map, v0.y, rs, 4 * q);
+                refine_note(e, em.thr, map, v1.y, rs, 4 * q + 1);
+                refine_note(e, em.thr, map, v2.y, rs, 4 * q + 2);
+                refine_note(e, em.thr, map, v3.y, rs, 4 * q + 3);
             }
         }
         *reinterpret_cast<float4 *>(mp + sN + 4 * q) =
@@ -832,8 +844,9 @@ __global__ void __launch_bounds__(T, T <= 512 ? 2 : 1) k_ring32eq(const RingArgs
     const uint16_t *pos = a.pos16 + a.pos_ofs[i4];
     float *mp = a.maps + (int64_t)map * a.npix;
     const int64_t sN = a.startN[p], sS = a.startS[p];
-    const int kind = e.kind[map];
-    const float hv = e.hvar[map], lam = e.lam[map];
+    const EpiMap em = epi_map(a, e, map);
+    const int kind = em.kind;
+    const float hv = em.hv, lam = em.lam;
 #pragma unroll 2
     for (int q = threadIdx.x; q < N / 4; q += T) {
         const ushort4 ps = *reinterpret_cast<const ushort4 *>(pos + 4 * q);
@@ -844,15 +857,15 @@ __global__ void __launch_bounds__(T, T <= 512 ? 2 : 1) k_ring32eq(const RingArgs
         };
         const c32 v0 = at(ps.x), v1 = at(ps.y), v2 = at(ps.z), v3 = at(ps.w);
         if (kind == GLG_EPI_LOGNORMAL) {
-            refine_note(e, map, v0.x, rn, 4 * q);
-            refine_note(e, map, v1.x, rn, 4 * q + 1);
-            refine_note(e, map, v2.x, rn, 4 * q + 2);
-            refine_note(e, map, v3.x, rn, 4 * q + 3);
+            refine_note(e, em.thr, map, v0.x, rn, 4 * q);
+            refine_note(e, em.thr, map, v1.x, rn, 4 * q + 1);
+            refine_note(e, em.thr, map, v2.x, rn, 4 * q + 2);
+            refine_note(e, em.thr, map, v3.x, rn, 4 * q + 3);
             if (!equator) {
-                refine_note(e, map, v0.y, rs, 4 * q);
-                refine_note(e, map, v1.y, rs, 4 * q + 1);
-                refine_note(e, map, v2.y, rs, 4 * q + 2);
-                refine_note(e, map, v3.y, rs, 4 * q + 3);
+                refine_note(e, em.thr, map, v0.y, rs, 4 * q);
+                refine_note(e, em.thr, map, v1.y, rs, 4 * q + 1);
+                refine_note(e, em.thr, map, v2.y, rs, 4 * q + 2);
+                refine_note(e, em.thr, map, v3.y, rs, 4 * q + 3);
             }
         }
         *reinterpret_cast<float4 *>(mp + sN + 4 * q) =
@@ -894,8 +907,9 @@ __device__ __forceinline__ void blu_ring(const RingArgs &a, const Epi32 &e, int 
         fft_dif_adjoint<-1, true>(Z, wh, M);
     float *mp = a.maps + (int64_t)map * a.npix;
     const int64_t sN = a.startN[p], sS = a.startS[p];
-    const int kind = e.kind[map];
-    const float hv = e.hvar[map], lam = e.lam[map];
+    const EpiMap em = epi_map(a, e, map);
+    const int kind = em.kind;
+    const float hv = em.hv, lam = em.lam;
     const float invM = 1.0f / (float)M;
 #pragma unroll 1
     for (int q = threadIdx.x; q < (n >> 2); q += T) {  // four pixels per thread, 16-byte stores
@@ -906,15 +920,15 @@ __device__ __forceinline__ void blu_ring(const RingArgs &a, const Epi32 &e, int 
         const c32 v2 = cscale(cmul(Z[zi(4 * q + 2)], c32{cb.x, cb.y}), invM);
         const c32 v3 = cscale(cmul(Z[zi(4 * q + 3)], c32{cb.z, cb.w}), invM);
         if (kind == GLG_EPI_LOGNORMAL) {
-            refine_note(e, map, v0.x, rn, 4 * q);
-            refine_note(e, map, v1.x, rn, 4 * q + 1);
-            refine_note(e, map, v2.x, rn, 4 * q + 2);
-            refine_note(e, map, v3.x, rn, 4 * q + 3);
+            refine_note(e, em.thr, map, v0.x, rn, 4 * q);
+            refine_note(e, em.thr, map, v1.x, rn, 4 * q + 1);
+            refine_note(e, em.thr, map, v2.x, rn, 4 * q + 2);
+            refine_note(e, em.thr, map, v3.x, rn, 4 * q + 3);
             if (!equator) {
-                refine_note(e, map, v0.y, rs, 4 * q);
-                refine_note(e, map, v1.y, rs, 4 * q + 1);
-                refine_note(e, map, v2.y, rs, 4 * q + 2);
-                refine_note(e, map, v3.y, rs, 4 * q + 3);
+                refine_note(e, em.thr, map, v0.y, rs, 4 * q);
+                refine_note(e, em.thr, map, v1.y, rs, 4 * q + 1);
+                refine_note(e, em.thr, map, v2.y, rs, 4 * q + 2);
+                refine_note(e, em.thr, map, v3.y, rs, 4 * q + 3);
             }
         }
         *reinterpret_cast<float4 *>(mp + sN + 4 * q) =
@@ -1134,6 +1148,7 @@ struct RefineArgs {
     int cap;
     const int4 *items;  // (map, ring, pixel within the ring, -)
     double hv[EPI_MAX], lam[EPI_MAX];
+    const glg_epi_dev *edev;  // when set: hv, lam from device memory
 };
 
 // One warp per listed pixel: g = F_0 + 2 Re sum_{m>0} F_m e^{i m phi} in FP64
@@ -1168,7 +1183,9 @@ __global__ void __launch_bounds__(256) k_refine(const RefineArgs r) {
         for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
         if (lane == 0) {
             const int64_t start = ring < r.npairs ? r.startN[p] : r.startS[p];
-            r.maps[(int64_t)map * r.npix + start + k] = (float)(r.lam[map] * expm1(v - r.hv[map]));
+            const double hv = r.edev ? r.edev->hv64[map] : r.hv[map];
+            const double lam = r.edev ? r.edev->lam64[map] : r.lam[map];
+            r.maps[(int64_t)map * r.npix + start + k] = (float)(lam * expm1(v - hv));
         }
     }
 }
@@ -1204,6 +1221,7 @@ static void ring_args(const glg_plan *P, const float2 *Ft, int nmaps, float *map
     a.twp = P->twp;
     for (int k = 0; k < 16; ++k) a.twp_ofs[k] = P->twp_ofs[k];
     a.err = nullptr;
+    a.edev = nullptr;
 }
 
 typedef void (*RingKernel)(const RingArgs, const Epi32);
@@ -1344,9 +1362,25 @@ bool glg_refine_wanted(const glg_epilogue *epi, int nmaps) {
     return false;
 }
 
+void glg_epi_dev_fill(const glg_epilogue *epi, int nmaps, glg_epi_dev *out) {
+    for (int k = 0; k < GLG_EPI_MAPS; ++k) {
+        const bool on = epi && k < nmaps;
+        const int kind = !on ? GLG_EPI_NONE : (epi->kinds ? epi->kinds[k] : epi->kind);
+        const double var = (on && epi->var) ? epi->var[k] : 0.0;
+        const double lam = (on && epi->lamda) ? epi->lamda[k] : 1.0;
+        out->kind[k] = kind;
+        out->hvar[k] = (float)(0.5 * var);
+        out->lam[k] = (float)lam;
+        out->thr[k] = on ? refine_threshold(epi, k, kind) : INFINITY;
+        out->hv64[k] = 0.5 * var;
+        out->lam64[k] = lam;
+    }
+}
+
 int glg_launch_refine(const glg_plan *P, const float2 *Ft, int nmaps, float *maps, const glg_epilogue *epi,
                       const glg_refine_list &rl, cudaStream_t st) {
-    if (!glg_refine_wanted(epi, nmaps)) return GLG_OK;
+    // a device epilogue is read at run time: the (possibly empty) list is always processed
+    if (!rl.edev && !glg_refine_wanted(epi, nmaps)) return GLG_OK;
     RefineArgs r;
     r.nrings = P->nrings;
     r.npairs = P->npairs;
@@ -1362,9 +1396,10 @@ int glg_launch_refine(const glg_plan *P, const float2 *Ft, int nmaps, float *map
     r.cap = rl.cap;
     r.items = rl.items;
     for (int k = 0; k < EPI_MAX; ++k) {
-        r.hv[k] = k < nmaps && epi->var ? 0.5 * epi->var[k] : 0.0;
-        r.lam[k] = k < nmaps && epi->lamda ? epi->lamda[k] : 1.0;
+        r.hv[k] = epi && k < nmaps && epi->var ? 0.5 * epi->var[k] : 0.0;
+        r.lam[k] = epi && k < nmaps && epi->lamda ? epi->lamda[k] : 1.0;
     }
+    r.edev = rl.edev;
     {
         GLG_LAUNCH_SCOPE("k_refine", st);
         k_refine<<<608, 256, 0, st>>>(r);
@@ -1414,6 +1449,7 @@ int glg_launch_ring_syn_f32_range(const glg_plan *P, const float2 *F, float2 *Ft
     e.ritems = rl ? rl->items : nullptr;
     a.gz = rl ? rl->gz : nullptr;
     a.err = rl ? rl->err : nullptr;
+    a.edev = rl ? rl->edev : nullptr;
     const bool whole = p0 == 0 && p1 == P->npairs;
     for (int b = 0; b < P->nbuckets; ++b) {
         const glg_ring_bucket &B = P->buckets[b];

@@ -118,6 +118,43 @@ extern "C" int glg_alm2map(const glg_plan *P, const void *alm, int nmaps, int fo
     return glg_launch_ring_syn(P, F, nmaps, (double *)maps, epi, ring_gbuf(P, ws, ring_coef_bytes(P, nmaps)), st);
 }
 
+// The fast synthesis with its epilogue in device memory (glg_epi_dev):
+// every step is a stream operation whose arguments do not depend on the
+// epilogue, so a capture of it replays with whatever epilogue was copied to
+// `epi_dev` before the replay.
+extern "C" int glg_alm2map_fast_devepi(const glg_plan *P, const void *alm, int nmaps, void *maps,
+                                       const void *epi_dev, void *ws, size_t ws_bytes, void *stream) {
+    GLG_REQUIRE(P != nullptr, "glg_alm2map_fast_devepi: null plan");
+    GLG_REQUIRE(nmaps >= 0 && nmaps <= GLG_EPI_MAPS, "glg_alm2map_fast_devepi: nmaps must be in [0, 40]");
+    if (nmaps == 0) return GLG_OK;
+    GLG_REQUIRE(alm && maps && epi_dev, "glg_alm2map_fast_devepi: null pointer");
+    GLG_REQUIRE(ws && ws_bytes >= glg_alm2map_workspace(P, nmaps, GLG_FORM_FAST),
+                "glg_alm2map_fast_devepi: workspace too small");
+    GLG_REQUIRE(P->fast_ready, "glg_alm2map_fast_devepi: the plan's fast tables are not built (run one fast "
+                               "synthesis first)");
+    cudaStream_t st = (cudaStream_t)stream;
+    FastWs w = fast_ws(P, nmaps, ws);
+    w.rl.edev = (const glg_epi_dev *)epi_dev;
+    cudaError_t e = cudaMemsetAsync(w.err, 0, GLG_WS_STATUS_BYTES, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(w.rl.hdr, 0, 256, st);
+    if (e != cudaSuccess) return glg_cuda_status(e, "glg_alm2map_fast_devepi: status reset");
+    const glg_tile_run all{0, (P->npairs + 127) / 128, 0, true};
+    int rc = glg_launch_leg_tc(P, (const float2 *)alm, nmaps, w.bpack, w.F, w.err, all, st);
+    if (rc) return rc;
+    rc = glg_launch_ring_syn_f32(P, w.F, w.Ft, nmaps, (float *)maps, nullptr, &w.rl, st);
+    if (rc) return rc;
+    return glg_launch_refine(P, w.Ft, nmaps, (float *)maps, nullptr, w.rl, st);
+}
+
+extern "C" size_t glg_epilogue_dev_bytes(void) { return sizeof(glg_epi_dev); }
+
+extern "C" int glg_epilogue_dev_fill(const glg_epilogue *epi, int nmaps, void *host_out) {
+    GLG_REQUIRE(host_out != nullptr, "glg_epilogue_dev_fill: null output");
+    GLG_REQUIRE(nmaps >= 0 && nmaps <= GLG_EPI_MAPS, "glg_epilogue_dev_fill: nmaps must be in [0, 40]");
+    glg_epi_dev_fill(epi, nmaps, (glg_epi_dev *)host_out);
+    return GLG_OK;
+}
+
 extern "C" size_t glg_alm2map_host_workspace(const glg_plan *P, int nmaps) {
     if (!P || nmaps <= 0) return 0;
     return glg_alm2map_workspace(P, nmaps, GLG_FORM_FAST) + sizeof(float) * (size_t)nmaps * P->npix;

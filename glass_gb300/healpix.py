@@ -226,46 +226,103 @@ class SynthGraph:
     """A fast-form synthesis captured once into a CUDA graph and replayed.
 
     Static buffers: ``alm`` (complex64 [nmaps, nalm], HEALPix order) and
-    ``maps`` (float32 [nmaps, npix]); the epilogue (kinds, variances, shifts)
-    is fixed at capture.  ``__call__(alm)`` copies its argument into the
-    static input (or pass ``None`` after writing ``self.alm`` in place),
-    replays the ~25 launches of the transform (B packing, tensor-core
-    contraction, transpose, one launch per ring-FFT size bucket) as one graph
-    launch and returns ``self.maps`` (overwritten by the next replay).
+    ``maps`` (float32 [nmaps, npix]), allocated here or passed in (``alm``,
+    ``maps``, ``ws``: a caller's launch buffers).  ``__call__(alm)`` copies
+    its argument into the static input (or pass ``None`` after writing
+    ``self.alm`` in place), replays the ~30 launches of the transform (status
+    reset, B packing, tensor-core contraction, transposes, one launch per
+    ring-FFT size bucket, tail refinement) as one graph launch and returns
+    ``self.maps`` (overwritten by the next replay).
+
+    The epilogue (kinds, variances, shifts) is fixed at capture, or, with
+    ``device_epilogue=True``, given per call: the kernels then read it from
+    a small device buffer that each call refills from page-locked host memory
+    on the replay's stream just before the replay (glg_alm2map_fast_devepi).
     """
 
+    _SLOTS = 256  # page-locked epilogue images in flight (a slot is reused only after its copy ran)
+
     def __init__(self, nside: int, lmax: int, nmaps: int, *, epilogue=None,
-                 device: torch.device | None = None):
+                 device: torch.device | None = None, device_epilogue: bool = False,
+                 alm: torch.Tensor | None = None, maps: torch.Tensor | None = None,
+                 ws: torch.Tensor | None = None):
         if not 1 <= nmaps <= FAST_MAX_MAPS:
             raise ValueError(f"nmaps must be in [1, {FAST_MAX_MAPS}]")
         device = torch.device("cuda", torch.cuda.current_device()) if device is None else device
         self.plan = get_plan(nside, lmax, device)
         self.nside, self.lmax, self.nmaps = nside, lmax, nmaps
-        self.alm = torch.zeros((nmaps, self.plan.nalm), dtype=torch.complex64, device=device)
-        self.maps = torch.empty((nmaps, self.plan.npix), dtype=torch.float32, device=device)
+        self.alm = alm[:nmaps] if alm is not None else \
+            torch.zeros((nmaps, self.plan.nalm), dtype=torch.complex64, device=device)
+        self.maps = maps[:nmaps] if maps is not None else \
+            torch.empty((nmaps, self.plan.npix), dtype=torch.float32, device=device)
+        if self.alm.dtype != torch.complex64 or tuple(self.alm.shape) != (nmaps, self.plan.nalm) or \
+                not self.alm.is_contiguous():
+            raise ValueError("alm must be a contiguous complex64 [nmaps, nalm] device tensor")
+        if self.maps.dtype != torch.float32 or tuple(self.maps.shape) != (nmaps, self.plan.npix) or \
+                not self.maps.is_contiguous():
+            raise ValueError("maps must be a contiguous float32 [nmaps, npix] device tensor")
         ws_bytes = int(lib().glg_alm2map_workspace(self.plan.handle, nmaps, _lib.FORM_FAST))
-        self.ws = torch.empty(ws_bytes, dtype=torch.uint8, device=device)
+        self.ws = ws if ws is not None and ws.numel() >= ws_bytes else \
+            torch.empty(ws_bytes, dtype=torch.uint8, device=device)
+        self.device_epilogue = bool(device_epilogue)
         self._epi = _make_epilogue(epilogue, nmaps) if epilogue is not None else None
+        if self.device_epilogue:
+            nb = int(lib().glg_epilogue_dev_bytes())
+            self.epi_dev = torch.empty(nb, dtype=torch.uint8, device=device)
+            self._slots = torch.empty((self._SLOTS, nb), dtype=torch.uint8, pin_memory=True)
+            self._slot_ev = [None] * self._SLOTS
+            self._slot = 0
         side = torch.cuda.Stream(device)
         side.wait_stream(torch.cuda.current_stream(device))
         with torch.cuda.stream(side):
-            autotune(self.plan, nmaps, self.maps, self.ws)
-            self._launch()  # builds the fast tables outside the capture
-            torch.cuda.current_stream(device).synchronize()
+            if not getattr(self.plan, "tuned", False):  # the plan's fast tables and FFT block sizes
+                autotune(self.plan, nmaps, self.maps, self.ws)
+                self._launch(host_epilogue=True)  # builds whatever the capture must not
+            if self.device_epilogue:
+                self.set_epilogue(epilogue)
+            side.synchronize()
             self.graph = torch.cuda.CUDAGraph()
             with torch.cuda.graph(self.graph, stream=side):
                 self._launch()
         torch.cuda.current_stream(device).wait_stream(side)
 
-    def _launch(self) -> None:
+    def _launch(self, host_epilogue: bool = False) -> None:
+        stream = c_p(stream_ptr(self.alm.device))
+        if self.device_epilogue and not host_epilogue:
+            check(lib().glg_alm2map_fast_devepi(self.plan.handle, c_p(ptr(self.alm)), self.nmaps,
+                                                c_p(ptr(self.maps)), c_p(ptr(self.epi_dev)), c_p(ptr(self.ws)),
+                                                self.ws.numel(), stream), "glg_alm2map_fast_devepi (graph)")
+            return
         epi = ctypes.byref(self._epi) if self._epi is not None else None
         check(lib().glg_alm2map(self.plan.handle, c_p(ptr(self.alm)), self.nmaps, _lib.FORM_FAST,
-                                c_p(ptr(self.maps)), epi, c_p(ptr(self.ws)), self.ws.numel(),
-                                c_p(stream_ptr(self.alm.device))), "glg_alm2map (graph)")
+                                c_p(ptr(self.maps)), epi, c_p(ptr(self.ws)), self.ws.numel(), stream),
+              "glg_alm2map (graph)")
 
-    def __call__(self, alm=None) -> torch.Tensor:
+    def set_epilogue(self, epilogue) -> None:
+        """Stage the epilogue of the next replay (device-epilogue graphs):
+        its image goes into the next page-locked slot and is copied to the
+        device buffer on the current stream."""
+        if not self.device_epilogue:
+            raise ValueError("this graph's epilogue was fixed at capture")
+        k = self._slot % self._SLOTS
+        self._slot += 1
+        if self._slot_ev[k] is not None:
+            self._slot_ev[k].synchronize()  # that slot's previous copy has been read
+        epi = _make_epilogue(epilogue, self.nmaps) if epilogue is not None else None
+        check(lib().glg_epilogue_dev_fill(ctypes.byref(epi) if epi is not None else None, self.nmaps,
+                                          c_p(self._slots[k].data_ptr())), "glg_epilogue_dev_fill")
+        self.epi_dev.copy_(self._slots[k], non_blocking=True)
+        ev = torch.cuda.Event()
+        ev.record(torch.cuda.current_stream(self.alm.device))
+        self._slot_ev[k] = ev
+
+    def __call__(self, alm=None, epilogue=None) -> torch.Tensor:
         if alm is not None:
             self.alm.copy_(torch.as_tensor(alm).reshape(self.alm.shape))
+        if self.device_epilogue:
+            self.set_epilogue(epilogue)
+        elif epilogue is not None:
+            raise ValueError("this graph's epilogue was fixed at capture (device_epilogue=False)")
         self.graph.replay()
         return self.maps
 

@@ -184,6 +184,17 @@ class _Group:
         # per launch in flight, checked when the launch's requests retire)
         self.status = torch.zeros(64, dtype=torch.int32, pin_memory=True)
         self.slot = 0
+        self.graphs: dict[int, hp.SynthGraph] = {}  # fast form: captured launches by map count
+
+    def graph(self, cnt: int) -> hp.SynthGraph:
+        """The captured fast synthesis of `cnt` maps on this group's buffers,
+        its epilogue read from device memory (captured on first use)."""
+        gr = self.graphs.get(cnt)
+        if gr is None:
+            gr = self.graphs[cnt] = hp.SynthGraph(self.nside, self.lmax, cnt, device_epilogue=True,
+                                                  alm=self.alm, maps=self.maps, ws=self.ws,
+                                                  device=self.alm.device)
+        return gr
 
 
 class Server:
@@ -201,16 +212,36 @@ class Server:
     after).  A request waits in the queue until all of that fits; idle
     groups (no request in service) give up their buffers and plans, least
     recently used first, when a new request needs the room.
+
+    Launches: with ``graphs=True`` (or ``GLASS_GB300_SERVING_GRAPHS=1``),
+    each fast (nside, lmax, map count) launch of a small transform (nside <=
+    ``GLASS_GB300_SERVING_GRAPH_NSIDE``, 256 by default) replays a CUDA graph
+    captured on first use over the group's buffers, its epilogue (kinds,
+    variances, shifts of the launch's shells) read from device memory
+    (``healpix.SynthGraph(device_epilogue=True)``); otherwise the kernels
+    are launched one by one (the default: measured no slower).
     """
 
     def __init__(self, hbm_budget: int = 120 << 30, max_maps_per_launch: int = 40,
-                 device: torch.device | None = None, form: str = "fast", batching: bool = True):
+                 device: torch.device | None = None, form: str = "fast", batching: bool = True,
+                 graphs: bool | None = None):
         if form not in ("fast", "plain"):
             raise ValueError(f"form must be 'plain' or 'fast', not {form!r}")
         self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else device
         self.budget = int(hbm_budget)
         self.form = form
         self.batching = bool(batching)
+        # fast form: each (nside, lmax, map count) launch replays a captured
+        # CUDA graph whose epilogue comes from device memory
+        if graphs is None:
+            graphs = os.environ.get("GLASS_GB300_SERVING_GRAPHS", "0") == "1"
+        self.graphs = bool(graphs) and form == "fast"
+        # graphs for the small transforms only, where the ~30 launches cost
+        # as much as the work.  Off by default: on the GB300 the serving
+        # workload measured no gain from them (capacity 529-577 req/s with
+        # and without, p99 higher with), its latency being set by the
+        # device work queued behind the large requests, not by launches
+        self.graph_nside = int(os.environ.get("GLASS_GB300_SERVING_GRAPH_NSIDE", "256"))
         self.max_maps = min(int(max_maps_per_launch), hp.FAST_MAX_MAPS) if batching else 1
         self.queue: collections.deque[Request] = collections.deque()
         self.active: list[_Active] = []
@@ -303,8 +334,13 @@ class Server:
                     if self.form == "fast":
                         st = g.status[g.slot % g.status.numel():][:1]
                         g.slot += 1
-                        maps = hp.synth(g.alm[:cnt], nside, lmax, epilogue=epi, form="fast",
-                                        out=g.maps[:cnt], ws=g.ws, status=st)
+                        if self.graphs and nside <= self.graph_nside:
+                            # one graph launch instead of ~30 kernel launches
+                            maps = g.graph(cnt)(None, epilogue=epi)
+                            st.copy_(g.ws[:4].view(torch.int32), non_blocking=True)
+                        else:
+                            maps = hp.synth(g.alm[:cnt], nside, lmax, epilogue=epi, form="fast",
+                                            out=g.maps[:cnt], ws=g.ws, status=st)
                     else:
                         maps = hp.synth(g.alm[:cnt], nside, lmax, epilogue=epi, form="plain", ws=g.ws)
                     for k, (a, s) in enumerate(chunk):

@@ -281,6 +281,21 @@ int glg_alm2map_host(const glg_plan *plan, const void *alm, int nmaps, void *map
  * count).  No counterpart in the reference. */
 int glg_host_output_runs(int nside, int64_t *out, int max_runs);
 
+/*
+ * Graph-capturable fast synthesis: glg_alm2map's fast form with the epilogue
+ * read from device memory at run time (epi_dev: glg_epilogue_dev_bytes()
+ * bytes, filled on the host by glg_epilogue_dev_fill and copied to the
+ * device before each launch or graph replay), so one captured CUDA graph
+ * serves every epilogue.  The plan's fast tables must exist (one fast
+ * glg_alm2map first).  nmaps <= 40; float32 maps.  Used by the serving loop
+ * (glass/fields.py:839-894 per request) and SynthGraph; no counterpart in
+ * the reference.  Check glg_workspace_status afterwards.
+ */
+size_t glg_epilogue_dev_bytes(void);
+int glg_epilogue_dev_fill(const glg_epilogue *epi, int nmaps, void *host_out);
+int glg_alm2map_fast_devepi(const glg_plan *plan, const void *alm, int nmaps, void *maps, const void *epi_dev,
+                            void *workspace, size_t workspace_bytes, void *stream);
+
 /* Status word of a fast-form workspace (synchronises `stream`): GLG_OK or
  * GLG_ERR_TIMEOUT.  No counterpart in the reference (no device waits there). */
 int glg_workspace_status(const void *workspace, void *stream);

@@ -625,3 +625,29 @@ def test_synth_graph_replays_equal_direct_calls(g):
         graph.status()
         ref = hp.synth(alm, nside, lmax, epilogue=epi, form="fast")
         torch.testing.assert_close(got, ref, rtol=0, atol=0)
+
+
+def test_synth_graph_device_epilogue(g):
+    """One captured graph, its epilogue read from device memory: replays
+    with different epilogues (Gaussian, lognormal, and a lognormal of
+    variance >= 4 that takes the FP64 tail refinement) equal direct calls
+    with those epilogues, bit for bit."""
+    import torch
+
+    from glass_gb300 import healpix as hp
+
+    nside, lmax, nm = 64, 128, 3
+    graph = hp.SynthGraph(nside, lmax, nm, device_epilogue=True)
+    L = g._lib.EPI_LOGNORMAL
+    # maps of standard deviation ~2.2 (variance ~5): a few pixels of the
+    # variance-5 lognormal maps cross the tail threshold, far fewer than the
+    # list holds, so the refined set does not depend on the listing order
+    alm = torch.as_tensor(random_alm(lmax, seed=9, nmaps=nm) * 0.043, device="cuda").to(torch.complex64)
+    epis = [None,
+            ([L, g._lib.EPI_NONE, L], [0.2, 0.0, 0.5], [1.0, 1.0, 2.0]),
+            ([L, L, L], [5.0, 0.3, 4.5], [0.7, 1.0, 1.5])]
+    for epi in epis:
+        got = graph(alm, epilogue=epi).clone()
+        graph.status()
+        ref = hp.synth(alm, nside, lmax, epilogue=epi, form="fast")
+        torch.testing.assert_close(got, ref, rtol=0, atol=0)

@@ -22,7 +22,10 @@ def _request(serving, nside, nshell, seed):
     return serving.Request(gls=gls, nside=nside, shifts=[float(x) for x in lam], seed=seed)
 
 
-def test_result_alone_equals_result_in_mix(cuda_lib):
+@pytest.mark.parametrize("graphs", [False, True])
+def test_result_alone_equals_result_in_mix(cuda_lib, graphs):
+    """Also through captured launch graphs with device epilogues (the mix
+    replays each (nside, map count) graph with other requests' shells)."""
     from glass_gb300 import serving
 
     alone = serving.Server(hbm_budget=8 << 30)
@@ -30,7 +33,7 @@ def test_result_alone_equals_result_in_mix(cuda_lib):
     alone.drain()
     ref = np.stack([m.cpu().numpy() for m in ra.maps])
 
-    mix = serving.Server(hbm_budget=8 << 30, max_maps_per_launch=16)
+    mix = serving.Server(hbm_budget=8 << 30, max_maps_per_launch=16, graphs=graphs)
     others = [_request(serving, nside, n, seed=100 + k)
               for k, (nside, n) in enumerate([(32, 7), (64, 4), (32, 3), (16, 9), (64, 6)])]
     for r in others[:2]:
