@@ -78,6 +78,25 @@ constexpr uint32_t WAIT_LIMIT = 1u << 22;
 // v + 7e-8 v rounds to v plus one whole ulp.)
 constexpr float ACC_BIAS = 7.0e-8f;
 constexpr int W_DRAIN = 12, W_MMA = 16, W_LOAD = 17, W_SEED = 18, W_MMA2 = 19;
+// Table path: the drain warps keep the running sums of their lane (2 N FP32
+// values) in registers instead of shared memory, which leaves that room to
+// P_lm tile slots.  The kernel is launched with LEG_REGS registers a thread;
+// each warpgroup then sets its own share (setmaxnreg): the producers and the
+// MMA / streaming warps give up registers, the drain warpgroup takes them.
+// The shares add up to the launch's total: 3 x 128 x 72 + 128 x 216 +
+// 128 x 48 = 61440 = 640 x 96 (a larger sum would wait forever).
+constexpr int LEG_REGS = 96, REGS_PROD = 72, REGS_DRAIN = 216, REGS_MISC = 48;
+static_assert(3 * 128 * REGS_PROD + 128 * REGS_DRAIN + 128 * REGS_MISC <= THREADS * LEG_REGS,
+              "warpgroup register shares above the launch's registers");
+static_assert(W_DRAIN == 12 && W_MMA == 16 && THREADS == 5 * 128, "warpgroups: 3 producer, drain, the rest");
+template <uint32_t R>
+__device__ __forceinline__ void regs_inc() {
+    asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(R));
+}
+template <uint32_t R>
+__device__ __forceinline__ void regs_dec() {
+    asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(R));
+}
 static_assert(W_DRAIN == 4 * CH, "one producer warp set per group of a chunk");
 static_assert((W_MMA2 + 1) * 32 == THREADS, "one warp per role after the producers and drains");
 static_assert(W_MMA % 4 != W_MMA2 % 4, "the two MMA-issuing warps on different SM sub-partitions");
@@ -160,10 +179,9 @@ constexpr int nbc_slots() {
     return room > 6 ? 6 : room;
 }
 template <int N>
-constexpr int plm_slots() {
-    constexpr int room = (226 * 1024 - 512 * (2 * N + 4) - nbc_slots<N, true>() * CH * 128 * N - 1024) /
-                         GLG_PLM_TILE_BYTES;
-    return room > 12 ? 12 : room;
+constexpr int plm_slots() {  // the running sums are in the drain warps' registers
+    constexpr int room = (226 * 1024 - nbc_slots<N, true>() * CH * 128 * N - 2048) / GLG_PLM_TILE_BYTES;
+    return room > 24 ? 24 : room;
 }
 
 struct SeedSlot {
@@ -188,7 +206,7 @@ struct Smem {
     } bs[NBC];
     std::conditional_t<T, PlmSlot, SeedSlot> sd[NS];
     static constexpr int ACC_LD = 2 * N + 4;  // floats per lane row (odd count of float4)
-    float acc[128][ACC_LD];    // FP32 sums of drained chunks, [lane][column]
+    float acc[T ? 1 : 128][T ? 4 : ACC_LD];  // FP32 sums of drained chunks, [lane][column] (recurrence path)
     uint64_t full_a[2], cdone[2], empty_d[2];
     uint64_t full_b[NBC], bempty[NBC];
     uint64_t sfull[NS], sempty[NS];
@@ -200,7 +218,7 @@ struct Smem {
 };
 
 template <int N, bool T>
-__global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
+__device__ __forceinline__ void leg_tc_body(const LegTcArgs &a) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     using SM = Smem<N, T>;
     SM &S = *reinterpret_cast<SM *>(smem_raw);
@@ -236,7 +254,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
         S.abort = 0;
         fence_barrier_init();
     }
-    for (int i = threadIdx.x; i < 128 * SM::ACC_LD; i += THREADS) (&S.acc[0][0])[i] = 0.f;
+    if constexpr (!T)
+        for (int i = threadIdx.x; i < 128 * SM::ACC_LD; i += THREADS) (&S.acc[0][0])[i] = 0.f;
     if (warp == 0) {
         tmem_alloc(&S.tmem_base, TMEM_COLS);
         tmem_relinquish();
@@ -282,6 +301,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
     // gg % NSEED (phase gg / NSEED).
     if (warp < W_DRAIN) {
         // ------------------------------------------------ lambda producers
+        if constexpr (T) regs_dec<REGS_PROD>();
         const int set = warp >> 2;
         uint32_t cc = 0, gc = 0;
         bool ok = true;
@@ -397,7 +417,65 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
         }
         if (!ok) fail();
     } else if (warp < W_MMA) {
-        // --------------------------------- drain: chunk sums -> smem -> F
+        // --------------------------------- drain: chunk sums -> F
+        if constexpr (T) {
+            regs_inc<REGS_DRAIN>();
+            // running sums of this lane (ring pair): E in columns 0..N-1, O
+            // in N..2N-1, added chunk by chunk in the order of the
+            // shared-memory path (same FP32 results)
+            float acc[2 * N];
+#pragma unroll
+            for (int c = 0; c < 2 * N; ++c) acc[c] = 0.f;
+            uint32_t cc = 0;
+            bool ok = true;
+            for (uint32_t ui = 0; ok; ++ui) {
+                int64_t u;
+                if (!next_unit(ui, u, true)) { ok = false; break; }
+                if (u >= a.nunits) break;
+                const int tile = a.tile0 + (int)(u % a.nrun);
+                const int m = unit_m(u / a.nrun, lmax);
+                const int G = (lmax - m + GLG_GROUP) / GLG_GROUP;
+                const int gf = a.tfirst[(int64_t)m * a.ntiles + tile];
+                for (int kc = 0, nch = (G - gf + CH - 1) / CH; kc < nch; ++kc, ++cc) {
+                    const uint32_t d = cc & 1u;
+                    if (!wait(&S.cdone[d], (cc >> 1) & 1u)) { ok = false; break; }
+                    fence_after_sync();
+                    static_assert((2 * N) % 32 == 0, "accumulator columns in pairs of 16");
+                    const uint32_t dcol = tb + lane_base + 2 * N * d;
+#pragma unroll
+                    for (int c0 = 0; c0 < 2 * N; c0 += 32) {
+                        uint32_t v[32];
+                        tmem_ld16(dcol + c0, *reinterpret_cast<uint32_t(*)[16]>(&v[0]));
+                        tmem_ld16(dcol + c0 + 16, *reinterpret_cast<uint32_t(*)[16]>(&v[16]));
+                        tmem_wait_ld();
+#pragma unroll
+                        for (int j = 0; j < 32; ++j) acc[c0 + j] += __uint_as_float(v[j]);
+                    }
+                    fence_before_sync();
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(&S.empty_d[d]);
+                }
+                if (!ok) break;
+                // unit complete: north = E + O, south = E - O
+                const int p = tile * 128 + r;
+                if (p < a.npairs) {
+                    const int rs = a.nrings - 1 - p;
+#pragma unroll
+                    for (int map = 0; map < N / 2; ++map) {
+                        if (map < a.nmaps) {
+                            const float er = acc[2 * map], ei = acc[2 * map + 1];
+                            const float orr = acc[N + 2 * map], oi = acc[N + 2 * map + 1];
+                            float2 *Fm = a.F + ((int64_t)map * (lmax + 1) + m) * a.nrings;
+                            Fm[p] = make_float2(er + orr, ei + oi);
+                            if (rs != p) Fm[rs] = make_float2(er - orr, ei - oi);
+                        }
+                    }
+                }
+#pragma unroll
+                for (int c = 0; c < 2 * N; ++c) acc[c] = 0.f;
+            }
+            if (!ok) fail();
+        } else {
         uint32_t cc = 0;
         bool ok = true;
         for (uint32_t ui = 0; ok; ++ui) {
@@ -459,7 +537,10 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
                 *reinterpret_cast<float4 *>(&S.acc[r][c0]) = make_float4(0.f, 0.f, 0.f, 0.f);
         }
         if (!ok) fail();
-    } else if (warp == W_MMA || warp == W_MMA2) {
+        }
+    } else {
+    if constexpr (T) regs_dec<REGS_MISC>();  // warps 16-19: one warpgroup
+    if (warp == W_MMA || warp == W_MMA2) {
         // ---------------------------------------------------------- MMA issue
         // Warp W_MMA issues the even-parity (E) accumulator's MMAs, warp
         // W_MMA2 the odd (O) one's, from different SM sub-partitions: each
@@ -614,12 +695,24 @@ __global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
         }
         __syncwarp();
     }
+    }
     fence_before_sync();
     __syncthreads();
     if (warp == 0) {
         fence_after_sync();
         tmem_dealloc(tb, TMEM_COLS);
     }
+}
+
+// The recurrence path (running sums in shared memory) and the table path
+// (running sums in the drain warps' registers, warpgroup register shares).
+template <int N>
+__global__ void __launch_bounds__(THREADS, 1) k_leg_tc(const LegTcArgs a) {
+    leg_tc_body<N, false>(a);
+}
+template <int N>
+__global__ void __maxnreg__(LEG_REGS) k_leg_tc_plm(const LegTcArgs a) {
+    leg_tc_body<N, true>(a);
 }
 
 // ------------------------------------------------------------------ packing
@@ -740,8 +833,21 @@ int launch_tc(const glg_plan *P, const float2 *alm, const float2 *alm2, int nspl
         GLG_LAUNCH_SCOPE("k_leg_tc", st);
         kern<<<(unsigned)grid, THREADS, smem, st>>>(a);
     };
-    if (a.plm) go(k_leg_tc<N, true>, sizeof(Smem<N, true>));
-    else go(k_leg_tc<N, false>, sizeof(Smem<N, false>));
+    if (a.plm) {
+        // the warpgroup register shares assume the launch's LEG_REGS registers a thread
+        static int regs = -1;
+        if (regs < 0) {
+            cudaFuncAttributes fa;
+            regs = cudaFuncGetAttributes(&fa, k_leg_tc_plm<N>) == cudaSuccess ? fa.numRegs : 0;
+        }
+        if (regs != LEG_REGS) {
+            glg_set_error("fast Legendre contraction: the table kernel was not built with its register count");
+            return GLG_ERR_UNSUPPORTED;
+        }
+        go(k_leg_tc_plm<N>, sizeof(Smem<N, true>));
+    } else {
+        go(k_leg_tc<N>, sizeof(Smem<N, false>));
+    }
     GLG_CHECK_LAUNCH("k_leg_tc");
     return GLG_OK;
 }
