@@ -48,7 +48,7 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "shell-maps/sec and pixels/sec at nside 2048 vs plain FP64 GPU @1e-6; p50/p99 latency"
 UNIT = "shell-maps/s"
-PASSES = 4  # tensor-core products per Legendre term (A_lo B_lo, A_hi B_lo, A_lo B_hi, A_hi B_hi)
+PASSES = 3  # tensor-core products per Legendre term (A_hi B_lo, A_lo B_hi, A_hi B_hi)
 WORKLOAD = dict(workload="40-shell lognormal field generation, nside 2048, lmax 4096", nshell=40, nside=2048,
                 lmax=4096)
 

@@ -1,5 +1,5 @@
 // Fast form of the Legendre sums: a shells-batched contraction on the
-// sm_103a tensor cores (tcgen05, split-precision TF32: 3xTF32 plus the lo x lo term).
+// sm_103a tensor cores (tcgen05, split-precision TF32: 3xTF32).
 //
 // For one ring tile (128 ring pairs, one per TMEM lane) and one m:
 //   D_E[p][n] = sum_{l-m even} lambda_lm(x_p) B[l][n],
@@ -19,8 +19,10 @@
 // carry d_l instead (B[l][n] = a_lm d_l), so the sums are unchanged.  B (the alm, split the same way), the
 // group's seeds and its recurrence coefficients are streamed into shared
 // memory with 1-D bulk copies.  Each group issues, per parity,
-//   D += A_lo B_lo + A_hi B_lo + A_lo B_hi + A_hi B_hi   (M = 128, N = 2 * maps, K = 8),
-// with both lo parts rounded to nearest TF32 (4 passes).
+//   D += A_hi B_lo + A_lo B_hi + A_hi B_hi   (M = 128, N = 2 * maps, K = 8),
+// with both lo parts rounded to nearest TF32 (3 passes; a fourth, A_lo B_lo,
+// of relative size 2^-22, changed the benchmark's worst lognormal shell by
+// 6e-10 and cost 2.4 ms, 9 % of the contraction).
 //
 // Groups before the first one where some ring of the tile has |lambda| >=
 // 2^-40 are zero on the whole tile and are skipped (the dense algorithmic
@@ -582,8 +584,7 @@ __device__ __forceinline__ void leg_tc_body(const LegTcArgs &a) {
 #pragma unroll
                     for (int q = 0; q < CH; ++q) {
                         if (q < ng) {
-                            mma_tf32_ts(dD, a0 + 32 * q + 8, d0 + q * GT + TT, IDESC, q > 0 ? 1u : 0u);
-                            mma_tf32_ts(dD, a0 + 32 * q + 0, d0 + q * GT + TT, IDESC, 1u);
+                            mma_tf32_ts(dD, a0 + 32 * q + 0, d0 + q * GT + TT, IDESC, q > 0 ? 1u : 0u);
                             mma_tf32_ts(dD, a0 + 32 * q + 8, d0 + q * GT, IDESC, 1u);
                         }
                     }
