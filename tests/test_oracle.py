@@ -87,6 +87,21 @@ def test_iternorm_matches_reference(golden):
         np.testing.assert_allclose(w, golden[f"iternorm_cfg2_nc{nc}"], rtol=1e-13, atol=1e-16)
 
 
+def test_iternorm_ulp_distance_to_reference(golden):
+    """The oracle's iternorm rows -- bit-exact with the GPU kernel
+    (tests/test_gpu_parity.py) -- against the reference's numpy rows on the
+    config-2 covariances: at most 2 ulp apart and about 87 % of the entries
+    identical (the sums run in another order than numpy's matmuls)."""
+    for nc in (5, 2):
+        wo, bad = of.iternorm_stack(golden[f"cls2cov_cfg2_nc{nc}"])
+        ref = golden[f"iternorm_cfg2_nc{nc}"]
+        big = np.maximum(np.abs(wo), np.abs(ref))
+        ulp = np.where(wo == ref, 0.0, np.abs(wo - ref) / np.spacing(np.where(big > 0, big, 1.0)))
+        assert bad == -1
+        assert ulp.max() <= 2.0
+        assert np.mean(ulp == 0) > 0.85
+
+
 @pytest.mark.parametrize("k", [0, 1, 2])
 @pytest.mark.parametrize("nd", ["0d", "nd"])
 def test_iternorm_reference_test_matrices(golden, k, nd):
