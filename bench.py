@@ -231,7 +231,7 @@ def run_cfg2(steps: int = 3) -> dict:
 def run_cfg5(nshell: int = 60, nside: int = 4096, lmax: int = 8192) -> dict:
     """Config 5: 60 lognormal shells at nside 4096 / lmax 8192 (config-3
     spectra, seed 5) streamed through the fast form in groups of shells (as
-    many as 60 % of the free device memory holds), each shell consumed as it comes: its
+    many as a 48 GB workspace allows), each shell consumed as it comes: its
     lognormal map added into the cumulative convergence (mean of the shells)
     and, for the first two, Poisson galaxy counts (5 per pixel) drawn from it
     as float32 and as float64 -- the counts must agree bit for bit, whichever

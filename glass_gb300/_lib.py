@@ -252,14 +252,6 @@ def get_plan(nside: int, lmax: int, device: torch.device | None = None) -> Plan:
     return p
 
 
-def plan_cached(nside: int, lmax: int, device: torch.device | None = None) -> bool:
-    """Whether the plan of (nside, lmax) is in the cache (its memory held)."""
-    device = torch.device("cuda", torch.cuda.current_device()) if device is None else device
-    key = (device.index if device.index is not None else torch.cuda.current_device(), nside, lmax)
-    with _PLAN_LOCK:
-        return key in _PLANS
-
-
 def clear_plans() -> None:
     with _PLAN_LOCK:
         _PLANS.clear()

@@ -196,21 +196,3 @@ def test_pinned_output_buffers_reused_only_when_dropped(monkeypatch):
     del e, keep
     e = f._pinned_maps(3, 5)
     assert id(e[1]) in (first, second) and len(f._PINNED) == 2
-
-
-def test_shell_group_size_follows_the_room(monkeypatch):
-    """Shells per batched transform: as many as the byte budget holds (the
-    free-memory room, or GLASS_GB300_BATCH_BYTES when set), at least one,
-    at most the shell count; one per shell with a numpy generator."""
-    import glass_gb300.fields as f
-
-    monkeypatch.delenv("GLASS_GB300_BATCH_BYTES", raising=False)
-    per = f._shell_bytes(4096, 8192, "fast")
-    assert 3e9 < per < 5e9  # two copies of the Legendre sums, map, alm, B columns
-    assert f._group_size(60, 4096, 8192, "fast", room=83 * per // 4) == 20
-    assert f._group_size(60, 4096, 8192, "fast", room=per // 2) == 1
-    assert f._group_size(40, 2048, 4096, "fast", room=200 << 30) == 40
-    assert f._group_size(40, 2048, 4096, "fast", host_rng=True, room=200 << 30) == 1
-    assert f._shell_bytes(2048, 4096, "plain") > f._shell_bytes(2048, 4096, "fast")
-    monkeypatch.setenv("GLASS_GB300_BATCH_BYTES", str(10 * per))
-    assert f._group_size(60, 4096, 8192, "fast", room=1) == 10
