@@ -264,6 +264,8 @@ def run_cfg5(nshell: int = 60, nside: int = 4096, lmax: int = 8192) -> dict:
     same, stream = [], torch.cuda.current_stream()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
+    _lib.timing_enable(True)
+    _lib.timing_reset()
     e0.record(stream)
     t_counts = 0.0
     for t, m in enumerate(g.generate(fields, gls, nside, rng=g.rng.Generator(42), form="fast")):
@@ -282,9 +284,14 @@ def run_cfg5(nshell: int = 60, nside: int = 4096, lmax: int = 8192) -> dict:
         del m
     e1.record(stream)
     torch.cuda.synchronize()
+    fast_kernels = {k: _lib.kernel_time(k) for k in ("k_leg_tc", "k_pack_b", "k_transpose32", "k_ring32",
+                                                       "k_ring32_blu", "k_ring32_blug", "k_alm_correlate",
+                                                       "k_iternorm", "k_refine", "k_poisson_counts")}
+    _lib.timing_enable(False)
     ms = e0.elapsed_time(e1) - t_counts
     out["fast"] = {"ms": ms, "shell_maps_per_s": nshell / (ms / 1e3), "pixels_per_s": nshell * npix / (ms / 1e3),
-                   "note": "includes the FP64 counts of two shells' float64 copies"}
+                   "note": "includes the FP64 counts of two shells' float64 copies",
+                   "kernel_ms_launches": fast_kernels}
     out["counts"] = {"bit_exact_f32_vs_f64_delta": all(same), "pixels_per_s": npix / (t_counts / 2 / 1e3),
                      "mean_per_pixel": 5.0}
     a = time.perf_counter()
