@@ -134,6 +134,7 @@ struct glg_plan {
     // copied whole into shared memory by the staged kernels)
     float2 *twp;
     int64_t twp_ofs[16];
+    int64_t twp3_ofs[16];  // the same for lengths 3 * 2^k (Bluestein lengths 6144, 12288), by k
 };
 
 // Radix passes of an FP32 ring FFT of length n (DIF order: 16s, then one 8,

@@ -555,6 +555,52 @@ size_t glg_ring32_smem(int kind, int n_or_M, int threads, bool fold) {
     return slots * sizeof(float2);
 }
 
+// Bluestein length of a ring of n pixels: the smallest power of two M >=
+// 2n - 1, or 3 * 2^k when that is smaller and the staged kernels take it
+// (M = 6144 or 12288, the ring pair's two rows of Legendre sums fitting the
+// transform buffer): 13.5 % fewer butterflies over the rings of nside 2048.
+static int blu_length(int n, int mmax) {
+    int M = 1;
+    while (M < 2 * n - 1) M <<= 1;
+    int M3 = 3;
+    while (M3 < 2 * n - 1) M3 <<= 1;
+    const size_t rows = 2 * (((size_t)(mmax + 2) * 8 + 15) & ~(size_t)15);
+    if (M3 < M && (M3 == 6144 || M3 == 12288) && rows <= sizeof(float2) * (size_t)glg_zsize(M3)) return M3;
+    return M;
+}
+
+// Radix passes of a Bluestein length in the device's order: 3 * 2^k lengths
+// start with their radix-3 pass, then as glg_fft32_radices.
+static int blu_radices(int M, int *r) {
+    if (M % 3 != 0) return glg_fft32_radices(M, r);
+    r[0] = 3;
+    return 1 + glg_fft32_radices(M / 3, r + 1);
+}
+
+// Forward DFT (e^{-2 pi i k t / M}) of a length 2^k or 3 * 2^k, FP64 (host).
+static void fft_host(std::vector<std::complex<double>> &x) {
+    const size_t M = x.size();
+    if (M % 3 != 0) {
+        fft_pow2_host(x);
+        return;
+    }
+    const size_t Q = M / 3;
+    std::vector<std::complex<double>> y[3];
+    for (int r = 0; r < 3; ++r) {
+        y[r].resize(Q);
+        for (size_t j = 0; j < Q; ++j) y[r][j] = x[3 * j + r];
+        fft_pow2_host(y[r]);
+    }
+    for (size_t k = 0; k < M; ++k) {
+        std::complex<double> acc = y[0][k % Q];
+        for (int r = 1; r < 3; ++r) {
+            const double ang = -2.0 * M_PI * (double)(((int64_t)r * (int64_t)k) % (int64_t)M) / (double)M;
+            acc += std::complex<double>(cos(ang), sin(ang)) * y[r][k % Q];
+        }
+        x[k] = acc;
+    }
+}
+
 static int build_fft32_tables(glg_plan *P, cudaStream_t st) {
     const int nside = P->nside, mmax = P->mmax;
     std::vector<int64_t> pos_ofs(nside + 2, 0), blu_ofs(nside + 1, -1), chirp_ofs(nside + 1, -1);
@@ -565,14 +611,13 @@ static int build_fft32_tables(glg_plan *P, cudaStream_t st) {
         int r[GLG_MAX_FFT_STAGES];
         pos_ofs[i + 1] = pos_ofs[i] + 4LL * i;
         if (glg_fft32_radices(4 * i, r) < 0) {
-            int M = 1;
-            while (M < 2 * 4 * i - 1) M <<= 1;
+            const int M = blu_length(4 * i, mmax);
             blu_M[i] = M;
             blu_ofs[i] = nblu;
             nblu += M;
             chirp_ofs[i] = nchirp;
             nchirp += 4 * i;
-            if (M > Mmax) Mmax = M;
+            if (M > Mmax && M % 3 != 0) Mmax = M;
         }
     }
     std::vector<uint16_t> pos16(pos_ofs[nside + 1]);
@@ -596,9 +641,9 @@ static int build_fft32_tables(glg_plan *P, cudaStream_t st) {
             h[t] = std::complex<double>(cos(ph), -sin(ph));
             if (t > 0) h[M - t] = h[t];
         }
-        fft_pow2_host(h);
+        fft_host(h);
         int mr[GLG_MAX_FFT_STAGES];
-        const int mns = glg_fft32_radices(M, mr);
+        const int mns = blu_radices(M, mr);
         for (int k = 0; k < M; ++k) {
             const int q = dif_pos_host(mr, mns, M, k);
             H[blu_ofs[i] + q] = make_float2((float)h[k].real(), (float)h[k].imag());
@@ -623,13 +668,21 @@ static int build_fft32_tables(glg_plan *P, cudaStream_t st) {
     int lgmax = 3;
     while ((1 << lgmax) < Mmax || (1 << lgmax) < 4 * nside) ++lgmax;
     std::vector<float2> twp;
-    for (int lg = 0; lg < 16; ++lg) P->twp_ofs[lg] = -1;
+    for (int lg = 0; lg < 16; ++lg) P->twp_ofs[lg] = P->twp3_ofs[lg] = -1;
     for (int lg = 3; lg <= lgmax && lg < 16; ++lg) {
         const int L = 1 << lg;
         P->twp_ofs[lg] = (int64_t)twp.size();
         twp.resize(twp.size() + ((glg_zsize(L / 2 + 1) + 1) & ~1) + 2, make_float2(0.f, 0.f));  // 16-byte sizes, slack
         for (int t = 0; t <= L / 2; ++t)
             twp[P->twp_ofs[lg] + glg_zi(t)] = make_float2((float)cos(2.0 * M_PI * t / L), (float)sin(2.0 * M_PI * t / L));
+    }
+    for (int k = 0; k < 16; ++k) {  // the 3 * 2^k Bluestein lengths in use
+        const int L = 3 << k;
+        if (std::find(blu_M.begin(), blu_M.end(), L) == blu_M.end()) continue;
+        P->twp3_ofs[k] = (int64_t)twp.size();
+        twp.resize(twp.size() + ((glg_zsize(L / 2 + 1) + 1) & ~1) + 2, make_float2(0.f, 0.f));
+        for (int t = 0; t <= L / 2; ++t)
+            twp[P->twp3_ofs[k] + glg_zi(t)] = make_float2((float)cos(2.0 * M_PI * t / L), (float)sin(2.0 * M_PI * t / L));
     }
     std::vector<float2> twMp;  // padded copy for class 3 (read from global memory)
     if (Mmax > 16384) {

@@ -334,9 +334,11 @@ __device__ void fft_dif_adjoint(c32 *Z, const c32 *wh, int n) {
 
 // Power-of-two transforms of a compile-time length N: the same passes (16s,
 // then one 8, 4 or 2) with every index, shift and mask a constant.
+// The passes of a compile-time length: 3 * 2^k lengths take their radix-3
+// pass first (the rest is a power of two), then 16s, then one 8, 4 or 2.
 template <int L>
 struct RadixOf {
-    static constexpr int value = L % 16 == 0 ? 16 : L;
+    static constexpr int value = L % 3 == 0 ? 3 : (L % 16 == 0 ? 16 : L);
 };
 
 // Per-pass twiddle tables of a compile-time length N: for every DIF pass
@@ -399,7 +401,7 @@ __device__ __forceinline__ c32 cmul_dir(c32 a, c32 w) {
 static int wtab_total_host(int N) {
     int tot = 0;
     for (int L = N; L > 1;) {
-        const int R = L % 16 == 0 ? 16 : L, msub = L / R;
+        const int R = L % 3 == 0 ? 3 : (L % 16 == 0 ? 16 : L), msub = L / R;
         if (L < N && msub > 1) tot += (R - 1) * msub;
         L /= R;
     }
@@ -415,14 +417,14 @@ template <int R, int DIR, bool ADJ, bool ZV, int N, int L>
 __device__ __forceinline__ void pass_ct(c32 *Z, const c32 *wh, const c32 *wp, int nv) {
     constexpr int msub = L / R, nbf = N / R, tsc = N / L;
     constexpr bool by_blk = tsc >= 32;
-    constexpr int lg_tsc = __builtin_ctz(tsc), lg_msub = __builtin_ctz(msub);
     constexpr bool cidx = msub >= 16;
     constexpr bool unit = msub == 1;
     const bool table = wp != nullptr && L < N && !unit;
     const c32 *wl = table ? wp + WOfs<N, L>::value : nullptr;
     for (int bf = threadIdx.x; bf < nbf; bf += blockDim.x) {
-        const int blk = by_blk ? bf & (tsc - 1) : bf >> lg_msub;
-        const int j1 = by_blk ? bf >> lg_tsc : bf & (msub - 1);
+        // divisions by constants (shifts and masks for powers of two)
+        const int blk = by_blk ? bf % tsc : bf / msub;
+        const int j1 = by_blk ? bf / tsc : bf % msub;
         const int base = blk * L + j1;
         const int ts = tsc * j1;
         const int zb = zi(base);
@@ -543,9 +545,15 @@ struct RingArgs {
     int64_t npix;
     const float2 *twp;   // padded half twiddle tables by log2 length (staged kernels)
     int64_t twp_ofs[16];
+    int64_t twp3_ofs[16];  // the same for lengths 3 * 2^k, by k
     int *err;            // status word for a staged copy that never arrived (or null)
     const glg_epi_dev *edev;  // epilogue in device memory (graph-captured calls), or null
 };
+
+// Offset of the padded half twiddle table of length M (2^k or 3 * 2^k) in twp.
+__device__ __forceinline__ int64_t twp_offset(const RingArgs &a, int M) {
+    return (M % 3 == 0) ? a.twp3_ofs[__ffs(M / 3) - 1] : a.twp_ofs[__ffs(M) - 1];
+}
 
 // The epilogue of one map: from the device epilogue when the call has one.
 struct EpiMap {
@@ -881,7 +889,7 @@ __global__ void __launch_bounds__(T, T <= 512 ? 2 : 1) k_ring32eq(const RingArgs
 // Bluestein transform of ring pair p, map `map`, in buffer Z (shared or
 // global memory) with the padded twiddle table wh of its length M and the
 // partial-sum scratch X (2 x blockDim).  Ends with the stores.
-template <int LOGM = 0>
+template <int MC = 0>  // compile-time transform length (0: the ring's, at run time)
 __device__ __forceinline__ void blu_ring(const RingArgs &a, const Epi32 &e, int map, int p, c32 *Z, c32 *X,
                                          const c32 *wh, bool folded = false, const c32 *wp = nullptr) {
     const int n = a.nph[p], i4 = n / 4, T = blockDim.x;
@@ -893,16 +901,16 @@ __device__ __forceinline__ void blu_ring(const RingArgs &a, const Epi32 &e, int 
     const float2 *FN = a.Ft + ((int64_t)map * a.nrings + rn) * (a.mmax + 1);
     const float2 *FS = a.Ft + ((int64_t)map * a.nrings + rs) * (a.mmax + 1);
     if (!folded) fold(FN, FS, equator, n, a.mmax, a.half[p], w2n, chirp, Z, Z, n, X);
-    if constexpr (LOGM > 0)  // the padding beyond n is zero: not written, not read
-        dif_ct<-1, (1 << LOGM), (1 << LOGM), true, false>(Z, wh, n, wp);
+    if constexpr (MC > 0)  // the padding beyond n is zero: not written, not read
+        dif_ct<-1, MC, MC, true, false>(Z, wh, n, wp);
     else
         fft_dif<-1, true>(Z, wh, M, n);
     const float2 *H = a.blu_H + a.blu_ofs[i4];
 #pragma unroll 8
     for (int k = threadIdx.x; k < M; k += T) Z[zi(k)] = cmul(Z[zi(k)], ldg(H + k));  // 8 loads in flight
     __syncthreads();
-    if constexpr (LOGM > 0)
-        adj_ct<-1, (1 << LOGM), (1 << LOGM)>(Z, wh, wp);
+    if constexpr (MC > 0)
+        adj_ct<-1, MC, MC>(Z, wh, wp);
     else
         fft_dif_adjoint<-1, true>(Z, wh, M);
     float *mp = a.maps + (int64_t)map * a.npix;
@@ -1038,10 +1046,10 @@ __device__ __forceinline__ void fold_staged(const float2 *stN, const float2 *stS
 // pair's rows of Legendre sums and the padded half twiddle table of M
 // bulk-copied into shared memory on one mbarrier, then the fold from shared
 // memory and blu_ring's transforms.  smem: Z[zsize(M)] | wh[zsize(M/2+1)].
-template <int LOGM, int T>
+template <int M, int T>
 __global__ void __launch_bounds__(T, T <= 512 ? 2 : 1) k_ring32_blus(const RingArgs a, const Epi32 e) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    constexpr int M = 1 << LOGM, NZ = ZSize<M>::value, NW = ZSize<M / 2 + 1>::value;
+    constexpr int NZ = ZSize<M>::value, NW = ZSize<M / 2 + 1>::value;
     constexpr int NI = (M / 4 + 1 + T - 1) / T, NK = (M / 2 + T - 1) / T;
     constexpr uint32_t BW = (uint32_t)(((NW * 8) + 15) & ~15);
     __shared__ __align__(8) uint64_t bar;
@@ -1068,7 +1076,7 @@ __global__ void __launch_bounds__(T, T <= 512 ? 2 : 1) k_ring32_blus(const RingA
         glg_tc::mbar_arrive_expect_tx(&bar, bN + bS + BW);
         glg_tc::bulk_g2s(smem_raw, FN - oN, bN, &bar);
         if (!equator) glg_tc::bulk_g2s(smem_raw + bN, FS - oS, bS, &bar);
-        glg_tc::bulk_g2s(wh, a.twp + a.twp_ofs[LOGM], BW, &bar);
+        glg_tc::bulk_g2s(wh, a.twp + twp_offset(a, M), BW, &bar);
     }
     if (!glg_tc::mbar_wait(&bar, 0, STAGE_WAIT_LIMIT)) {
         if (threadIdx.x == 0 && a.err) atomicExch(a.err, GLG_ERR_TIMEOUT);
@@ -1079,7 +1087,7 @@ __global__ void __launch_bounds__(T, T <= 512 ? 2 : 1) k_ring32_blus(const RingA
     fold_staged<NI, NK>(reinterpret_cast<const float2 *>(smem_raw) + oN,
                         reinterpret_cast<const float2 *>(smem_raw + bN) + oS, equator, n, a.mmax, a.half[p],
                         a.tw32 + a.tw_ofs[i4], a.chirp + a.chirp_ofs[i4], Z);
-    blu_ring<LOGM>(a, e, map, p, Z, nullptr, wh, true, wp);
+    blu_ring<M>(a, e, map, p, Z, nullptr, wh, true, wp);
 }
 
 // Class 1: Bluestein.  smem: Z[M] (the south fold scratch sits at n..2n-1) |
@@ -1095,7 +1103,7 @@ __global__ void __launch_bounds__(TMAX_POW2) k_ring32_blu(const RingArgs a, cons
     c32 *wh = X + 2 * T;
     const int stride = a.Mmax / M;
     for (int t = threadIdx.x; t <= M / 2; t += T) wh[zi(t)] = ldg(a.twM + (int64_t)t * stride);
-    blu_ring<LOGM>(a, e, map, p, Z, X, wh);
+    blu_ring<(1 << LOGM)>(a, e, map, p, Z, X, wh);
 }
 
 // Class 3: Bluestein lengths too large for shared memory (M = 32768, the
@@ -1219,7 +1227,10 @@ static void ring_args(const glg_plan *P, const float2 *Ft, int nmaps, float *map
     a.maps = maps;
     a.npix = P->npix;
     a.twp = P->twp;
-    for (int k = 0; k < 16; ++k) a.twp_ofs[k] = P->twp_ofs[k];
+    for (int k = 0; k < 16; ++k) {
+        a.twp_ofs[k] = P->twp_ofs[k];
+        a.twp3_ofs[k] = P->twp3_ofs[k];
+    }
     a.err = nullptr;
     a.edev = nullptr;
 }
@@ -1252,13 +1263,15 @@ static bool staged_eq_ok(const glg_plan *P, const glg_ring_bucket &B) {
     return rows <= sizeof(float2) * (size_t)glg_zsize(n) && eq_staged_smem(n) <= 227 * 1024;
 }
 
-// The staged Bluestein kernels take M = 2^13 (512 threads) and 2^14 (1024)
+// The staged Bluestein kernels take M = 6144, 8192 (512 threads), 12288, 16384 (1024)
 // when the two staged rows fit the transform buffer and every ring of the
 // bucket has at least as many pixels as the block has threads.
 static bool staged_blu_ok(const glg_plan *P, const glg_ring_bucket &B, int count) {
     const int M = B.size;
-    if ((M != 8192 && M != 16384) || !P->twp || P->twp_ofs[M == 8192 ? 13 : 14] < 0 || count <= 0) return false;
-    const int T = M == 8192 ? 512 : 1024;
+    if ((M != 6144 && M != 8192 && M != 12288 && M != 16384) || !P->twp || count <= 0) return false;
+    if ((M % 3 == 0 ? P->twp3_ofs[__builtin_ctz((unsigned)(M / 3))] : P->twp_ofs[__builtin_ctz((unsigned)M)]) < 0)
+        return false;
+    const int T = M >= 12288 ? 1024 : 512;
     const int *bp = P->bucket_pairs_host + B.first;
     for (int i = 0; i < B.count; ++i) {
         const int p = bp[i];
@@ -1288,9 +1301,14 @@ static int launch_bucket(const glg_plan *P, const glg_ring_bucket &B, int thread
         k_ring32_blug<<<g3, threads, smem, st>>>(a, e, (int)grid);
         GLG_CHECK_LAUNCH("k_ring32_blug");
     } else if (B.kind == 1 && staged_blu_ok(P, B, count)) {
-        const int lg = __builtin_ctz((unsigned)B.size);
-        const int T = lg >= 14 ? 1024 : 512;
-        const RingKernel kern = lg >= 14 ? k_ring32_blus<14, 1024> : k_ring32_blus<13, 512>;
+        RingKernel kern;
+        int T;
+        switch (B.size) {
+            case 16384: kern = k_ring32_blus<16384, 1024>; T = 1024; break;
+            case 12288: kern = k_ring32_blus<12288, 1024>; T = 1024; break;
+            case 8192: kern = k_ring32_blus<8192, 512>; T = 512; break;
+            default: kern = k_ring32_blus<6144, 512>; T = 512; break;
+        }
         const size_t sm = eq_staged_smem(B.size);
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         GLG_LAUNCH_SCOPE("k_ring32_blu", st);

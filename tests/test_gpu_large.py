@@ -66,6 +66,24 @@ def test_alm2map_plain_and_fast_cfg3_size(g):
     assert rel_rms(fast.cpu().numpy()[0], ref[0]) < FAST_RMS
 
 
+def test_fast_bluestein_lengths_3_pow2(g):
+    """nside 1024 / lmax 2048 takes Bluestein length 6144 = 3 * 2^11 for the
+    ring lengths 4i in (2048, 3072] with a large prime factor (nside 2048
+    takes 12288 in the test above): the fast maps agree with the plain FP64
+    maps everywhere, ring by ring."""
+    import torch
+
+    from glass_gb300 import healpix as hp
+
+    nside, lmax = 1024, 2048
+    alm = _alm(lmax, 2, seed=23)
+    plain = np.asarray(g.healpix.alm2map(list(alm), nside, pol=False))
+    fast = hp.synth(torch.as_tensor(alm, device="cuda").to(torch.complex64), nside, lmax, form="fast").cpu().numpy()
+    assert rel_rms(fast, plain) < FAST_RMS
+    scale = np.sqrt(np.mean(plain**2))
+    assert np.max(np.abs(fast - plain)) < 2e-5 * scale
+
+
 def test_generate_cfg2_vs_oracle(g):
     """Config 2: 10 correlated lognormal shells at nside 512 / lmax 1024,
     device Philox stream; plain to 1e-12 of the oracle, fast to 1e-6 RMS."""
