@@ -731,7 +731,7 @@ def main() -> None:
     ap.add_argument("--nside", type=int, default=2048)
     ap.add_argument("--lmax", type=int, default=4096)
     ap.add_argument("--plain-steps", type=int, default=1)
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-shells", type=int, default=1)
     ap.add_argument("--serving", type=int, default=2000, help="requests of the serving workload (0: off)")
     ap.add_argument("--serving-plain", type=int, default=60,

@@ -306,6 +306,128 @@ __global__ void k_alm_correlate(const T *__restrict__ w, const int nshell, const
     }
 }
 
+// The fast form's window sum with the variate window in registers: the
+// same elements, sums and summation order as k_alm_correlate<float2, float>,
+// for windows k + 1 <= WT.  One warp per l and 32 consecutive m (a block: 8
+// l x 32 m), so the warp's lanes share every w coefficient: per group of
+// CR_SB shells the warp stages its l's w rows into its own shared memory,
+// right-aligned in rows of WT coefficients (slot j holds the coefficient of
+// z_{t-(WT-1-j)}, zero where that variate is absent or older than the
+// window: adding 0 * z leaves the running sum's bits unchanged), and each
+// lane draws its CR_SB variates into its own column; the sum then reads the
+// coefficients as 16-byte broadcasts.  No block-wide barrier.
+// The window is a ring of WT registers and the shell loop is unrolled WT
+// times, so every ring slot is a constant.
+constexpr int CR_SB = 8, CR_WARPS = 8;
+
+template <int WT>
+__global__ void __launch_bounds__(32 * CR_WARPS, 2)
+    k_alm_correlate_rw(const float *__restrict__ w, const int nshell, const int lmax, const int k, const int64_t t0,
+                       const float2 *__restrict__ z, const int64_t z_first, const uint64_t seed,
+                       const uint64_t sid_base, float2 *__restrict__ alm) {
+    static_assert(WT % CR_SB == 0 && WT % 4 == 0 && WT <= 64, "window slots");
+    __shared__ __align__(16) float wsm[CR_WARPS][CR_SB][WT];
+    __shared__ __align__(16) float2 zsm[CR_WARPS][CR_SB][32];
+    const int kp = k + 1;
+    const int wi = (int)(threadIdx.x >> 5), lane = (int)(threadIdx.x & 31);
+    const int l = blockIdx.x * CR_WARPS + wi, m0 = blockIdx.y * 32;
+    if (l > lmax || m0 > l) return;  // the warp's whole row lies outside m <= l <= lmax
+    const int m = m0 + lane;
+    const bool valid = m <= l;
+    const int64_t nalm = glg_nalm(lmax);
+    const int64_t g = (int64_t)l * (l + 1) / 2 + m;              // GLASS index
+    const int64_t ix = (int64_t)m * (2 * lmax + 1 - m) / 2 + l;  // HEALPix index
+    const int L = lmax + 1;
+    const int64_t zlo = t0 - k > 0 ? t0 - k : 0;
+    auto fetch = [&](int64_t t) -> float2 {
+        if (z != nullptr) return z[(t - z_first) * nalm + g];
+        return philox_cnormal_f32(seed, sid_base + (uint64_t)t, (uint64_t)g);
+    };
+    float2 *zc = &zsm[wi][0][lane];  // this lane's column: zc[sb * 32]
+    float(*wr)[WT] = wsm[wi];
+    // the window before t0: z_{t0-d} in register WT - d (d = 1 .. WT - 1),
+    // drawn CR_SB at a time through the column
+    float2 zr[WT];
+#pragma unroll
+    for (int i = 0; i < WT; ++i) zr[i] = make_float2(0.f, 0.f);
+    if (valid && t0 > zlo) {
+#pragma unroll
+        for (int q = 0; q < WT / CR_SB; ++q) {
+#pragma unroll 1
+            for (int s = 0; s < CR_SB; ++s) {
+                const int d = q * CR_SB + s + 1;
+                zc[s * 32] = (d < WT && t0 - d >= zlo) ? fetch(t0 - d) : make_float2(0.f, 0.f);
+            }
+#pragma unroll
+            for (int s = 0; s < CR_SB; ++s) {
+                const int d = q * CR_SB + s + 1;
+                if (d < WT) zr[WT - d] = zc[s * 32];
+            }
+        }
+    }
+    // w rows of shells ub .. ub + nsb - 1 (lanes over the slots) and their variates
+    auto stage = [&](int ub, int nsb) {
+        __syncwarp();  // the previous group's rows and variates are read
+#pragma unroll
+        for (int sb = 0; sb < CR_SB; ++sb) {
+            if (sb < nsb) {
+                const int64_t t = t0 + ub + sb;
+                const int dmax = t < k ? (int)t : k;
+                const float *row = w + ((size_t)(ub + sb) * L + l) * kp + k;
+#pragma unroll
+                for (int j = lane; j < WT; j += 32) {
+                    const int d = WT - 1 - j;
+                    wr[sb][j] = d <= dmax ? row[-d] : 0.f;
+                }
+            }
+        }
+        if (valid) {
+#pragma unroll 1
+            for (int sb = 0; sb < nsb; ++sb) zc[sb * 32] = fetch(t0 + ub + sb);
+        }
+        __syncwarp();
+    };
+    // shell u, row sb: the window sum, oldest variate first; slot(j) is the
+    // register of the variate whose coefficient sits in row slot j
+    auto shell = [&](int u, int sb, auto slot) {
+        float re = 0.f, im = 0.f;
+#pragma unroll
+        for (int j = 0; j < WT; j += 4) {
+            const float4 c4 = *reinterpret_cast<const float4 *>(&wr[sb][j]);
+            const float2 z0 = zr[slot(j)], z1 = zr[slot(j + 1)], z2 = zr[slot(j + 2)], z3 = zr[slot(j + 3)];
+            re = fmaf(c4.x, z0.x, re);
+            im = fmaf(c4.x, z0.y, im);
+            re = fmaf(c4.y, z1.x, re);
+            im = fmaf(c4.y, z1.y, im);
+            re = fmaf(c4.z, z2.x, re);
+            im = fmaf(c4.z, z2.y, im);
+            re = fmaf(c4.w, z3.x, re);
+            im = fmaf(c4.w, z3.y, im);
+        }
+        if (m == 0) {
+            re = re + im;
+            im = 0.f;
+        }
+        if (valid) alm[(int64_t)u * nalm + ix] = make_float2(re, im);
+    };
+    for (int c0 = 0; c0 < nshell; c0 += WT) {
+#pragma unroll
+        for (int q = 0; q < WT / CR_SB; ++q) {
+            const int ub = c0 + q * CR_SB;
+            if (ub >= nshell) break;
+            const int nsb = nshell - ub < CR_SB ? nshell - ub : CR_SB;
+            stage(ub, nsb);
+#pragma unroll
+            for (int sb = 0; sb < CR_SB; ++sb) {
+                if (sb >= nsb) break;
+                const int uu = q * CR_SB + sb;  // a constant once unrolled: shell t0 + c0 + uu sits in register uu
+                zr[uu] = valid ? zc[sb * 32] : make_float2(0.f, 0.f);
+                shell(ub + sb, sb, [uu](int j) { return (uu + j + 1) % WT; });
+            }
+        }
+    }
+}
+
 // ----------------------------------------------------------- multalm etc.
 
 template <typename T2>
@@ -424,6 +546,18 @@ extern "C" int glg_alm_correlate(const void *w, int nshell, int lmax, int k, int
     while (threads > CT_L && smem_for(threads) > 200 * 1024) threads /= 2;
     const size_t smem = smem_for(threads);
     cudaStream_t st = (cudaStream_t)stream;
+    if (dtype == GLG_F32 && window <= 48) {  // the fast form's register window
+        const dim3 g2((lmax + CR_WARPS) / CR_WARPS, (lmax + 32) / 32);
+        using KR = void (*)(const float *, int, int, int, int64_t, const float2 *, int64_t, uint64_t, uint64_t, float2 *);
+        static const KR kr[6] = {k_alm_correlate_rw<8>,  k_alm_correlate_rw<16>, k_alm_correlate_rw<24>,
+                                 k_alm_correlate_rw<32>, k_alm_correlate_rw<40>, k_alm_correlate_rw<48>};
+        GLG_LAUNCH_SCOPE("k_alm_correlate", st);
+        kr[(window + 7) / 8 - 1]<<<g2, 32 * CR_WARPS, 0, st>>>((const float *)w, nshell, lmax, k, t0,
+                                                                  (const float2 *)z, z_first, seed, sid_base,
+                                                                  (float2 *)alm);
+        GLG_CHECK_LAUNCH("k_alm_correlate");
+        return GLG_OK;
+    }
     dim3 grid((lmax + CT_L) / CT_L, (lmax + threads / CT_L) / (threads / CT_L));
     GLG_LAUNCH_SCOPE("k_alm_correlate", st);
     if (dtype == GLG_F64) {

@@ -193,6 +193,51 @@ def test_correlated_alm_vs_reference_fixture(g, golden):
     np.testing.assert_allclose(alm, golden["generate_alm_all"], rtol=0, atol=1e-15)
 
 
+def _correlate(g, w, nshell, lmax, k, t0, z, z_first, dtype, out):
+    import torch
+
+    from glass_gb300._lib import c_p, check, lib, ptr, stream_ptr
+
+    check(lib().glg_alm_correlate(c_p(ptr(w)), nshell, lmax, k, t0, None if z is None else c_p(ptr(z)), z_first,
+                                  ctypes.c_uint64(42), ctypes.c_uint64(7), dtype, c_p(ptr(out)),
+                                  c_p(stream_ptr(torch.device("cuda", 0)))), "glg_alm_correlate")
+
+
+@pytest.mark.parametrize(("nshell", "lmax", "k", "split", "hostz"),
+                         [(12, 300, 5, 5, False), (12, 300, 5, 7, True), (50, 200, 39, 23, False),
+                          (30, 130, 0, 11, False), (9, 64, 47, 4, True), (20, 70, 60, 9, False)])
+def test_alm_correlate_fast_window(g, nshell, lmax, k, split, hostz):
+    """The fast form's correlated alm (register window for k + 1 <= 48, the
+    shared-memory window above): within FP32 rounding of the FP64 sums, and a
+    call split into two groups of shells (the second drawing its window of
+    earlier variates again) gives the same bits as one call."""
+    import torch
+
+    from glass_gb300 import _lib
+
+    kp, nalm = k + 1, (lmax + 1) * (lmax + 2) // 2
+    gen = torch.Generator().manual_seed(nshell + k)
+    w64 = (torch.randn((nshell, lmax + 1, kp), generator=gen, dtype=torch.float64) * 0.3).cuda()
+    w32 = w64.float()
+    z64 = torch.randn((nshell, nalm), generator=gen, dtype=torch.complex128).cuda() if hostz else None
+    z32 = z64.to(torch.complex64) if hostz else None
+    ref = torch.empty((nshell, nalm), dtype=torch.complex128, device="cuda")
+    _correlate(g, w64, nshell, lmax, k, 0, z64, 0, _lib.GLG_F64, ref)
+    one = torch.empty((nshell, nalm), dtype=torch.complex64, device="cuda")
+    _correlate(g, w32, nshell, lmax, k, 0, z32, 0, _lib.GLG_F32, one)
+    two = torch.empty_like(one)
+    _correlate(g, w32[:split].contiguous(), split, lmax, k, 0, z32[:split].contiguous() if hostz else None, 0,
+               _lib.GLG_F32, two[:split])
+    zlo = max(0, split - k)
+    _correlate(g, w32[split:].contiguous(), nshell - split, lmax, k, split,
+               z32[zlo:].contiguous() if hostz else None, zlo, _lib.GLG_F32, two[split:])
+    torch.cuda.synchronize()
+    assert torch.equal(torch.view_as_real(one), torch.view_as_real(two))
+    d = (one.to(torch.complex128) - ref).abs()
+    assert float(d.max()) < 1e-5 * float(ref.abs().max())
+    assert float(torch.sqrt((d * d).mean() / (ref.abs() ** 2).mean())) < 1e-6
+
+
 def test_generate_philox_vs_oracle(g):
     """Config-1 sizes (3 shells, nside 64, lmax 128) with the device stream."""
     gls = spectra_cfg1(3, 128)
