@@ -500,7 +500,7 @@ def run_ours(args, rank: int, world: int) -> dict | None:
     torch.cuda.synchronize()
     kt = {k: _lib.kernel_time(k) for k in ("k_leg_tc", "k_pack_b", "k_transpose32", "k_ring32",
                                            "k_ring32_blu", "k_alm_correlate", "k_iternorm",
-                                           "k_cls2cov", "k_cltovar")}
+                                           "k_refine", "k_cls2cov", "k_cltovar")}
     _lib.timing_enable(False)
     leg_ms, leg_n = kt["k_leg_tc"]
     nalm = (lmax + 1) * (lmax + 2) // 2

@@ -1159,11 +1159,46 @@ struct RefineArgs {
     const glg_epi_dev *edev;  // when set: hv, lam from device memory
 };
 
-// One warp per listed pixel: g = F_0 + 2 Re sum_{m>0} F_m e^{i m phi} in FP64
-// from the FP32 Legendre sums of its ring (lane L takes m = L + 32 j, summed
-// by Horner in z^32 from the top, then times z^L; angles reduced exactly as
-// integer multiples of pi / nph), a fixed-order warp sum, and the lognormal
-// value in FP64 stored over the FP32 one.
+// Float-float ("double-single") arithmetic: a value hi + lo with |lo| <=
+// half an ulp of hi, about 48 significant bits, from FP32 operations only
+// (error-free sums and FMA products, Dekker 1971 / Knuth TAOCP 4.2.2): on
+// this GPU the FP32 pipe issues some 64 times the FP64 one.  The _rn
+// intrinsics keep the compiler from fusing a product into a sum, which
+// would break the error-free transformations.
+struct f2f {
+    float hi, lo;
+};
+__device__ __forceinline__ f2f ff_of(double d) {
+    const float h = (float)d;
+    return {h, (float)(d - (double)h)};
+}
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+// x * c - y * d + f (c, d float-float, f an exact float)
+__device__ __forceinline__ f2f ff_rot(f2f x, f2f c, f2f y, f2f d, float f) {
+    const float p1 = __fmul_rn(x.hi, c.hi), e1 = fmaf(x.hi, c.hi, -p1);
+    const float p2 = __fmul_rn(-y.hi, d.hi), e2 = fmaf(-y.hi, d.hi, -p2);
+    float s1, t1, s2, t2;
+    two_sum(p1, p2, s1, t1);
+    two_sum(s1, f, s2, t2);
+    float lo = __fadd_rn(__fadd_rn(e1, e2), __fadd_rn(t1, t2));
+    lo = fmaf(x.hi, c.lo, lo);
+    lo = fmaf(x.lo, c.hi, lo);
+    lo = fmaf(-y.hi, d.lo, lo);
+    lo = fmaf(-y.lo, d.hi, lo);
+    const float hi = __fadd_rn(s2, lo);
+    return {hi, __fsub_rn(lo, __fsub_rn(hi, s2))};
+}
+
+// One warp per listed pixel: g = F_0 + 2 Re sum_{m>0} F_m e^{i m phi} from
+// the FP32 Legendre sums of its ring (lane L takes m = L + 32 j, summed by
+// Horner in z^32 from the top, then times z^L; angles reduced exactly as
+// integer multiples of pi / nph) in float-float arithmetic, a fixed-order
+// FP64 warp sum, and the lognormal value in FP64 stored over the FP32 one.
+// Lane 0 evaluates z^32 (its own z^L is 1) and hands it to the warp.
 __global__ void __launch_bounds__(256) k_refine(const RefineArgs r) {
     const int lane = threadIdx.x & 31;
     const int n0 = r.hdr[1];
@@ -1174,20 +1209,22 @@ __global__ void __launch_bounds__(256) k_refine(const RefineArgs r) {
         const int p = ring < r.npairs ? ring : r.nrings - 1 - ring;
         const int64_t nph = r.nph[p], a1 = 2LL * k + r.half[p];  // phi = pi a1 / nph
         const float2 *F = r.Ft + ((int64_t)map * r.nrings + ring) * (r.mmax + 1);
-        double zc, zs, lc, ls;
-        sincospi((double)((32 * a1) % (2 * nph)) / (double)nph, &zs, &zc);     // z^32
-        sincospi((double)((lane * a1) % (2 * nph)) / (double)nph, &ls, &lc);   // z^L
-        double sr = 0.0, si = 0.0;
+        double c, sn;
+        sincospi((double)(((lane ? lane : 32) * a1) % (2 * nph)) / (double)nph, &sn, &c);
+        const double zc64 = __shfl_sync(0xffffffffu, c, 0), zs64 = __shfl_sync(0xffffffffu, sn, 0);
+        const double lc = lane ? c : 1.0, ls = lane ? sn : 0.0;  // z^L
+        const f2f zc = ff_of(zc64), zs = ff_of(zs64);
+        f2f sr = {0.f, 0.f}, si = {0.f, 0.f};
         const int jt = (r.mmax - lane) >= 0 ? (r.mmax - lane) / 32 : -1;
         for (int j = jt; j >= 0; --j) {
             const int m = lane + 32 * j;
             const float2 f = F[m];
-            const double cm = m ? 2.0 : 1.0;
-            const double tr = fma(sr, zc, fma(-si, zs, cm * (double)f.x));
-            si = fma(sr, zs, fma(si, zc, cm * (double)f.y));
+            const float cm = m ? 2.f : 1.f;  // exact scalings
+            const f2f tr = ff_rot(sr, zc, si, zs, cm * f.x);
+            si = ff_rot(sr, zs, si, {-zc.hi, -zc.lo}, cm * f.y);  // sr zs + si zc + cm f.y
             sr = tr;
         }
-        double v = sr * lc - si * ls;
+        double v = ((double)sr.hi + (double)sr.lo) * lc - ((double)si.hi + (double)si.lo) * ls;
         for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
         if (lane == 0) {
             const int64_t start = ring < r.npairs ? r.startN[p] : r.startS[p];
