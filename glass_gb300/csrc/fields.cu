@@ -308,7 +308,7 @@ __global__ void k_alm_correlate(const T *__restrict__ w, const int nshell, const
 
 // The fast form's window sum with the variate window in registers: the
 // same elements, sums and summation order as k_alm_correlate<float2, float>,
-// for windows k + 1 <= WT.  One warp per l and 32 consecutive m (a block: 8
+// for windows k + 1 <= WT <= 40.  One warp per l and 32 consecutive m (a block: 8
 // l x 32 m), so the warp's lanes share every w coefficient: per group of
 // CR_SB shells the warp stages its l's w rows into its own shared memory,
 // right-aligned in rows of WT coefficients (slot j holds the coefficient of
@@ -325,7 +325,7 @@ __global__ void __launch_bounds__(32 * CR_WARPS, 2)
     k_alm_correlate_rw(const float *__restrict__ w, const int nshell, const int lmax, const int k, const int64_t t0,
                        const float2 *__restrict__ z, const int64_t z_first, const uint64_t seed,
                        const uint64_t sid_base, float2 *__restrict__ alm) {
-    static_assert(WT % CR_SB == 0 && WT % 4 == 0 && WT <= 64, "window slots");
+    static_assert(WT % CR_SB == 0 && WT % 4 == 0 && WT <= 40, "window slots");
     __shared__ __align__(16) float wsm[CR_WARPS][CR_SB][WT];
     __shared__ __align__(16) float2 zsm[CR_WARPS][CR_SB][32];
     const int kp = k + 1;
@@ -365,28 +365,41 @@ __global__ void __launch_bounds__(32 * CR_WARPS, 2)
             }
         }
     }
-    // w rows of shells ub .. ub + nsb - 1 (lanes over the slots) and their variates
+    // w rows of shells ub .. ub + CR_SB - 1 (lanes over the slots) into
+    // registers, zero where absent: loaded one group ahead, so that the
+    // loads are in flight while the current group's variates and sums run
+    constexpr int NH = (WT + 31) / 32;
+    float pre[CR_SB][NH];
+    auto load_rows = [&](int ub) {
+#pragma unroll
+        for (int sb = 0; sb < CR_SB; ++sb) {
+            const int64_t t = t0 + ub + sb;
+            const int dmax = t < k ? (int)t : k;
+            const float *row = w + ((size_t)(ub + sb) * L + l) * kp + k;
+#pragma unroll
+            for (int h = 0; h < NH; ++h) {
+                const int j = lane + 32 * h, d = WT - 1 - j;
+                pre[sb][h] = (ub + sb < nshell && j < WT && d <= dmax) ? row[-d] : 0.f;
+            }
+        }
+    };
+    // the staged rows and the variates of shells ub .. ub + nsb - 1
     auto stage = [&](int ub, int nsb) {
         __syncwarp();  // the previous group's rows and variates are read
 #pragma unroll
         for (int sb = 0; sb < CR_SB; ++sb) {
-            if (sb < nsb) {
-                const int64_t t = t0 + ub + sb;
-                const int dmax = t < k ? (int)t : k;
-                const float *row = w + ((size_t)(ub + sb) * L + l) * kp + k;
 #pragma unroll
-                for (int j = lane; j < WT; j += 32) {
-                    const int d = WT - 1 - j;
-                    wr[sb][j] = d <= dmax ? row[-d] : 0.f;
-                }
-            }
+            for (int h = 0; h < NH; ++h)
+                if (lane + 32 * h < WT) wr[sb][lane + 32 * h] = pre[sb][h];
         }
+        load_rows(ub + CR_SB);
         if (valid) {
 #pragma unroll 1
             for (int sb = 0; sb < nsb; ++sb) zc[sb * 32] = fetch(t0 + ub + sb);
         }
         __syncwarp();
     };
+    load_rows(0);
     // shell u, row sb: the window sum, oldest variate first; slot(j) is the
     // register of the variate whose coefficient sits in row slot j
     auto shell = [&](int u, int sb, auto slot) {
@@ -546,11 +559,11 @@ extern "C" int glg_alm_correlate(const void *w, int nshell, int lmax, int k, int
     while (threads > CT_L && smem_for(threads) > 200 * 1024) threads /= 2;
     const size_t smem = smem_for(threads);
     cudaStream_t st = (cudaStream_t)stream;
-    if (dtype == GLG_F32 && window <= 48) {  // the fast form's register window
+    if (dtype == GLG_F32 && window <= 40) {  // the fast form's register window
         const dim3 g2((lmax + CR_WARPS) / CR_WARPS, (lmax + 32) / 32);
         using KR = void (*)(const float *, int, int, int, int64_t, const float2 *, int64_t, uint64_t, uint64_t, float2 *);
-        static const KR kr[6] = {k_alm_correlate_rw<8>,  k_alm_correlate_rw<16>, k_alm_correlate_rw<24>,
-                                 k_alm_correlate_rw<32>, k_alm_correlate_rw<40>, k_alm_correlate_rw<48>};
+        static const KR kr[5] = {k_alm_correlate_rw<8>, k_alm_correlate_rw<16>, k_alm_correlate_rw<24>,
+                                 k_alm_correlate_rw<32>, k_alm_correlate_rw<40>};
         GLG_LAUNCH_SCOPE("k_alm_correlate", st);
         kr[(window + 7) / 8 - 1]<<<g2, 32 * CR_WARPS, 0, st>>>((const float *)w, nshell, lmax, k, t0,
                                                                   (const float2 *)z, z_first, seed, sid_base,

@@ -205,9 +205,9 @@ def _correlate(g, w, nshell, lmax, k, t0, z, z_first, dtype, out):
 
 @pytest.mark.parametrize(("nshell", "lmax", "k", "split", "hostz"),
                          [(12, 300, 5, 5, False), (12, 300, 5, 7, True), (50, 200, 39, 23, False),
-                          (30, 130, 0, 11, False), (9, 64, 47, 4, True), (20, 70, 60, 9, False)])
+                          (30, 130, 0, 11, False), (9, 64, 39, 4, True), (9, 64, 47, 4, True), (20, 70, 60, 9, False)])
 def test_alm_correlate_fast_window(g, nshell, lmax, k, split, hostz):
-    """The fast form's correlated alm (register window for k + 1 <= 48, the
+    """The fast form's correlated alm (register window for k + 1 <= 40, the
     shared-memory window above): within FP32 rounding of the FP64 sums, and a
     call split into two groups of shells (the second drawing its window of
     earlier variates again) gives the same bits as one call."""
