@@ -733,14 +733,22 @@ __global__ void __launch_bounds__(256) k_pack_b(int mmax, int lmax, int nmaps, i
                                                 const float2 *__restrict__ alm, const float2 *__restrict__ alm2,
                                                 int nsplit, float *__restrict__ bpack) {
     const int64_t idx = blockIdx.x * 256LL + threadIdx.x;
-    if (idx >= ngroups * 2 * N) return;
+    // 2N is a multiple of 32: a warp's items share one group gg, and the
+    // warp finds its m (the last m with goff[m] <= gg) by a 32-way search,
+    // each lane testing one of 32 candidates per round
     const int64_t gg = idx / (2 * N);
+    if (gg >= ngroups) return;  // whole warps
     const int item = (int)(idx - gg * 2 * N);
-    int lo = 0, hi = mmax + 1;  // m = the last m with goff[m] <= gg
+    const int lane = (int)(threadIdx.x & 31);
+    int lo = 0, hi = mmax + 1;  // goff[lo] <= gg < goff[hi] (goff[mmax + 1] = ngroups)
     while (hi - lo > 1) {
-        const int mid = (lo + hi) >> 1;
-        if (goff[mid] <= gg) lo = mid;
-        else hi = mid;
+        const int step = (hi - lo + 31) / 32;
+        const int c = lo + lane * step;
+        const bool ok = c < hi && goff[c] <= gg;
+        const unsigned bal = __ballot_sync(0xffffffffu, ok);
+        const int last = 31 - __clz(bal);  // lane 0 tests lo itself: at least one lane holds
+        lo = lo + last * step;
+        hi = lo + step < hi ? lo + step : hi;
     }
     const int m = lo;
     const int g = (int)(gg - goff[m]);
