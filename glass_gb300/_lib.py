@@ -61,6 +61,7 @@ _SIGNATURES = {
     "glg_philox_normals": ([c_u64, c_u64, c_i64, c_i64, c_i, c_p, c_p], c_i),
     "glg_cls2cov": ([c_p, c_p, c_i, c_i, c_i, c_p, c_p, c_p, c_p], c_i),
     "glg_alm_correlate": ([c_p, c_i, c_i, c_i, c_i64, c_p, c_i64, c_u64, c_u64, c_i, c_p, c_p], c_i),
+    "glg_gather_host": ([c_p, c_p, c_i, c_p, c_i], c_i),
     "glg_multalm": ([c_p, c_p, c_i, c_i, c_p, c_p], c_i),
     "glg_almxfl": ([c_p, c_p, c_i, c_i, c_i, c_i, c_p, c_p], c_i),
     "glg_autotune_fast": ([c_p, c_i, c_p, c_p, c_sz, c_p], c_i),

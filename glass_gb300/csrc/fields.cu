@@ -3,6 +3,10 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include <string.h>
+
+#include <algorithm>
+#include <thread>
 #include <vector>
 
 #include "glg_internal.cuh"
@@ -537,6 +541,36 @@ extern "C" int glg_philox_normals(uint64_t seed, uint64_t sid, int64_t offset, i
     GLG_LAUNCH_SCOPE("k_philox_normals", (cudaStream_t)stream);
     k_philox_normals<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(seed, sid, offset, n, dtype, out);
     GLG_CHECK_LAUNCH("k_philox_normals");
+    return GLG_OK;
+}
+
+extern "C" int glg_gather_host(const void *const *src, const int64_t *bytes, int n, void *dst, int nthreads) {
+    GLG_REQUIRE(n >= 0, "glg_gather_host: negative count");
+    if (n == 0) return GLG_OK;
+    GLG_REQUIRE(src && bytes && dst, "glg_gather_host: null pointer");
+    std::vector<int64_t> off(n + 1, 0);
+    for (int i = 0; i < n; ++i) {
+        GLG_REQUIRE(bytes[i] >= 0 && (bytes[i] == 0 || src[i]), "glg_gather_host: bad buffer");
+        off[i + 1] = off[i] + bytes[i];
+    }
+    const int64_t total = off[n];
+    // at least 2 MB a thread: below that, starting a thread costs more than it copies
+    int nt = nthreads < 1 ? 1 : (nthreads > 32 ? 32 : nthreads);
+    while (nt > 1 && total / nt < ((int64_t)2 << 20)) --nt;
+    // thread t copies destination bytes [total t / nt, total (t + 1) / nt)
+    auto run = [&](int t) {
+        const int64_t b0 = total * t / nt, b1 = total * (t + 1) / nt;
+        int i = (int)(std::upper_bound(off.begin(), off.end(), b0) - off.begin()) - 1;
+        for (int64_t b = b0; b < b1; ++i) {
+            const int64_t e = off[i + 1] < b1 ? off[i + 1] : b1;
+            if (e > b) memcpy((char *)dst + b, (const char *)src[i] + (b - off[i]), (size_t)(e - b));
+            b = e;
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nt; ++t) pool.emplace_back(run, t);
+    run(0);
+    for (auto &th : pool) th.join();
     return GLG_OK;
 }
 

@@ -253,10 +253,14 @@ class _FieldBatcher:
         if self.numpy_out:
             # concatenated straight into pinned memory: one asynchronous copy
             # (the caching host allocator keeps the buffer until it is done)
-            parts = gls if all(isinstance(g, np.ndarray) and g.dtype == np.float64 and g.ndim == 1 for g in gls) \
-                else [np.asarray(g, dtype=np.float64).reshape(-1) for g in gls if g is not None]
+            parts = [g if (isinstance(g, np.ndarray) and g.dtype == np.float64 and g.ndim == 1
+                           and g.flags.c_contiguous) else np.ascontiguousarray(g, dtype=np.float64).reshape(-1)
+                     for g in gls if g is not None]
             flat_h = torch.empty(int(offs[-1]), dtype=torch.float64, pin_memory=True)
-            np.concatenate(parts, out=flat_h.numpy())
+            # one host copy split over threads (glg_gather_host), then one upload
+            src = (ctypes.c_void_p * len(parts))(*[q.ctypes.data for q in parts])
+            nb = (ctypes.c_int64 * len(parts))(*[q.nbytes for q in parts])
+            check(lib().glg_gather_host(src, nb, len(parts), c_p(flat_h.data_ptr()), 8), "glg_gather_host")
             flat = flat_h.to(self.device, non_blocking=True)
         else:
             dev, f64 = self.device, torch.float64

@@ -106,6 +106,14 @@ int glg_cls2cov(const double *flat, const int64_t *offs, int nf, int nl, int nc,
                 double *var, uint64_t *status, void *stream);
 
 /*
+ * Host-only: concatenate n host buffers (src[i], bytes[i] bytes each) into
+ * dst, in order, split over up to nthreads host threads (the copy of the
+ * spectra into one page-locked block before their upload, in place of the
+ * single-threaded numpy concatenation).  No device call.
+ */
+int glg_gather_host(const void *const *src, const int64_t *bytes, int n, void *dst, int nthreads);
+
+/*
  * Standard complex normals of the counter-based stream that replaces the
  * reference's numpy draw standard_normal((z_size, 2)) @ [1, 1j]
  * (glass/fields.py:407; generator seam glass/rng.py:21-55).  Element e of

@@ -86,3 +86,29 @@ def test_host_output_runs_tile_the_rings_and_pixels():
         assert all(a[1] == b[0] for a, b in zip(bands, bands[1:]))
     assert lib.glg_host_output_runs(0, out.ctypes.data, 8) == _lib.GLG_ERR_INVALID
     assert lib.glg_host_output_runs(2048, out.ctypes.data, 7) == _lib.GLG_ERR_INVALID
+
+
+def test_gather_host_concatenates_in_order():
+    """glg_gather_host (host memcpy split over threads, no device call) equals
+    numpy's concatenation, for thread counts whose byte ranges start and end
+    inside pieces, with empty pieces, and rejects bad arguments."""
+    import numpy as np
+
+    from glass_gb300 import _lib
+
+    lib = _lib.load_library(require_gpu=False)
+    rng = np.random.default_rng(0)
+    for sizes in ([4097] * 820, [0, 5, 0, 300_000, 1, 0, 700_001, 3], [1_000_003]):
+        parts = [rng.standard_normal(n) for n in sizes]
+        ref = np.concatenate(parts)
+        for nt in (1, 3, 8, 64):
+            out = np.full(ref.size, np.nan)
+            src = (ctypes.c_void_p * len(parts))(*[p.ctypes.data for p in parts])
+            nb = (ctypes.c_int64 * len(parts))(*[p.nbytes for p in parts])
+            assert lib.glg_gather_host(src, nb, len(parts), out.ctypes.data, nt) == _lib.GLG_OK
+            np.testing.assert_array_equal(out, ref)
+    assert lib.glg_gather_host(None, None, 0, None, 4) == _lib.GLG_OK
+    assert lib.glg_gather_host(None, None, 2, None, 4) == _lib.GLG_ERR_INVALID
+    bad = (ctypes.c_int64 * 1)(-8)
+    src = (ctypes.c_void_p * 1)(8)
+    assert lib.glg_gather_host(src, bad, 1, ctypes.c_void_p(8), 1) == _lib.GLG_ERR_INVALID
