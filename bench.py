@@ -54,7 +54,7 @@ WORKLOAD = dict(workload="40-shell lognormal field generation, nside 2048, lmax 
                 lmax=4096)
 
 
-def spectra_cfg3(nshell: int, lmax: int, seed: int = 0):
+def spectra_powerlaw13(nshell: int, lmax: int, seed: int = 0):
     rng = np.random.default_rng(seed)
     amp = 10 ** rng.uniform(-3, -1, nshell)
     lam = rng.uniform(0.5, 3.0, nshell)
@@ -65,7 +65,7 @@ def spectra_cfg3(nshell: int, lmax: int, seed: int = 0):
     return gls, lam
 
 
-def spectra_cfg2(nshell: int, lmax: int, seed: int = 0):
+def spectra_damped12(nshell: int, lmax: int, seed: int = 0):
     """Request spectra of the serving workload: A_i (l+1)^-1.2 e^{-(l/800)^2},
     A_i log-uniform in [1e-3, 1e-1], correlation exp(-|i-j|/1.5), shifts
     uniform in [0.5, 2]."""
@@ -89,7 +89,7 @@ def _serving_requests(n: int, seed: int):
     for i in range(n):
         nside = int(rng.choice([128, 256, 512, 1024]))
         nshell = int(rng.integers(3, 21))
-        gls, lam = spectra_cfg2(nshell, 2 * nside, seed=seed * 100003 + i)
+        gls, lam = spectra_damped12(nshell, 2 * nside, seed=seed * 100003 + i)
         reqs.append(serving.Request(gls=gls, nside=nside, shifts=[float(x) for x in lam], seed=1000 + i))
     return reqs
 
@@ -161,8 +161,8 @@ def run_serving(args) -> dict:
     return out
 
 
-def run_cfg2(steps: int = 3) -> dict:
-    """Config 2: 10 correlated lognormal shells at nside 512 / lmax 1024
+def run_shells10(steps: int = 3) -> dict:
+    """10 correlated lognormal shells at nside 512 / lmax 1024
     (spectra A_i (l+1)^-1.2 e^{-(l/800)^2}, correlation e^{-|i-j|/1.5},
     shifts in [0.5, 2], from seed 0), device-resident.  Plain FP64 and fast
     forms timed with CUDA events (best of `steps`), the fast form's error per
@@ -174,7 +174,7 @@ def run_cfg2(steps: int = 3) -> dict:
     import glass_gb300 as g
 
     nshell, nside, lmax = 10, 512, 1024
-    gls_np, lam = spectra_cfg2(nshell, lmax, seed=0)
+    gls_np, lam = spectra_damped12(nshell, lmax, seed=0)
     gls = [torch.as_tensor(c, device="cuda") for c in gls_np]
     fields = [g.grf.Lognormal(float(x)) for x in lam]
     out = {"workload": "10-shell lognormal field generation, nside 512, lmax 1024", "nshell": nshell,
@@ -229,8 +229,8 @@ def run_cfg2(steps: int = 3) -> dict:
     return out
 
 
-def run_cfg5(nshell: int = 60, nside: int = 4096, lmax: int = 8192) -> dict:
-    """Config 5: 60 lognormal shells at nside 4096 / lmax 8192 (config-3
+def run_shells60(nshell: int = 60, nside: int = 4096, lmax: int = 8192) -> dict:
+    """60 lognormal shells at nside 4096 / lmax 8192 (the 40-shell benchmark's
     spectra, seed 5) streamed through the fast form in groups of shells (as
     many as a 48 GB workspace allows), each shell consumed as it comes: its
     lognormal map added into the cumulative convergence (mean of the shells)
@@ -247,7 +247,7 @@ def run_cfg5(nshell: int = 60, nside: int = 4096, lmax: int = 8192) -> dict:
 
     _lib.clear_plans()
     torch.cuda.empty_cache()
-    gls_np, lam = spectra_cfg3(nshell, lmax, seed=5)
+    gls_np, lam = spectra_powerlaw13(nshell, lmax, seed=5)
     gls = [torch.as_tensor(c, device="cuda") for c in gls_np]
     fields = [g.grf.Lognormal(float(x)) for x in lam]
     npix = 12 * nside * nside
@@ -458,7 +458,7 @@ def run_ours(args, rank: int, world: int) -> dict | None:
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
     torch.cuda.set_device(dev)
     nshell, nside, lmax = args.nshell, args.nside, args.lmax
-    gls_np, lam = spectra_cfg3(nshell, lmax)
+    gls_np, lam = spectra_powerlaw13(nshell, lmax)
     gls_dev = [torch.as_tensor(c, device=dev) for c in gls_np]
     ell = np.arange(lmax + 1)
     shell_variances = [np.sum((2 * ell + 1) * gls_np[k * (k + 1) // 2]) / (4 * np.pi) for k in range(nshell)]
@@ -523,7 +523,7 @@ def run_ours(args, rank: int, world: int) -> dict | None:
                 "traffic": traffic, "traffic_unit": "bytes per launch", "peak_note": peak_note, "passes": PASSES,
                 "issued_frac": (PASSES * achieved / peak_tf) if achieved else None,
                 "algorithmic_flops_per_launch": flops}
-    # the same figure against the driver-measured bf16 GEMM rate halved (the
+    # the same figure against the measured bf16 GEMM rate halved (the
     # tensor pipe's tf32 rate is half its bf16 rate)
     bf_half = peaks.get("bf16_tflops", 1900.0) / 2.0
     if traffic:  # the same launch against the measured copy bandwidth
@@ -616,13 +616,13 @@ def run_ours(args, rank: int, world: int) -> dict | None:
                "d2h_bytes_per_step": d2h}
 
     serving = run_serving(args) if (args.serving > 0 or args.serving_plain > 0) else None
-    cfg2 = run_cfg2() if args.cfg2 else None
-    cfg5 = None
-    if args.cfg5:
+    shells10 = run_shells10() if args.shells10 else None
+    shells60 = None
+    if args.shells60:
         try:
-            cfg5 = run_cfg5()
+            shells60 = run_shells60()
         except Exception as exc:  # noqa: BLE001 - recorded, the headline stands
-            cfg5 = {"error": f"{type(exc).__name__}: {exc}"}
+            shells60 = {"error": f"{type(exc).__name__}: {exc}"}
     cpu = cpu_baseline(args) if args.cpu_baseline else None
     res = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -634,7 +634,8 @@ def run_ours(args, rank: int, world: int) -> dict | None:
         "pixels_per_sec": value * npix, "e2e": e2e, "plain_fp64": plain, "roofline": roofline, "points": points,
         "kernel_ms_per_step": {k: v[0] for k, v in kt.items()},
         "kernel_launches_per_step": {k: v[1] for k, v in kt.items()}, "gpu_launches": launches,
-        "clocks": clk.summary(), "cpu_baseline": cpu, "serving": serving, "cfg2": cfg2, "cfg5": cfg5,
+        "clocks": clk.summary(), "cpu_baseline": cpu, "serving": serving,
+        "shells10_nside512": shells10, "shells60_nside4096": shells60,
     }
     return res
 
@@ -646,7 +647,7 @@ def cpu_baseline(args) -> dict:
     import oracle.fields as of
     import oracle.rng as orng
 
-    gls, lam = spectra_cfg3(args.nshell, args.lmax)
+    gls, lam = spectra_powerlaw13(args.nshell, args.lmax)
     sample = max(1, args.cpu_shells)
     a = time.perf_counter()
     it = of.generate_lognormal(gls, args.nside, list(lam), ncorr=None,
@@ -712,14 +713,14 @@ def ncu_case(which: str) -> None:
     if which == "alm":
         from glass_gb300 import fields
 
-        gls = [torch.as_tensor(c, device="cuda") for c in spectra_cfg3(40, 4096)[0]]
+        gls = [torch.as_tensor(c, device="cuda") for c in spectra_powerlaw13(40, 4096)[0]]
         b = fields._FieldBatcher(gls, 2048, None, g.rng.Generator(42), "fast")
         for _ in range(2):
             alm = b.alm(0, 40)
             torch.cuda.synchronize()
         print("ncu case done", float(alm.abs().max()))
         return
-    gls, lam = spectra_cfg2(8, 2048, seed=1)
+    gls, lam = spectra_damped12(8, 2048, seed=1)
     gls = [torch.as_tensor(c, device="cuda") for c in gls]
     fields = [g.grf.Lognormal(float(x)) for x in lam]
     for _ in range(2):
@@ -744,10 +745,10 @@ def main() -> None:
     ap.add_argument("--serving-plain", type=int, default=60,
                     help="requests of the FP64 unbatched serving comparison (0: off)")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
-    ap.add_argument("--no-cfg2", dest="cfg2", action="store_false",
-                    help="skip the config-2 record (10 shells, nside 512)")
-    ap.add_argument("--no-cfg5", dest="cfg5", action="store_false",
-                    help="skip the config-5 record (60 shells, nside 4096, streamed)")
+    ap.add_argument("--no-shells10", dest="shells10", action="store_false",
+                    help="skip the 10-shell nside-512 record")
+    ap.add_argument("--no-shells60", dest="shells60", action="store_false",
+                    help="skip the 60-shell nside-4096 streamed record")
     ap.add_argument("--no-points", dest="points", action="store_false",
                     help="skip the galaxy counts / positions aside")
     ap.add_argument("--ncu-case", nargs="?", const="sht", choices=["sht", "alm", "leg"],

@@ -42,13 +42,13 @@ def cuda_lib():
     return _lib.lib()
 
 
-def spectra_cfg1(nshell: int, lmax: int):
+def spectra_powerlaw15(nshell: int, lmax: int):
     ell = np.arange(lmax + 1)
     auto = 1e-2 * (ell + 1.0) ** -1.5
     return [np.exp(-abs(i - j) / 2) * auto for i in range(nshell) for j in range(i, -1, -1)]
 
 
-def spectra_cfg2(nshell: int, lmax: int, seed: int = 0):
+def spectra_damped12(nshell: int, lmax: int, seed: int = 0):
     rng = np.random.default_rng(seed)
     amp = 10 ** rng.uniform(-3, -1, nshell)
     lam = rng.uniform(0.5, 2.0, nshell)

@@ -32,7 +32,7 @@ HERE = pathlib.Path(__file__).resolve().parent
 ROOT = HERE.parent.parent
 
 
-def spectra_cfg1(nshell: int, lmax: int) -> list[np.ndarray]:
+def spectra_powerlaw15(nshell: int, lmax: int) -> list[np.ndarray]:
     """Auto C_l = 1e-2 (l+1)^-1.5, cross exp(-|i-j|/2) sqrt(C^ii C^jj), GLASS order."""
     ell = np.arange(lmax + 1)
     auto = 1e-2 * (ell + 1.0) ** -1.5
@@ -43,7 +43,7 @@ def spectra_cfg1(nshell: int, lmax: int) -> list[np.ndarray]:
     return gls
 
 
-def spectra_cfg2(nshell: int, lmax: int, seed: int = 0):
+def spectra_damped12(nshell: int, lmax: int, seed: int = 0):
     """A_i log-uniform [1e-3, 1e-1]; C^ii = A_i (l+1)^-1.2 exp(-(l/800)^2); corr exp(-|i-j|/1.5)."""
     rng = np.random.default_rng(seed)
     amp = 10 ** rng.uniform(-3, -1, nshell)
@@ -92,8 +92,8 @@ def main() -> None:
                 out[f"iternorm_k{k}_{nd}_row{i}"] = np.asarray(w)
                 out[f"iternorm_k{k}_{nd}_in{i}"] = np.asarray(rows[i])
 
-    # iternorm on cls2cov rows of a 6-shell / lmax-40 config-2-like spectrum set
-    gls6, _ = spectra_cfg2(6, 40, seed=3)
+    # iternorm on cls2cov rows of a 6-shell / lmax-40 damped power-law spectrum set
+    gls6, _ = spectra_damped12(6, 40, seed=3)
     for nc in (5, 2):
         covs = [np.array(c, copy=True) for c in glass.cls2cov(gls6, 41, 6, nc)]
         ws = list(glass.iternorm(iter(covs)))
@@ -104,7 +104,7 @@ def main() -> None:
 
     # _generate_grf alm and generate_lognormal maps, 3 shells cfg-1 spectra
     nside, lmax = 8, 16
-    gls3 = spectra_cfg1(3, lmax)
+    gls3 = spectra_powerlaw15(3, lmax)
     for i, g in enumerate(gls3):
         out[f"gls3_{i}"] = g
     for tag, ncorr in (("all", None), ("nc1", 1)):
@@ -115,7 +115,7 @@ def main() -> None:
         out[f"generate_maps_{tag}"] = np.stack(maps)
 
     # generate_lognormal (deprecated wrapper, shift 1.0) on 4 cfg-2 shells
-    gls4, _ = spectra_cfg2(4, 24, seed=5)
+    gls4, _ = spectra_damped12(4, 24, seed=5)
     for i, g in enumerate(gls4):
         out[f"gls4_{i}"] = g
     captured.clear()

@@ -1,5 +1,5 @@
-"""GPU parity at the benchmarked sizes: config 2 (10 shells, nside 512,
-lmax 1024) and config 3 (nside 2048, lmax 4096), against the oracle.
+"""GPU parity at the benchmarked sizes: 10 shells at nside 512 / lmax 1024 and
+the nside 2048 / lmax 4096 transform of the 40-shell benchmark, against the oracle.
 
 The plain form is FP64 throughout and must match the oracle's FP64 ring SHT
 (C Legendre sums + numpy FFTs, pinned against brute-force sums at small
@@ -16,7 +16,7 @@ import pytest
 import oracle.fields as of
 import oracle.rng as orng
 import oracle.sht as osht
-from tests.conftest import rel_err, spectra_cfg2
+from tests.conftest import rel_err, spectra_damped12
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-12
@@ -45,14 +45,14 @@ def rel_rms(a, b) -> float:
     return float(np.sqrt(np.mean((a - b) ** 2)) / np.sqrt(np.mean(b**2)))
 
 
-def test_alm2map_plain_cfg2_size(g):
+def test_alm2map_plain_nside512(g):
     nside, lmax = 512, 1024
     alm = _alm(lmax, 10, seed=21)
     got = g.healpix.alm2map(list(alm), nside, pol=False)
     assert rel_err(got, osht.alm2map(alm, nside, lmax)) < TOL
 
 
-def test_alm2map_plain_and_fast_cfg3_size(g):
+def test_alm2map_plain_and_fast_nside2048(g):
     import torch
 
     from glass_gb300 import healpix as hp
@@ -84,11 +84,11 @@ def test_fast_bluestein_lengths_3_pow2(g):
     assert np.max(np.abs(fast - plain)) < 2e-5 * scale
 
 
-def test_generate_cfg2_vs_oracle(g):
-    """Config 2: 10 correlated lognormal shells at nside 512 / lmax 1024,
+def test_generate_10_shells_nside512_vs_oracle(g):
+    """10 correlated lognormal shells at nside 512 / lmax 1024,
     device Philox stream; plain to 1e-12 of the oracle, fast to 1e-6 RMS."""
     nshell, nside, lmax = 10, 512, 1024
-    gls, lam = spectra_cfg2(nshell, lmax, seed=0)
+    gls, lam = spectra_damped12(nshell, lmax, seed=0)
     fields = [g.grf.Lognormal(float(x)) for x in lam]
     ref = np.stack(list(of.generate_lognormal(
         gls, nside, [float(x) for x in lam], z_of_shell=lambda t, s: orng.complex_normals(42, t, 0, s))))
@@ -100,7 +100,7 @@ def test_generate_cfg2_vs_oracle(g):
         assert rel_rms(fast[s], ref[s]) < FAST_RMS
 
 
-def test_map2alm_and_from_convergence_cfg2_size(g):
+def test_map2alm_and_from_convergence_nside512(g):
     nside = 512
     lmax = 3 * nside - 1
     alm = _alm(1000, 1, seed=23, slope=-1.5)[0] * 1e-2
@@ -124,23 +124,23 @@ def test_map2alm_and_from_convergence_cfg2_size(g):
     assert rel_err(gamma, g0 + 1j * g1) < 1e-11
 
 
-def _spectra_cfg3(amps, lmax, corr=3.0):
+def _spectra_powerlaw13(amps, lmax, corr=3.0):
     ell = np.arange(lmax + 1)
     auto = [a * (ell + 1.0) ** -1.3 for a in amps]
     n = len(amps)
     return [np.exp(-abs(i - j) / corr) * np.sqrt(auto[i] * auto[j]) for i in range(n) for j in range(i, -1, -1)]
 
 
-def test_generate_fast_high_variance_cfg3(g):
-    """Config-3 spectra (A_i (l+1)^-1.3, correlation e^{-|i-j|/3}) at the
-    top of config 3's amplitude range, nside 2048 / lmax 4096: the shell with
+def test_generate_fast_high_variance_nside2048(g):
+    """The benchmark's spectra (A_i (l+1)^-1.3, correlation e^{-|i-j|/3}) at
+    the top of their amplitude range, nside 2048 / lmax 4096: the shell with
     A = 0.1 has sigma^2 = 7.5, where the lognormal transform amplifies the
     Gaussian field's error most.  Every fast lognormal shell within 1e-6
     relative RMS of the FP64 form (which matches the oracle to 1e-12 at this
-    size, test_alm2map_plain_and_fast_cfg3_size)."""
+    size, test_alm2map_plain_and_fast_nside2048)."""
     nside, lmax = 2048, 4096
     amps = [0.1, 0.08, 0.05]
-    gls = _spectra_cfg3(amps, lmax)
+    gls = _spectra_powerlaw13(amps, lmax)
     lam = [2.7, 0.6, 1.5]
     fields = [g.grf.Lognormal(x) for x in lam]
     var = [float(np.sum((2 * np.arange(lmax + 1) + 1) * gls[k * (k + 1) // 2]) / (4 * np.pi)) for k in range(3)]
@@ -154,7 +154,7 @@ def test_generate_fast_high_variance_cfg3(g):
 def test_accuracy_report(g):
     """The fast form's per-output error report: one record per shell, equal
     to the error computed by hand from the two forms' maps."""
-    gls, lam = spectra_cfg2(4, 128, seed=3)
+    gls, lam = spectra_damped12(4, 128, seed=3)
     fields = [g.grf.Lognormal(float(x)) for x in lam]
     rep = g.accuracy_report(fields, gls, 64, seed=5)
     assert [r["shell"] for r in rep] == [0, 1, 2, 3]
@@ -167,8 +167,8 @@ def test_accuracy_report(g):
         assert abs(r["max_abs"] - np.max(np.abs(fast[s].astype(np.float64) - plain[s]))) < 1e-12
 
 
-def test_cfg5_size_fast_vs_plain_and_counts(g):
-    """Config-5 sizes, nside 4096 / lmax 8192, at two shells: the fast form
+def test_nside4096_fast_vs_plain_and_counts(g):
+    """The streamed 60-shell sizes, nside 4096 / lmax 8192, at two shells: the fast form
     (lambda from the FP32 recurrence -- the P_lm table would take 1.1 TB --
     and Bluestein rings of M = 32768 in global memory) within 1e-6 RMS of the
     FP64 form on Gaussian fields; Poisson galaxy counts (n = 5 per pixel)
@@ -182,7 +182,7 @@ def test_cfg5_size_fast_vs_plain_and_counts(g):
     torch.cuda.empty_cache()
     try:
         nside, lmax = 4096, 8192
-        gls = _spectra_cfg3([0.02, 0.005], lmax)
+        gls = _spectra_powerlaw13([0.02, 0.005], lmax)
         fields = [g.grf.Normal(), g.grf.Normal()]
         gls_d = [torch.as_tensor(c, device="cuda") for c in gls]
         fast = list(g.generate(fields, gls_d, nside, rng=g.rng.Generator(3), form="fast"))

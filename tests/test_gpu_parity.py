@@ -16,7 +16,7 @@ import pytest
 import oracle.fields as of
 import oracle.rng as orng
 import oracle.sht as osht
-from tests.conftest import random_alm, rel_err, spectra_cfg1, spectra_cfg2
+from tests.conftest import random_alm, rel_err, spectra_powerlaw15, spectra_damped12
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-12
@@ -52,7 +52,7 @@ def test_iternorm_bit_exact_vs_oracle(g, golden):
 
 
 def test_iternorm_bit_exact_large_k(g):
-    gls, _ = spectra_cfg2(40, 300, seed=4)
+    gls, _ = spectra_damped12(40, 300, seed=4)
     cov = np.stack([c.copy() for c in of.cls2cov(gls, 301, 40, 39)])
     w, bad = _iternorm_gpu(cov)
     wo, bado = of.iternorm_stack(cov)
@@ -239,8 +239,8 @@ def test_alm_correlate_fast_window(g, nshell, lmax, k, split, hostz):
 
 
 def test_generate_philox_vs_oracle(g):
-    """Config-1 sizes (3 shells, nside 64, lmax 128) with the device stream."""
-    gls = spectra_cfg1(3, 128)
+    """3 shells at nside 64 / lmax 128 with the device stream."""
+    gls = spectra_powerlaw15(3, 128)
     r = g.rng.Generator(42)
     maps = np.stack(list(g.generate_lognormal(gls, 64, rng=r)))
     sid0 = 0
@@ -251,7 +251,7 @@ def test_generate_philox_vs_oracle(g):
 
 def test_generate_batched_matches_per_shell(g):
     """Batched shells (one SHT launch) equal shell-by-shell results."""
-    gls, lam = spectra_cfg2(6, 64, seed=2)
+    gls, lam = spectra_damped12(6, 64, seed=2)
     fields = [g.grf.Lognormal(float(x)) for x in lam]
     a = np.stack(list(g.generate(fields, gls, 32, rng=g.rng.Generator(5))))
     import os
@@ -297,7 +297,7 @@ def test_generate_not_posdef_raises_at_shell(g):
 def test_torch_in_torch_out(g):
     import torch
 
-    gls = [torch.as_tensor(c, device="cuda") for c in spectra_cfg1(2, 16)]
+    gls = [torch.as_tensor(c, device="cuda") for c in spectra_powerlaw15(2, 16)]
     maps = list(g.generate([g.grf.Lognormal(), g.grf.Lognormal()], gls, 8))
     assert all(isinstance(m, torch.Tensor) and m.is_cuda for m in maps)
 
@@ -392,7 +392,7 @@ def test_alm2map_fast_table_and_recurrence_paths(g):
 
 def test_generate_fast_vs_plain(g):
     """Same Philox stream: fast form within 1e-6 RMS of the FP64 plain form."""
-    gls, lam = spectra_cfg2(6, 128, seed=1)
+    gls, lam = spectra_damped12(6, 128, seed=1)
     fields = [g.grf.Lognormal(float(x)) for x in lam]
     plain = np.stack(list(g.generate(fields, gls, 64, rng=g.rng.Generator(3), form="plain")))
     fast = np.stack(list(g.generate(fields, gls, 64, rng=g.rng.Generator(3), form="fast")))
@@ -644,7 +644,7 @@ def test_fast_maps_written_to_host_memory(g, nside, lmax):
     g._lib.host_device_pointer(pinned)  # mapped pinned memory has a device address
     with pytest.raises(ValueError):
         g._lib.host_device_pointer(torch.empty(4))  # pageable memory has none
-    gls, lam = spectra_cfg2(4, 2 * nside)
+    gls, lam = spectra_damped12(4, 2 * nside)
     fields = [g.grf.Lognormal(float(x)) for x in lam]
     a = list(g.generate(fields, gls, nside, rng=g.rng.Generator(3), form="fast"))
     b = list(g.generate(fields, [torch.as_tensor(c, device="cuda") for c in gls], nside, rng=g.rng.Generator(3),

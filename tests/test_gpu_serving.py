@@ -12,13 +12,13 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
-from tests.conftest import spectra_cfg2
+from tests.conftest import spectra_damped12
 
 pytestmark = pytest.mark.gpu
 
 
 def _request(serving, nside, nshell, seed):
-    gls, lam = spectra_cfg2(nshell, 2 * nside, seed=seed)
+    gls, lam = spectra_damped12(nshell, 2 * nside, seed=seed)
     return serving.Request(gls=gls, nside=nside, shifts=[float(x) for x in lam], seed=seed)
 
 

@@ -90,7 +90,7 @@ def test_iternorm_matches_reference(golden):
 def test_iternorm_ulp_distance_to_reference(golden):
     """The oracle's iternorm rows -- bit-exact with the GPU kernel
     (tests/test_gpu_parity.py) -- against the reference's numpy rows on the
-    config-2 covariances: at most 2 ulp apart and about 87 % of the entries
+    the 10-shell covariances: at most 2 ulp apart and about 87 % of the entries
     identical (the sums run in another order than numpy's matmuls)."""
     for nc in (5, 2):
         wo, bad = of.iternorm_stack(golden[f"cls2cov_cfg2_nc{nc}"])

@@ -82,7 +82,7 @@ def test_fast_spin_table_budget(g):
 
 @pytest.mark.parametrize("nside", [64, 512])
 def test_from_convergence_fast_vs_plain(g, nside):
-    """Config-2 size at nside 512 (lmax 1535): potential, deflection and the
+    """The 10-shell size at nside 512 (lmax 1535): potential, deflection and the
     discretized shear of a convergence map, fast vs FP64, <= 1e-6 RMS each."""
     lmax = 3 * nside - 1
     alm = _red_alm(lmax, 9, slope=-1.5) * 1e-2
