@@ -310,11 +310,12 @@ __global__ void k_alm_correlate(const T *__restrict__ w, const int nshell, const
     }
 }
 
-// The fast form's window sum with the variate window in registers: the
-// same elements, sums and summation order as k_alm_correlate<float2, float>,
-// for windows k + 1 <= WT <= 40.  One warp per l and 32 consecutive m (a block: 8
-// l x 32 m), so the warp's lanes share every w coefficient: per group of
-// CR_SB shells the warp stages its l's w rows into its own shared memory,
+// The fast form's window sum (glass/fields.py:401-425) with the variate
+// window in registers: the same elements, sums and summation order as
+// k_alm_correlate<float2, float>, for windows k + 1 <= WT <= 40.  One warp
+// per l and 32 consecutive m (a block: 8 l x 32 m), so the warp's lanes
+// share every w coefficient: per group of CR_SB shells the warp stages its
+// l's w rows (loaded into registers one group ahead) into its own shared memory,
 // right-aligned in rows of WT coefficients (slot j holds the coefficient of
 // z_{t-(WT-1-j)}, zero where that variate is absent or older than the
 // window: adding 0 * z leaves the running sum's bits unchanged), and each
