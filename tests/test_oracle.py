@@ -58,6 +58,57 @@ def test_extended_range_large_m():
     assert np.abs(F).max() > 1e-3  # non-negligible near the equator
 
 
+def _lambda_mp(l, m, z):  # noqa: E741
+    """Normalised lambda_lm(z) (Condon-Shortley phase) in 50-digit arithmetic:
+    the closed form of lambda_mm from sqrt(1 - z^2), then the three-term
+    recurrence in l."""
+    mp = pytest.importorskip("mpmath").mp
+    mp.dps = 50
+    z = mp.mpf(z)
+    v = mp.mpf(1) / (4 * mp.pi)
+    for k in range(1, m + 1):
+        v *= mp.mpf(2 * k - 1) / (2 * k)
+    p2 = (-1) ** m * mp.sqrt((2 * m + 1) * v) * mp.sqrt(1 - z * z) ** m
+    if l == m:
+        return p2
+    p1 = mp.sqrt(2 * m + 3) * z * p2
+    for n in range(m + 2, l + 1):
+        a = mp.sqrt(mp.mpf(4 * n * n - 1) / (n * n - m * m))
+        b = mp.sqrt(mp.mpf((n - 1) ** 2 - m * m) / (4 * (n - 1) ** 2 - 1))
+        p2, p1 = p1, a * (z * p1 - b * p2)
+    return p1
+
+
+def test_legendre_at_benchmark_degrees_vs_50_digit_values():
+    """The oracle's FP64 Legendre sums at the benchmark's nside 2048 / lmax 4096
+    against 50-digit values at the same ring heights z (one unit alm per map,
+    so F_m(ring) = lambda_lm(z_ring)).  The 50-digit recurrence agrees with
+    mpmath's hypergeometric spherical harmonics to 20 digits.  Away from the
+    poles the FP64 values are within 1e-12 of the scale sqrt((2l+1)/4pi); on
+    the two rings nearest each pole (z = 1 - 8e-8), where the recurrence at
+    l = 4096 loses more to rounding, within 1e-9."""
+    mpmath = pytest.importorskip("mpmath")
+    mpmath.mp.dps = 50
+    for ell, m, th in [(4096, 2048, 0.7), (4096, 10, 0.01)]:
+        ref = mpmath.re(mpmath.spherharm(ell, m, th, 0))
+        assert abs(_lambda_mp(ell, m, mpmath.cos(th)) - ref) < mpmath.mpf(10) ** -20
+    nside, lmax = 2048, 4096
+    z = osht.ring_info(nside)[0]
+    rings = np.array([1, 2, 64, 700, 2048, 4096, 6000, 8190], dtype=np.intc)  # 1-based ring numbers
+    pairs = [(4096, 0), (4096, 1), (4096, 2048), (4096, 4096), (3001, 1500), (100, 7)]
+    alm = np.zeros((len(pairs), osht.nalm(lmax)), complex)
+    for k, (ell, m) in enumerate(pairs):
+        alm[k, osht.alm_index(ell, m, lmax)] = 1.0
+    F = osht.alm2ring(alm, nside, lmax, rings)
+    for k, (ell, m) in enumerate(pairs):
+        scale = np.sqrt((2 * ell + 1) / (4 * np.pi))
+        for j, r in enumerate(rings):
+            ref = float(_lambda_mp(ell, m, float(z[r - 1])))
+            tol = 1e-9 if r in (1, 2, 8190) else 1e-12
+            assert abs(F[k, j, m].real - ref) < tol * scale, (ell, m, r, F[k, j, m].real, ref)
+            assert F[k, j, m].imag == 0.0
+
+
 def test_philox_known_answers():
     # Random123 Philox4x32-10 published known-answer vectors
     np.testing.assert_array_equal(orng.philox4x32_10([0, 0, 0, 0], [0, 0]),
