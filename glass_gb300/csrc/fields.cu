@@ -497,7 +497,8 @@ extern "C" int glg_iternorm(const double *cov, int64_t nrows, int64_t nl, int k,
                             uint64_t *status, void *stream) {
     GLG_REQUIRE(cov && w && status, "glg_iternorm: null pointer");
     GLG_REQUIRE(nrows >= 0 && nl >= 0, "glg_iternorm: negative size");
-    GLG_REQUIRE(k >= 0 && k <= 126, "glg_iternorm: k must be in [0, 126]");
+    // two k x k FP64 matrices and two k-vectors of one mode in shared memory: k <= 120
+    GLG_REQUIRE(k >= 0 && k <= 120, "glg_iternorm: k must be in [0, 120] (shared memory of one mode)");
     cudaStream_t st = (cudaStream_t)stream;
     cudaError_t e = cudaMemsetAsync(status, 0xff, sizeof(uint64_t), st);
     if (e != cudaSuccess) return glg_cuda_status(e, "glg_iternorm: status reset");

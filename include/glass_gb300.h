@@ -88,7 +88,8 @@ int glg_plan_info(const glg_plan *plan, int *nside, int *lmax, int *nrings, int6
  * variance becomes negative, to the first such row -- the caller then raises
  * "covariance matrix is not positive definite" (glass/fields.py:180-181).
  * Asynchronous; allocates nothing.  Bit-identical to the fixed-order
- * restatement in oracle/orc_sht.c.  Limit: k <= 126.
+ * restatement in oracle/orc_sht.c.  Limit: k <= 120 (the two k x k FP64
+ * matrices of one mode l live in one block's shared memory).
  */
 int glg_iternorm(const double *cov, int64_t nrows, int64_t nl, int k, double *w,
                  uint64_t *status, void *stream);

@@ -48,7 +48,7 @@ def test_invalid_arguments_report_errors_without_gpu():
     assert rc == _lib.GLG_ERR_INVALID
     rc = lib.glg_iternorm(ctypes.c_void_p(8), 1, 1, 200, ctypes.c_void_p(8), ctypes.c_void_p(8), None)
     assert rc == _lib.GLG_ERR_INVALID
-    assert "126" in _lib.last_error()
+    assert "120" in _lib.last_error()
     rc = lib.glg_alm2map_host(None, None, 1, None, None, None, 0, None)
     assert rc == _lib.GLG_ERR_INVALID
     assert "null plan" in _lib.last_error()
